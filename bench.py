@@ -1,0 +1,402 @@
+#!/usr/bin/env python
+"""FDK cone-beam reconstruction benchmark on GB300.
+
+Workload: 1024^3 FP32 volume from 720 x 1024^2 uint16 projections (0.15 mm
+pitch, SOD 300 mm, SDD 900 mm), log transform + Hann ramp + voxel-driven
+backprojection.  Seeded synthetic 40-ellipsoid phantom (densities
+0.1-2.0 /cm), Poisson counts at I0 = 60000.  One step = one full
+reconstruction.  Metric: GUPS (voxel-projection updates per second); the
+chosen form stores filtered projections in FP16 (FP32 math and
+accumulation), the plain form in FP32.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank reconstructs its own volume (independent
+scans, no data exchange): weak scaling, time = max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+I0 = 60000.0
+N_ELLIPSOIDS = 40
+PHANTOM_SEED = 11
+FLOPS_PER_UPDATE = 14  # z-column walk: v, floor/frac, 3 lerps, weighted accumulate
+PEAK_FP32_NOMINAL = 152 * 128 * 2 * 2.070e9 / 1e12  # TFLOP/s at the 2070 MHz max SM clock
+CPU_SAMPLE_SLICES = (508, 509, 510, 511, 512, 513, 514, 515)
+RMSE_SLICES = ((480, 512, 544), (1010,))
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-rmse", action="store_true", help="skip the FP64 oracle accuracy check")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload():
+    from tomokvas_gb300.geometry import config
+
+    return config("c2")
+
+
+def phantom(g):
+    from tomokvas_gb300.phantom import random_ellipsoids
+
+    return random_ellipsoids(N_ELLIPSOIDS, g.fov_radius_cm, g.Z * g.voxel_cm / 2, seed=PHANTOM_SEED)
+
+
+CONFIG = {
+    "workload": "fdk_1024cube_from_720x1024sq_u16",
+    "projections": [720, 1024, 1024],
+    "volume": [1024, 1024, 1024],
+    "geometry": "circular 360 deg, pitch 0.15 mm, SOD 300 mm, SDD 900 mm, voxel 0.05 mm",
+    "filter": "log + cosine weight + Hann-windowed ramp, pad 2048 (shared-memory FFT)",
+    "input": "uint16 counts, I0=60000 (resident in HBM for value; pinned host for e2e)",
+    "l2": "inputs (1.51 GB raw, 3.0 GB filtered) exceed the 129 MB L2; no flush needed",
+}
+
+
+# ------------------------------------------------------------------ helpers
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid=None):
+        self.uuid = uuid
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        rows = []
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            if self.uuid and self.uuid not in f[0]:
+                continue
+            rows.append(f)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
+
+
+def cpu_sample(g, nthreads, slices=CPU_SAMPLE_SLICES):
+    """FP32 restatement of the reference (oracle port) on sampled slices, from
+    raw uint16 projections generated on the CPU for the detector rows they need."""
+    from oracle import oracle as orc
+
+    G = orc.geom_from(g)
+    z = np.array(slices, dtype=np.int32)
+    lo, hi = orc.rows_needed(G, z)
+    band = g.replace(H=hi - lo + 1, cZ=g.cZ - lo)
+    line = orc.project_ellipsoids(phantom(g), orc.geom_from(band), "proj", nthreads)  # [N][band][W]
+    rng = np.random.default_rng(5)
+    raw = np.zeros((g.N, g.H, g.W), dtype=np.uint16)  # rows outside the band are never read
+    raw[:, lo:hi + 1] = np.clip(rng.poisson(I0 * np.exp(-line.astype(np.float64))), 0, 65535)
+    t0 = time.perf_counter()
+    orc.fdk_u16_f32_sampled(raw, G, I0, window="hann", zlist=z, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    upd = len(slices) * g.X * g.Y * g.N
+    return upd / dt / 1e9, dt, f"{len(slices)} central slices of the 1024^3 volume x 720 projections " \
+                               f"(log/weight/filter of detector rows {lo}-{hi} only)"
+
+
+def emit(obj):
+    print(json.dumps(obj), flush=True)
+
+
+# --------------------------------------------------------- reference arm
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    g = workload()
+    cores = os.cpu_count() or 1
+    vals, secs = [], []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        gups, dt, sample = cpu_sample(g, cores)
+        if i >= args.warmup:
+            vals.append(gups)
+            secs.append(dt)
+    v = statistics.mean(vals)
+    upd = g.updates
+    emit({"impl": "reference", "metric": "GUPS", "value": v, "unit": "GUPS", "n_gpus": args.gpus,
+          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
+          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+          "data": "synthetic: seeded 40-ellipsoid phantom, Poisson counts I0=60000", "config": CONFIG,
+          "s_per_volume": upd / (v * 1e9),
+          "cpu_baseline": {"value": v, "unit": "GUPS", "cores": cores, "kind": "port", "sample": sample,
+                           "what": "FP32 restatement of the reference FDK (oracle/tk_oracle.c), the reference "
+                                   "has no CPU implementation of the path"},
+          "e2e": {"value": v, "unit": "GUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    return 0
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+
+    from tomokvas_gb300 import _build, _lib, device
+    from tomokvas_gb300.fbp import FilteredBackProjection
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+        torch.cuda.set_device(0)
+    _build.build()
+    _lib.load()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    g = workload()
+    ell = phantom(g)
+    stream = torch.cuda.current_stream()
+    # synthetic raw counts, resident in HBM
+    line = device.phantom_project(g, ell, _lib.TK_LAYOUT_PROJECTION)
+    gen = torch.Generator(device="cuda").manual_seed(PHANTOM_SEED + rank)
+    counts = torch.poisson(I0 * torch.exp(-line), generator=gen).clamp_(0, 65535)
+    raw = counts.to(torch.int32).to(torch.int16)  # uint16 bits
+    del line, counts
+    ff = device.flatfield(flat_value=I0, A=1.0, B=0.0, invert=True, floor_counts=0.5)
+    vol = torch.empty((g.Z, g.Y, g.X), dtype=torch.float32, device="cuda")
+    upd = g.updates
+
+    def timed(precision, steps, warmup, sample_clocks=False):
+        q, scale = device.alloc_filtered(g, precision)
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+
+        def one(e=None):
+            if e:
+                e[0].record(stream)
+            device.filter_projections(g, raw, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff,
+                                      _lib.TK_WINDOW_HANN, precision, out=(q, scale))
+            if e:
+                e[1].record(stream)
+            device.backproject(g, q, scale if precision != _lib.TK_F32 else None, precision, vol=vol)
+            if e:
+                e[2].record(stream)
+
+        for _ in range(warmup):
+            one()
+        barrier()
+        uuid = str(getattr(torch.cuda.get_device_properties(torch.cuda.current_device()), "uuid", "") or "")
+        sampler = ClockSampler(uuid or None) if sample_clocks else None
+        if sampler:
+            sampler.start()
+            time.sleep(0.4)
+        barrier()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for i in range(steps):
+            one(ev[i])
+        t_end.record(stream)
+        barrier()
+        clocks = sampler.stop() if sampler else None
+        total_ms = t_start.elapsed_time(t_end)
+        filt = [e[0].elapsed_time(e[1]) for e in ev]
+        bp = [e[1].elapsed_time(e[2]) for e in ev]
+        total_ms = max_over_ranks(total_ms)
+        del q, scale
+        return total_ms / steps, statistics.mean(filt), statistics.mean(bp), clocks
+
+    K, W = args.steps, args.warmup
+    ms16, f16_filter, f16_bp, clocks = timed(_lib.TK_F16, K, W, sample_clocks=(rank == 0))
+    vol16 = {tuple(zs): vol[torch.tensor(zs, device="cuda")].cpu().numpy() for zs in RMSE_SLICES}
+    ms32, f32_filter, f32_bp, _ = timed(_lib.TK_F32, K, W)
+    vol32 = {tuple(zs): vol[torch.tensor(zs, device="cuda")].cpu().numpy() for zs in RMSE_SLICES}
+    value = world * upd / (ms16 * 1e-3) / 1e9
+    plain = world * upd / (ms32 * 1e-3) / 1e9
+    flags = device.device_error_flags()
+
+    # end to end through the reference-facing handle: pinned host raw in, pinned host volume out
+    e2e = None
+    if not args.no_e2e:
+        raw_h = torch.empty(raw.shape, dtype=torch.int16, pin_memory=True)
+        raw_h.copy_(raw)
+        vol_h = torch.empty((g.Z, g.Y, g.X), dtype=torch.float32, pin_memory=True)
+        del vol
+        torch.cuda.empty_cache()
+        from tomokvas_gb300.fbp import VolumeSink
+
+        zb = 128
+        sink = VolumeSink(g.X, g.Y, g.Z, zb, out=vol_h.numpy())
+        fbp = FilteredBackProjection(raise_on_error=True)
+        fbp.SetGPUid(torch.cuda.current_device())
+        fbp.SetBlockSize(zb)
+        fbp.SetSinogramProperties(None, g.W, g.cX, g.N, g.H, g.cZ, g.dfi, g.D, g.tau)
+        fbp.SetReconstructionProperties(sink, g.X, g.cx, g.Y, g.cy, g.Z, g.cz, g.rot)
+        fbp.SetScaleXYZ(g.scale)
+        fbp.SetFilter("hann")
+        fbp.SetPrecision("f16")
+        raw_np = raw_h.numpy().view(np.uint16)
+
+        def e2e_step():
+            fbp.SetProjectionsU16(raw_np, "projection", flat_value=I0)
+            fbp.Initialize()
+            fbp.CalculateReconstruction()
+
+        for _ in range(W):
+            e2e_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(K):
+            e2e_step()
+        barrier()
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / K)
+        fbp.close()
+        e2e = {"value": world * upd / e2e_s / 1e9, "unit": "GUPS", "s_per_volume": e2e_s,
+               "h2d_bytes_per_step": int(raw.numel() * 2), "d2h_bytes_per_step": int(g.X * g.Y * g.Z * 4),
+               "api": "C ABI tk_fdk_* (FilteredBackProjection mirror): u16 projections from pinned host, "
+                      "volume to pinned host via the bin_siz-style block sink, 128-slice blocks"}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    # accuracy on sampled slices vs the FP64 oracle (untimed)
+    rmse = None
+    if not args.no_rmse:
+        from oracle import oracle as orc
+
+        G = orc.geom_from(g)
+        raw_np = raw.cpu().numpy().view(np.uint16)
+        sino = orc.log_u16(raw_np, np.float32(I0))
+        num16 = num32 = den = 0.0
+        for zs in RMSE_SLICES:
+            ref = orc.fdk_f64(sino, G, "hann", np.array(zs, dtype=np.int32))
+            num16 += float(np.sum((vol16[tuple(zs)] - ref) ** 2))
+            num32 += float(np.sum((vol32[tuple(zs)] - ref) ** 2))
+            den += float(np.sum(ref ** 2))
+        del sino
+        rmse = {"chosen_f16_vs_fp64": (num16 / den) ** 0.5, "plain_f32_vs_fp64": (num32 / den) ** 0.5,
+                "slices": [z for zs in RMSE_SLICES for z in zs], "metric": "relative RMSE"}
+
+    cores = os.cpu_count() or 1
+    cpu_gups, cpu_s, sample = cpu_sample(g, cores)
+
+    bp_tflops = upd * FLOPS_PER_UPDATE / (f16_bp * 1e-3) / 1e12
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "bp_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("f16_bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    bp_bytes = g.N * g.H * g.W * 2 + g.X * g.Y * g.Z * 4  # FP16 projections read once + volume written once
+    out = {
+        "metric": "GUPS", "value": value, "unit": "GUPS", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms16, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 math, f16-stored filtered projections", "data": "synthetic: seeded 40-ellipsoid phantom, "
+        "Poisson counts I0=60000 (no dataset)", "config": CONFIG,
+        "s_per_volume": ms16 * 1e-3,
+        "plain": {"value": plain, "unit": "GUPS", "ms_per_step": ms32, "s_per_volume": ms32 * 1e-3,
+                  "dtype": "f32 math, f32-stored filtered projections", "filter_ms": f32_filter, "bp_ms": f32_bp},
+        "chosen_vs_plain": plain and value / plain,
+        "stages_ms": {"filter": f16_filter, "backprojection": f16_bp},
+        "rmse": rmse,
+        "e2e": e2e,
+        "gpu_launches": 4 * K,
+        "device_error_flags": flags,
+        "roofline": {"bound": "fp32", "kernel": "bp_tma_kernel<StoreF16,16,16,32,4>",
+                     "achieved": bp_tflops, "peak": PEAK_FP32_NOMINAL, "unit": "TFLOP/s",
+                     "frac": bp_tflops / PEAK_FP32_NOMINAL, "traffic": traffic,
+                     "flops_per_update": FLOPS_PER_UPDATE,
+                     "peak_source": "nominal FP32 CUDA-core rate 152 SM x 128 lanes x 2 x 2070 MHz; "
+                                    "MEASURED_PEAKS.json has no FP32 figure (the kernel is SM-bound, not HBM or "
+                                    "tensor)"},
+        "roofline_hbm": {"bound": "hbm", "achieved": bp_bytes / (f16_bp * 1e-3) / 1e9, "peak": hbm_peak,
+                         "unit": "GB/s", "frac": bp_bytes / (f16_bp * 1e-3) / 1e9 / hbm_peak,
+                         "note": "algorithmic bytes of the backprojection (informational)"},
+        "cpu_baseline": {"value": cpu_gups, "unit": "GUPS", "cores": cores, "kind": "port", "sample": sample,
+                         "seconds": cpu_s},
+        "clocks": clocks,
+    }
+    emit(out)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,208 @@
+/*
+ * tk_fdk.h -- C ABI of the GB300-native FDK cone-beam reconstructor.
+ *
+ * Drop-in replacement for the GPU engine of Lukas-kV/TomoKvas, class
+ * FilteredBackProjection (FBPG/kernel.cuh:82-151, FBPG/kernel.cu:219-897).
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns a tk_status; tk_last_error() holds the message of the last
+ * failure on the calling thread.  Reference citations are file:line inside
+ * the TomoKvas repository.
+ *
+ * Conventions (identical to the reference):
+ *   sinogram-major input  [H][N][W]  (row, angle, column) -- the layout
+ *       cra_con::LoadData produces (FBPG/mucat_file.cpp:244-249);
+ *   projection-major input [N][H][W] -- the detector frame order of the
+ *       .CRA raw file (FBPG/mucat_file.cpp:255-267);
+ *   volume [Z][Y][X] float32 (FBPG/kernel.cu:116-117).
+ * Filtered projections are kept on the device projection-major.
+ */
+#ifndef TK_FDK_H
+#define TK_FDK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TK_FDK_ABI_VERSION 1
+
+typedef enum tk_status {
+    TK_OK = 0,
+    TK_ERR_INVALID = 1,     /* bad argument or geometry */
+    TK_ERR_CUDA = 2,        /* CUDA runtime error (message in tk_last_error) */
+    TK_ERR_OOM = 3,         /* device or host allocation failed / over budget */
+    TK_ERR_STATE = 4,       /* call out of sequence (e.g. before initialize) */
+    TK_ERR_IO = 5,          /* file I/O failure */
+    TK_ERR_DEVICE = 6,      /* a kernel reported a failed self-check */
+    TK_ERR_UNSUPPORTED = 7  /* valid request this build does not handle */
+} tk_status;
+
+typedef enum tk_window {   /* ramp filter apodisation */
+    TK_WINDOW_RAMLAK = 0,  /* reference filter: FillFilter/RamLak, kernel.cu:783-802 */
+    TK_WINDOW_SHEPP_LOGAN = 1,
+    TK_WINDOW_HANN = 2
+} tk_window;
+
+typedef enum tk_precision {  /* storage of filtered projections; math stays FP32 */
+    TK_F32 = 0,
+    TK_F16 = 1,
+    TK_BF16 = 2
+} tk_precision;
+
+typedef enum tk_layout {
+    TK_LAYOUT_SINOGRAM = 0,   /* [H][N][W], reference SetSinogramProperties */
+    TK_LAYOUT_PROJECTION = 1  /* [N][H][W], detector frames */
+} tk_layout;
+
+typedef enum tk_input {
+    TK_INPUT_F32 = 0,  /* line integrals */
+    TK_INPUT_U16 = 1   /* raw intensities, log-transformed on the GPU */
+} tk_input;
+
+/* Reference parameter set.  Fields map one-to-one onto the arguments of
+ * SetSinogramProperties (kernel.cu:479-497), SetReconstructionProperties
+ * (kernel.cu:524-537), SetScaleXYZ (kernel.cu:308-311) and SetAxisDirection
+ * (kernel.cu:499-507). */
+typedef struct tk_geometry {
+    int W, N, H;     /* sin_X (columns), sin_Y (angles), sin_Z (rows) */
+    float cX, cZ;    /* detector centre: column of the rotation axis, row */
+    float dfi;       /* angular step (rad) */
+    float D;         /* source-axis distance in virtual pixels */
+    float tau;       /* virtual pixel pitch at the axis (cm) */
+    int X, Y, Z;     /* volume size */
+    float cx, cy, cz;/* volume centre arguments of SetReconstructionProperties */
+    float rot;       /* rotation offset (rad) */
+    float scale;     /* voxel pitch in virtual pixels */
+    int dirx, diry, dirz; /* axis flips */
+} tk_geometry;
+
+/* Flat-field + log for raw uint16 input, rsq::FlatFieldCorrection
+ * (FBPG/rsq_load.cpp:299-325):
+ *   p = A * log((I - dark) / (flat - dark)) + B,  negated when invert != 0.
+ * dark/flat are device pointers to [H][W] floats, or NULL to use the scalar.
+ * (I - dark) and (flat - dark) are floored at floor_counts (> 0). */
+typedef struct tk_flatfield {
+    const float *dark;
+    const float *flat;
+    float dark_value;
+    float flat_value;
+    float A, B;
+    int invert;
+    float floor_counts;
+} tk_flatfield;
+
+/* ---------------------------------------------------------------- misc */
+
+int tk_version(void);
+const char *tk_last_error(void);
+/* FilteredBackProjection::GetFreeMemInfo (kernel.cu:313-322). */
+size_t tk_get_free_mem_info(int gpu);
+/* Pad length of the reference FFT filter, p = 2 * nextpow2(W) (kernel.cu:570-573). */
+int tk_pad_length(int W);
+/* z offset of a whole-volume backprojection: aZ = scale * (z + zoff). */
+float tk_default_zoff(const tk_geometry *g);
+/* Per-block z offsets of the reference's Z-block schedule (kernel.cu:398-400,
+ * 821).  Writes at most cap offsets; returns the number of blocks. */
+int tk_zblock_offsets(const tk_geometry *g, int zb, float *zoff_out, int cap);
+/* Reads and (if clear) resets the device-side self-check bits of the current
+ * device.  Synchronises the device. */
+int tk_device_error_flags(unsigned *flags_out, int clear);
+
+/* ------------------------------------------- stage API (device buffers) */
+/* All pointers are device pointers; `stream` is a cudaStream_t (NULL = the
+ * legacy default stream).  Calls are asynchronous with respect to the host. */
+
+/* Preprocessing + ramp filter: fuses the uint16 log transform
+ * (rsq_load.cpp:299-325), the cosine pre-weight (RB_comma3DKernel,
+ * kernel.cu:179-201) and the row-wise ramp filter (fConvolution,
+ * kernel.cu:557-781).  Output d_q is projection-major [N][H][Wp] with row
+ * pitch Wp = (W + 7) & ~7 elements, in `precision`, equal to the reference's
+ * unnormalised C2R output times the storage scale s.  For TK_F32, s = 1 and
+ * d_q_scale may be NULL.  For 16-bit storage, s is a power of two chosen on
+ * the device from the data so that values stay well inside the format's
+ * range; it is written to the device float *d_q_scale. */
+int tk_filter_projections(const tk_geometry *g, const void *d_in, int input_type, int layout,
+                          const tk_flatfield *ff, int window, void *d_q, int precision,
+                          float *d_q_scale, void *stream);
+
+/* Voxel-driven cone-beam backprojection (FBPConeKernel + fQ3D,
+ * kernel.cu:68-177) of filtered projections d_q ([N][H][Wp] as written by
+ * tk_filter_projections, storage scale in the device float *d_q_scale, or
+ * 1 when d_q_scale is NULL) into the slab d_vol[nz][Y][X] whose slices sit
+ * at aZ = scale*(z + zoff).  accumulate != 0 adds to the slab
+ * (CollectionKernel, kernel.cu:203-215). */
+int tk_backproject(const tk_geometry *g, const void *d_q, int precision, const float *d_q_scale,
+                   int nz, float zoff, float *d_vol, int accumulate, void *stream);
+
+/* Device bytes tk_fdk_device needs as workspace (filtered projections plus
+ * a 256-byte header holding the storage scale). */
+size_t tk_fdk_workspace_bytes(const tk_geometry *g, int precision);
+
+/* Whole FDK on device buffers: filter into d_workspace, backproject into
+ * d_vol[Z][Y][X].  Allocates nothing. */
+int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_type, int layout,
+                  const tk_flatfield *ff, int window, int precision,
+                  void *d_workspace, size_t workspace_bytes, float *d_vol, void *stream);
+
+/* Analytic cone-beam line integrals of ellipsoids (seeded synthetic input).
+ * ell: host array of nell records of 16 doubles: centre[3] (cm), semi-axes[3]
+ * (cm), rotation world->local[9], density (1/cm).  Output device float
+ * array in `layout`. */
+int tk_phantom_project(const tk_geometry *g, const double *ell, int nell, int layout,
+                       float *d_out, void *stream);
+
+/* ------------------------------ FilteredBackProjection mirror (handle) */
+/* One handle = one FilteredBackProjection object (kernel.cuh:82-151).
+ * Call order as in FBPG/para_TC.cpp:130-153: setters -> initialize ->
+ * calculate_reconstruction -> destroy.  The host sinogram passed to
+ * set_sinogram_properties is borrowed until tk_fdk_initialize returns. */
+
+typedef struct tk_fdk tk_fdk;
+
+/* bin_siz::GetBlock(block, collecting) (FBPG/mucat_file.cpp:576-642): returns
+ * a host buffer of X*Y*ZB floats for Z block `block`.  When `collecting` is
+ * set the buffer already holds the partial volume of earlier angle blocks
+ * and the engine adds its result to it.  Calling the sink for block n
+ * releases the buffer of block n-1.  NULL aborts the reconstruction. */
+typedef float *(*tk_block_sink)(void *user, int block, int collecting);
+
+int tk_fdk_create(tk_fdk **out);                                   /* kernel.cu:219-253 */
+void tk_fdk_destroy(tk_fdk *h);                                    /* kernel.cu:255-281, no device reset */
+int tk_fdk_set_gpu_id(tk_fdk *h, int id);                          /* SetGPUid kernel.cu:283-286 */
+int tk_fdk_set_block_size(tk_fdk *h, int zb);                      /* SetBlockSize kernel.cu:288-291 */
+int tk_fdk_set_allocation_limit(tk_fdk *h, long long bytes);       /* SetAllocationLimit kernel.cu:303-306 */
+int tk_fdk_set_collecting(tk_fdk *h, int collecting);              /* SetCollecting kernel.cu:293-296 */
+int tk_fdk_set_show_info(tk_fdk *h, int show);                     /* SetShowInfo kernel.cu:298-301 */
+int tk_fdk_set_axis_direction(tk_fdk *h, int x, int y, int z);     /* SetAxisDirection kernel.cu:499-507 */
+int tk_fdk_set_sinogram_properties(tk_fdk *h, const float *sinogram, int W, float cX, int N, int H,
+                                   float cZ, float dfi, float D, float tau); /* kernel.cu:479-497 */
+int tk_fdk_set_reconstruction_properties(tk_fdk *h, int X, float cx, int Y, float cy, int Z, float cz,
+                                         float rot);               /* kernel.cu:524-537 */
+int tk_fdk_set_scale_xyz(tk_fdk *h, float scale);                  /* SetScaleXYZ kernel.cu:308-311 */
+/* Extensions with no reference setter. */
+int tk_fdk_set_projections_u16(tk_fdk *h, const uint16_t *raw, int layout, const float *dark_hw,
+                               const float *flat_hw, float dark_value, float flat_value, float A, float B,
+                               int invert, float floor_counts);   /* rsq_load.cpp:299-325 */
+int tk_fdk_set_input_layout(tk_fdk *h, int layout);
+int tk_fdk_set_filter(tk_fdk *h, int window);
+int tk_fdk_set_precision(tk_fdk *h, int precision);
+int tk_fdk_set_stream(tk_fdk *h, void *stream);
+/* Initialize (kernel.cu:324-428): select the device, allocate, copy the
+ * projections to the GPU, build the angle tables. */
+int tk_fdk_initialize(tk_fdk *h);
+/* CalculateReconstruction (kernel.cu:804-897): filter, then backproject Z
+ * block by Z block and hand every block to the sink, exactly following the
+ * reference's block schedule (including its last-slice quirk). */
+int tk_fdk_calculate_reconstruction(tk_fdk *h, tk_block_sink sink, void *user);
+/* Whole volume into a device buffer d_vol[Z][Y][X] (all Z slices). */
+int tk_fdk_reconstruct_device(tk_fdk *h, float *d_vol);
+/* Seconds spent in the stages of the last call (filter, backprojection,
+ * transfers), measured with CUDA events. */
+int tk_fdk_get_timings(tk_fdk *h, float *filter_ms, float *bp_ms, float *h2d_ms, float *d2h_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TK_FDK_H */

@@ -1,0 +1,258 @@
+"""GPU parity: every stage of the CUDA path against the CPU oracle.
+
+All device work goes through libtk_fdk.so's C ABI; torch only allocates
+device memory.  Tolerances (relative RMSE over the volume, max-abs relative
+to max |volume|):
+  FP32 path vs FP32 restatement of the reference   rmse <= 1e-5, max <= 1e-4
+  FP32 path vs FP64 oracle                          rmse <= 1e-5
+  FP16 storage vs FP64 oracle                       rmse <= 5e-4
+  BF16 storage vs FP64 oracle                       rmse <= 4e-3
+"""
+import numpy as np
+import pytest
+
+from _util import max_abs, rel_rmse, small_geometry
+from tomokvas_gb300 import _lib, device
+from tomokvas_gb300.fbp import FilteredBackProjection, VolumeSink
+from tomokvas_gb300.phantom import counts_u16, head_phantom, random_ellipsoids
+
+pytestmark = pytest.mark.gpu
+
+F32_RMSE, F32_MAX, F16_RMSE, BF16_RMSE = 1e-5, 1e-4, 5e-4, 4e-3
+
+
+def exact_centring(orc, g):
+    zoff = orc.zblocks(orc.geom_from(g))
+    if len(zoff) * g.zb < g.Z:
+        return False
+    z = np.arange(g.Z)
+    return bool(np.all(np.float32(z % g.zb) + zoff[z // g.zb] == np.float32(z - (g.Z - 1) / 2.0)))
+
+
+def to_dev(a, torch):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.fixture(scope="module")
+def case(orc, cuda):
+    """Small head phantom, 120 x 64^2 projections, 64^3 volume (exact Z centring)."""
+    g = small_geometry()
+    G = orc.geom_from(g)
+    ell = head_phantom(g.fov_radius_cm * 0.9, seed=1)
+    sino = orc.project_ellipsoids(ell, G, "sino")  # [H][N][W], FP64 analytic
+    return g, G, ell, sino
+
+
+def test_phantom_projector_matches_oracle(orc, cuda, case):
+    import torch
+
+    g, G, ell, sino = case
+    d = device.phantom_project(g, ell, _lib.TK_LAYOUT_SINOGRAM)
+    torch.cuda.synchronize()
+    assert rel_rmse(d.cpu().numpy(), sino) < 1e-5
+
+
+@pytest.mark.parametrize("window", ["ramlak", "shepp_logan", "hann"])
+@pytest.mark.parametrize("layout", ["sinogram", "projection"])
+def test_filter_stage_matches_oracle(orc, cuda, case, window, layout):
+    import torch
+
+    g, G, ell, sino = case
+    q_ref = orc.filter_f32(orc.weight_f32(sino, G), G, window)  # [H][N][W], reference scale
+    src = sino if layout == "sinogram" else np.transpose(sino, (1, 0, 2))
+    q, s = device.filter_projections(g, to_dev(src, torch), _lib.TK_INPUT_F32, _lib.LAYOUTS[layout],
+                                     window=_lib.WINDOWS[window])
+    torch.cuda.synchronize()
+    qd = q.cpu().numpy()[:, :, :g.W]
+    assert float(s.item()) == 1.0
+    assert rel_rmse(qd, np.transpose(q_ref, (1, 0, 2))) < 2e-6
+
+
+def test_bp_stage_matches_oracle(orc, cuda, case):
+    import torch
+
+    g, G, ell, sino = case
+    q_ref = orc.filter_f32(orc.weight_f32(sino, G), G)
+    vol_ref = orc.bp_f32(q_ref, G)
+    qp = np.zeros((g.N, g.H, device.row_pitch(g.W)), dtype=np.float32)
+    qp[:, :, :g.W] = np.transpose(q_ref, (1, 0, 2))
+    vol = device.backproject(g, to_dev(qp, torch), None)
+    torch.cuda.synchronize()
+    v = vol.cpu().numpy()
+    assert rel_rmse(v, vol_ref) < 2e-6
+    assert max_abs(v, vol_ref) < 2e-5 * np.abs(vol_ref).max()
+    assert device.device_error_flags() == 0
+
+
+def test_fdk_f32_matches_restatement_and_fp64(orc, cuda, case):
+    import torch
+
+    g, G, ell, sino = case
+    vol = device.fdk_device(g, to_dev(sino, torch))
+    torch.cuda.synchronize()
+    v = vol.cpu().numpy()
+    v32 = orc.fdk_f32(sino, G)
+    v64 = orc.fdk_f64(sino, G)
+    assert rel_rmse(v, v32) < F32_RMSE and max_abs(v, v32) < F32_MAX * np.abs(v32).max()
+    assert rel_rmse(v, v64) < F32_RMSE
+
+
+@pytest.mark.parametrize("precision,tol", [("f16", F16_RMSE), ("bf16", BF16_RMSE)])
+def test_fdk_16bit_storage_vs_fp64(orc, cuda, case, precision, tol):
+    import torch
+
+    g, G, ell, sino = case
+    vol = device.fdk_device(g, to_dev(sino, torch), precision=_lib.PRECISIONS[precision])
+    torch.cuda.synchronize()
+    v64 = orc.fdk_f64(sino, G)
+    assert rel_rmse(vol.cpu().numpy(), v64) < tol
+    assert device.device_error_flags() == 0
+
+
+@pytest.mark.parametrize("kw", [
+    dict(W=60, N=50, H=45, vol=(50, 37, 29)),                  # ragged sizes, W not a multiple of 8
+    dict(W=64, N=90, H=64, vol=(48, 48, 48), voxel_mm=1.2),   # scale 1.5
+    dict(W=64, N=72, H=70, vol=(40, 40, 40), dirx=1, diry=1, dirz=1, rot=0.3),
+    dict(W=66, N=40, H=40, vol=(32, 32, 32)),                 # W = 2 mod 4 (|FFT| filter)
+])
+def test_fdk_geometries(orc, cuda, kw):
+    import torch
+
+    g = small_geometry(**kw)
+    G = orc.geom_from(g)
+    ell = head_phantom(g.fov_radius_cm * 0.8, seed=5)
+    sino = orc.project_ellipsoids(ell, G, "sino")
+    vol = device.fdk_device(g, to_dev(sino, torch))
+    torch.cuda.synchronize()
+    v = vol.cpu().numpy()
+    v64 = orc.fdk_f64(sino, G)
+    assert rel_rmse(v, v64) < F32_RMSE
+    if exact_centring(orc, g):  # the restatement follows the reference's block schedule
+        v32 = orc.fdk_f32(sino, G)
+        assert rel_rmse(v, v32) < F32_RMSE
+
+
+def test_u16_log_path(orc, cuda, case):
+    import torch
+
+    g, G, ell, sino = case
+    raw = counts_u16(np.transpose(sino, (1, 0, 2)), 60000.0, seed=7)  # [N][H][W]
+    ff = device.flatfield(flat_value=60000.0, A=1.0, B=0.0, invert=True, floor_counts=0.5)
+    vol = device.fdk_device(g, to_dev(raw, torch), _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff,
+                            window=_lib.TK_WINDOW_HANN)
+    torch.cuda.synchronize()
+    p = orc.log_u16(raw, np.float32(60000.0))
+    v64 = orc.fdk_f64(p, G, "hann")
+    assert rel_rmse(vol.cpu().numpy(), v64) < F32_RMSE
+
+
+def test_u16_per_pixel_flat_dark(orc, cuda, case):
+    import torch
+
+    g, G, ell, sino = case
+    rng = np.random.default_rng(1)
+    flat = rng.uniform(50000, 60000, size=(g.H, g.W)).astype(np.float32)
+    dark = rng.uniform(50, 150, size=(g.H, g.W)).astype(np.float32)
+    lam = flat[None] * np.exp(-np.transpose(sino, (1, 0, 2))) + dark[None]
+    raw = np.clip(np.round(lam), 0, 65535).astype(np.uint16)
+    ff = device.flatfield(flat=to_dev(flat, torch), dark=to_dev(dark, torch), A=2.0, B=0.1, invert=True)
+    vol = device.fdk_device(g, to_dev(raw, torch), _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff)
+    torch.cuda.synchronize()
+    p = orc.log_u16(raw, flat, dark, A=2.0, B=0.1, invert=True)
+    assert rel_rmse(vol.cpu().numpy(), orc.fdk_f64(p, G)) < F32_RMSE
+
+
+def test_handle_block_schedule_matches_restatement(orc, cuda):
+    """FilteredBackProjection mirror with a bin_siz-like sink, Z=255 / ZB=30
+    (inexact reference Z centring) and the last-slice quirk case Z=33 / ZB=16."""
+    for vol_shape, zb in [((48, 48, 255), 30), ((40, 40, 33), 16)]:
+        g = small_geometry(W=64, N=60, H=300 if vol_shape[2] > 100 else 64, vol=vol_shape, zb=zb)
+        G = orc.geom_from(g)
+        ell = head_phantom(g.fov_radius_cm * 0.8, seed=2)
+        sino = orc.project_ellipsoids(ell, G, "sino")
+        out = VolumeSink(g.X, g.Y, g.Z, zb)
+        fbp = FilteredBackProjection(raise_on_error=True)
+        fbp.SetGPUid(0)
+        fbp.SetBlockSize(zb)
+        fbp.SetSinogramProperties(sino, g.W, g.cX, g.N, g.H, g.cZ, g.dfi, g.D, g.tau)
+        fbp.SetReconstructionProperties(out, g.X, g.cx, g.Y, g.cy, g.Z, g.cz, g.rot)
+        fbp.SetScaleXYZ(g.scale)
+        assert fbp.Initialize() == 0
+        assert fbp.CalculateReconstruction() == 0
+        fbp.close()
+        v32 = orc.fdk_f32(sino, G)
+        assert rel_rmse(out.volume, v32) < F32_RMSE
+        assert max_abs(out.volume, v32) < F32_MAX * np.abs(v32).max()
+        nblk = len(orc.zblocks(G))
+        assert [b for b, _ in out.blocks_requested] == list(range(nblk))
+        if (g.Z - 1) % zb == 0:
+            assert np.all(out.volume[-1] == 0)
+
+
+def test_collecting_angle_blocks_sum_to_full(orc, cuda, case):
+    """Angle sub-blocks accumulated through the sink (para_TC.cpp:117-155)."""
+    g, G, ell, sino = case
+    n1 = g.N // 2
+    out = VolumeSink(g.X, g.Y, g.Z, g.zb)
+    for k, (b0, b1) in enumerate([(0, n1), (n1, g.N)]):
+        part = np.ascontiguousarray(sino[:, b0:b1])
+        fbp = FilteredBackProjection(raise_on_error=True)
+        fbp.SetBlockSize(g.zb)
+        fbp.SetCollecting(k > 0)
+        fbp.SetSinogramProperties(part, g.W, g.cX, b1 - b0, g.H, g.cZ, g.dfi, g.D, g.tau)
+        fbp.SetReconstructionProperties(out, g.X, g.cx, g.Y, g.cy, g.Z, g.cz, float(np.float32(b0 * g.dfi)))
+        fbp.Initialize()
+        fbp.CalculateReconstruction()
+        fbp.close()
+    full = orc.fdk_f64(sino, G)
+    assert rel_rmse(out.volume, full) < F32_RMSE
+
+
+def test_reconstruct_to_device_and_precisions(orc, cuda, case):
+    import torch
+
+    g, G, ell, sino = case
+    v64 = orc.fdk_f64(sino, G)
+    for prec, tol in [("f32", F32_RMSE), ("f16", F16_RMSE)]:
+        fbp = FilteredBackProjection(raise_on_error=True)
+        fbp.SetSinogramProperties(sino, g.W, g.cX, g.N, g.H, g.cZ, g.dfi, g.D, g.tau)
+        fbp.SetReconstructionProperties(None, g.X, g.cx, g.Y, g.cy, g.Z, g.cz, g.rot)
+        fbp.SetPrecision(prec)
+        fbp.Initialize()
+        vol = torch.empty((g.Z, g.Y, g.X), dtype=torch.float32, device="cuda")
+        fbp.ReconstructToDevice(vol.data_ptr())
+        t = fbp.Timings()
+        fbp.close()
+        assert rel_rmse(vol.cpu().numpy(), v64) < tol
+        assert t["bp_ms"] > 0 and t["filter_ms"] > 0
+
+
+def test_full_size_1024_sampled_slices(orc, cuda):
+    """The 720 x 1024^2 uint16 workload at full size: GPU vs FP64 oracle on
+    sampled slices (the oracle filters only the detector rows they need)."""
+    import torch
+    from tomokvas_gb300.geometry import config
+
+    g = config("c2")
+    G = orc.geom_from(g)
+    ell = random_ellipsoids(40, g.fov_radius_cm, g.Z * g.voxel_cm / 2, seed=11)
+    line = device.phantom_project(g, ell, _lib.TK_LAYOUT_PROJECTION)  # [N][H][W]
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    counts = torch.poisson(60000.0 * torch.exp(-line), generator=gen).clamp_(0, 65535)
+    raw = counts.to(torch.int32).to(torch.int16)  # the bits of uint16 counts
+    del line, counts
+    ff = device.flatfield(flat_value=60000.0)
+    raw_h = raw.cpu().numpy().view(np.uint16)
+    sino = orc.log_u16(raw_h, np.float32(60000.0))  # [H][N][W]
+    groups = [np.array([480, 512, 544], dtype=np.int32), np.array([1010], dtype=np.int32)]
+    refs = [orc.fdk_f64(sino, G, "hann", zs) for zs in groups]  # one narrow row band each
+    del sino
+    for prec, tol in [(_lib.TK_F32, F32_RMSE), (_lib.TK_F16, F16_RMSE)]:
+        vol = device.fdk_device(g, raw, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff,
+                                window=_lib.TK_WINDOW_HANN, precision=prec)
+        torch.cuda.synchronize()
+        for zs, ref in zip(groups, refs):
+            v = vol[torch.from_numpy(zs).long().cuda()].cpu().numpy()
+            assert rel_rmse(v, ref) < tol, (prec, zs)
+        del vol
+    assert device.device_error_flags() == 0

@@ -1,0 +1,612 @@
+// tk_capi.cu -- C ABI of the GB300 FDK engine (include/tk_fdk.h).
+//
+// Stage entry points (device buffers, caller's stream), the whole-FDK device
+// entry point, and the handle that mirrors FilteredBackProjection
+// (Lukas-kV/TomoKvas FBPG/kernel.cuh:82-151, FBPG/kernel.cu:219-897).
+#include "tk_common.cuh"
+#include "tk_internal.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace tk {
+
+// ---------------------------------------------------------------- errors
+static thread_local char g_err[1024] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    return e == cudaErrorMemoryAllocation ? TK_ERR_OOM : TK_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------- geometry
+int reference_pad_length(int W)
+{
+    int p = 2;
+    while (p < W) p *= 2;  // kernel.cu:570-573
+    return p * 2;
+}
+
+int validate_geometry(const tk_geometry *g)
+{
+    TK_CHECK(g, TK_ERR_INVALID, "geometry is NULL");
+    TK_CHECK(g->W > 0 && g->N > 0 && g->H > 0, TK_ERR_INVALID, "sinogram size %dx%dx%d invalid", g->W, g->N,
+             g->H);
+    TK_CHECK(g->X > 0 && g->Y > 0 && g->Z >= 0, TK_ERR_INVALID, "volume size %dx%dx%d invalid", g->X, g->Y, g->Z);
+    TK_CHECK(std::isfinite(g->D) && g->D > 0.f, TK_ERR_INVALID, "distance D must be > 0");
+    TK_CHECK(std::isfinite(g->tau) && g->tau > 0.f, TK_ERR_INVALID, "sampling tau must be > 0");
+    TK_CHECK(std::isfinite(g->scale) && g->scale != 0.f, TK_ERR_INVALID, "scale must be finite and non-zero");
+    TK_CHECK(std::isfinite(g->dfi) && std::isfinite(g->rot) && std::isfinite(g->cX) && std::isfinite(g->cZ) &&
+                 std::isfinite(g->cx) && std::isfinite(g->cy) && std::isfinite(g->cz),
+             TK_ERR_INVALID, "non-finite geometry parameter");
+    TK_CHECK(g->W <= 4096 && g->H <= 65535 && g->N <= (1 << 20), TK_ERR_UNSUPPORTED,
+             "sinogram %dx%dx%d beyond supported limits (W<=4096, H<=65535)", g->W, g->N, g->H);
+    return TK_OK;
+}
+
+// CalcSinCos (kernel.cu:430-441): beta_rad = beta * delta_f + rot is formed
+// in float, sin/cos are taken in double and stored as float.
+void build_trig(const tk_geometry &g, float *cos_out, float *sin_out)
+{
+    for (int b = 0; b < g.N; ++b) {
+        const float bf = (float)b * g.dfi;
+        const double beta_rad = (double)(float)(bf + g.rot);
+        cos_out[b] = (float)std::cos(beta_rad);
+        sin_out[b] = (float)std::sin(beta_rad);
+    }
+}
+
+// ------------------------------------------------------- device error word
+__device__ unsigned g_device_err;
+
+unsigned *device_error_word()
+{
+    static unsigned *addr[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!addr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_device_err) != cudaSuccess) return nullptr;
+        addr[dev] = static_cast<unsigned *>(p);
+    }
+    return addr[dev];
+}
+
+}  // namespace tk
+
+using namespace tk;
+
+// ======================================================================== misc
+extern "C" int tk_version(void) { return TK_FDK_ABI_VERSION; }
+
+extern "C" const char *tk_last_error(void) { return tk::g_err; }
+
+extern "C" size_t tk_get_free_mem_info(int gpu)
+{
+    int prev = 0;
+    if (cudaGetDevice(&prev) != cudaSuccess) return 0;
+    if (cudaSetDevice(gpu) != cudaSuccess) return 0;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) fr = 0;
+    cudaSetDevice(prev);
+    return fr;
+}
+
+extern "C" int tk_pad_length(int W) { return W > 0 ? reference_pad_length(W) : -1; }
+
+extern "C" float tk_default_zoff(const tk_geometry *g)
+{
+    return g ? (float)(-((double)g->Z - 1.0) / 2.0 - (double)g->cz) : 0.f;
+}
+
+// kernel.cu:398-400 and 821: nr_Z = (Z-1)/ZB in float, ceil, dcorZ, and
+// recn.dZ = dZ + (n - nr_blocks/2.)*ZB + dcorZ with dZ = -centre_Z.
+extern "C" int tk_zblock_offsets(const tk_geometry *g, int zb, float *zoff_out, int cap)
+{
+    if (!g || zb <= 0) {
+        set_error("zblock offsets: bad arguments");
+        return -TK_ERR_INVALID;
+    }
+    const float nr_Z = (float)(g->Z - 1) / (float)zb;
+    const int nblk = (int)std::ceil(nr_Z);
+    const float dcorZ = (nblk - nr_Z) * zb / 2;
+    const float dZ = -g->cz;
+    for (int n = 0; n < nblk && n < cap && zoff_out; ++n)
+        zoff_out[n] = (float)((double)dZ + (n - (float)nblk / 2.) * zb + (double)dcorZ);
+    return nblk < 0 ? 0 : nblk;
+}
+
+extern "C" int tk_device_error_flags(unsigned *flags_out, int clear)
+{
+    unsigned *w = device_error_word();
+    TK_CHECK(w, TK_ERR_CUDA, "device error word unavailable");
+    TK_CUDA(cudaDeviceSynchronize());
+    unsigned v = 0;
+    TK_CUDA(cudaMemcpy(&v, w, sizeof(v), cudaMemcpyDeviceToHost));
+    if (clear) TK_CUDA(cudaMemset(w, 0, sizeof(unsigned)));
+    if (flags_out) *flags_out = v;
+    return TK_OK;
+}
+
+// ================================================================== stage API
+extern "C" int tk_filter_projections(const tk_geometry *g, const void *d_in, int input_type, int layout,
+                                     const tk_flatfield *ff, int window, void *d_q, int precision, float *d_q_scale,
+                                     void *stream)
+{
+    if (int rc = validate_geometry(g)) return rc;
+    return launch_filter(*g, d_in, input_type, layout, ff, window, d_q, precision, d_q_scale,
+                         static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tk_backproject(const tk_geometry *g, const void *d_q, int precision, const float *d_q_scale, int nz,
+                              float zoff, float *d_vol, int accumulate, void *stream)
+{
+    if (int rc = validate_geometry(g)) return rc;
+    return launch_backproject(*g, d_q, precision, d_q_scale, nz, zoff, d_vol, accumulate,
+                              static_cast<cudaStream_t>(stream));
+}
+
+static constexpr size_t kWsHeader = 256;
+
+extern "C" size_t tk_fdk_workspace_bytes(const tk_geometry *g, int precision)
+{
+    if (!g || precision < TK_F32 || precision > TK_BF16) return 0;
+    return kWsHeader + filtered_bytes(*g, precision);
+}
+
+extern "C" int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_type, int layout,
+                             const tk_flatfield *ff, int window, int precision, void *d_workspace,
+                             size_t workspace_bytes, float *d_vol, void *stream)
+{
+    if (int rc = validate_geometry(g)) return rc;
+    TK_CHECK(precision >= TK_F32 && precision <= TK_BF16, TK_ERR_INVALID, "bad precision %d", precision);
+    const size_t need = tk_fdk_workspace_bytes(g, precision);
+    TK_CHECK(d_workspace && workspace_bytes >= need, TK_ERR_INVALID, "workspace of %zu B needed, %zu given", need,
+             workspace_bytes);
+    TK_CHECK((reinterpret_cast<uintptr_t>(d_workspace) & 255) == 0, TK_ERR_INVALID,
+             "workspace must be 256-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float *d_scale = static_cast<float *>(d_workspace);
+    void *d_q = static_cast<char *>(d_workspace) + kWsHeader;
+    if (int rc = launch_filter(*g, d_in, input_type, layout, ff, window, d_q, precision, d_scale, st)) return rc;
+    return launch_backproject(*g, d_q, precision, d_scale, g->Z, tk_default_zoff(g), d_vol, 0, st);
+}
+
+extern "C" int tk_phantom_project(const tk_geometry *g, const double *ell, int nell, int layout, float *d_out,
+                                  void *stream)
+{
+    TK_CHECK(g, TK_ERR_INVALID, "geometry is NULL");
+    return launch_phantom(*g, ell, nell, layout, d_out, static_cast<cudaStream_t>(stream));
+}
+
+// ======================================================= handle (engine object)
+struct tk_fdk {
+    int dev = 0;
+    int zb = 16;                                 // size_of_Z_block default (kernel.cu:243)
+    long long alloc_limit = 1024ll * 1024 * 1024; // memory_limit default (kernel.cu:244)
+    int collecting = 0;
+    int show = 0;
+    tk_geometry g{};
+    bool have_sino = false, have_rec = false;
+    const void *host_in = nullptr;
+    int input_type = TK_INPUT_F32;
+    int layout = TK_LAYOUT_SINOGRAM;
+    const float *host_dark = nullptr, *host_flat = nullptr;
+    tk_flatfield ff{};
+    int window = TK_WINDOW_RAMLAK;
+    int precision = TK_F32;
+    cudaStream_t stream = nullptr, copy_stream = nullptr;
+    bool own_stream = false;
+    // device state
+    void *d_in = nullptr;
+    size_t d_in_cap = 0;
+    void *d_ws = nullptr;  // [header | filtered projections]
+    size_t d_ws_cap = 0;
+    float *d_dark = nullptr, *d_flat = nullptr;
+    size_t dfl_cap = 0;
+    float *d_block[2] = {nullptr, nullptr};
+    size_t block_cap = 0;
+    bool initialized = false, filtered = false;
+    cudaEvent_t ev[8] = {};
+    float t_filter = 0, t_bp = 0, t_h2d = 0, t_d2h = 0;
+};
+
+static void release_device(tk_fdk *h)
+{
+    cudaFree(h->d_in);
+    cudaFree(h->d_ws);
+    cudaFree(h->d_dark);
+    cudaFree(h->d_flat);
+    cudaFree(h->d_block[0]);
+    cudaFree(h->d_block[1]);
+    h->d_in = h->d_ws = nullptr;
+    h->d_dark = h->d_flat = nullptr;
+    h->d_block[0] = h->d_block[1] = nullptr;
+    h->d_in_cap = h->d_ws_cap = h->dfl_cap = h->block_cap = 0;
+}
+
+static int ensure(void **p, size_t *cap, size_t need)
+{
+    if (*cap >= need && *p) return TK_OK;
+    cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    TK_CUDA(cudaMalloc(p, need));
+    *cap = need;
+    return TK_OK;
+}
+
+extern "C" int tk_fdk_create(tk_fdk **out)
+{
+    TK_CHECK(out, TK_ERR_INVALID, "create: out is NULL");
+    *out = new (std::nothrow) tk_fdk();
+    TK_CHECK(*out, TK_ERR_OOM, "create: out of host memory");
+    return TK_OK;
+}
+
+extern "C" void tk_fdk_destroy(tk_fdk *h)
+{
+    if (!h) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    if (h->initialized || h->stream || h->d_ws) {
+        cudaSetDevice(h->dev);
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+        release_device(h);
+        for (auto &e : h->ev)
+            if (e) cudaEventDestroy(e);
+        if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+        if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+        cudaSetDevice(prev);
+    }
+    delete h;
+}
+
+#define TK_H(h) TK_CHECK(h, TK_ERR_INVALID, "handle is NULL")
+
+extern "C" int tk_fdk_set_gpu_id(tk_fdk *h, int id)
+{
+    TK_H(h);
+    TK_CHECK(!h->initialized, TK_ERR_STATE, "set_gpu_id after initialize");
+    h->dev = id;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_block_size(tk_fdk *h, int zb)
+{
+    TK_H(h);
+    TK_CHECK(zb > 0, TK_ERR_INVALID, "block size must be > 0");
+    h->zb = zb;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_allocation_limit(tk_fdk *h, long long bytes)
+{
+    TK_H(h);
+    TK_CHECK(bytes > 0, TK_ERR_INVALID, "allocation limit must be > 0");
+    h->alloc_limit = bytes;  // recorded; the engine keeps each array in one allocation
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_collecting(tk_fdk *h, int collecting)
+{
+    TK_H(h);
+    h->collecting = collecting ? 1 : 0;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_show_info(tk_fdk *h, int show)
+{
+    TK_H(h);
+    h->show = show ? 1 : 0;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_axis_direction(tk_fdk *h, int x, int y, int z)
+{
+    TK_H(h);
+    // SetAxisDirection only ever sets the masks (kernel.cu:499-507)
+    if (x) h->g.dirx = 1;
+    if (y) h->g.diry = 1;
+    if (z) h->g.dirz = 1;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_sinogram_properties(tk_fdk *h, const float *sinogram, int W, float cX, int N, int H,
+                                              float cZ, float dfi, float D, float tau)
+{
+    TK_H(h);
+    h->host_in = sinogram;
+    h->input_type = TK_INPUT_F32;
+    h->g.W = W;
+    h->g.cX = cX;
+    h->g.N = N;
+    h->g.H = H;
+    h->g.cZ = cZ;
+    h->g.dfi = dfi;
+    h->g.D = D;
+    h->g.tau = tau;
+    h->have_sino = true;
+    h->filtered = false;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_reconstruction_properties(tk_fdk *h, int X, float cx, int Y, float cy, int Z, float cz,
+                                                    float rot)
+{
+    TK_H(h);
+    h->g.X = X;
+    h->g.cx = cx;
+    h->g.Y = Y;
+    h->g.cy = cy;
+    h->g.Z = Z;
+    h->g.cz = cz;
+    h->g.rot = rot;
+    if (h->g.scale == 0.f) h->g.scale = 1.f;  // recn.scale default (kernel.cu:237)
+    h->have_rec = true;
+    h->filtered = false;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_scale_xyz(tk_fdk *h, float scale)
+{
+    TK_H(h);
+    h->g.scale = scale;
+    h->filtered = false;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_projections_u16(tk_fdk *h, const uint16_t *raw, int layout, const float *dark_hw,
+                                          const float *flat_hw, float dark_value, float flat_value, float A, float B,
+                                          int invert, float floor_counts)
+{
+    TK_H(h);
+    TK_CHECK(layout == TK_LAYOUT_SINOGRAM || layout == TK_LAYOUT_PROJECTION, TK_ERR_INVALID, "bad layout");
+    TK_CHECK(floor_counts > 0.f, TK_ERR_INVALID, "floor_counts must be > 0");
+    TK_CHECK(flat_hw || flat_value > 0.f, TK_ERR_INVALID, "flat field missing");
+    h->host_in = raw;
+    h->input_type = TK_INPUT_U16;
+    h->layout = layout;
+    h->host_dark = dark_hw;
+    h->host_flat = flat_hw;
+    h->ff.dark_value = dark_value;
+    h->ff.flat_value = flat_value;
+    h->ff.A = A;
+    h->ff.B = B;
+    h->ff.invert = invert ? 1 : 0;
+    h->ff.floor_counts = floor_counts;
+    h->filtered = false;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_input_layout(tk_fdk *h, int layout)
+{
+    TK_H(h);
+    TK_CHECK(layout == TK_LAYOUT_SINOGRAM || layout == TK_LAYOUT_PROJECTION, TK_ERR_INVALID, "bad layout");
+    h->layout = layout;
+    h->filtered = false;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_filter(tk_fdk *h, int window)
+{
+    TK_H(h);
+    TK_CHECK(window >= TK_WINDOW_RAMLAK && window <= TK_WINDOW_HANN, TK_ERR_INVALID, "bad window %d", window);
+    h->window = window;
+    h->filtered = false;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_precision(tk_fdk *h, int precision)
+{
+    TK_H(h);
+    TK_CHECK(precision >= TK_F32 && precision <= TK_BF16, TK_ERR_INVALID, "bad precision %d", precision);
+    h->precision = precision;
+    h->filtered = false;
+    return TK_OK;
+}
+extern "C" int tk_fdk_set_stream(tk_fdk *h, void *stream)
+{
+    TK_H(h);
+    TK_CHECK(!h->initialized, TK_ERR_STATE, "set_stream after initialize");
+    h->stream = static_cast<cudaStream_t>(stream);
+    h->own_stream = false;
+    return TK_OK;
+}
+
+static int elapsed(cudaEvent_t a, cudaEvent_t b, float *acc)
+{
+    float ms = 0;
+    TK_CUDA(cudaEventElapsedTime(&ms, a, b));
+    *acc += ms;
+    return TK_OK;
+}
+
+// Initialize (kernel.cu:324-428): device, allocations, host->device copy.
+extern "C" int tk_fdk_initialize(tk_fdk *h)
+{
+    TK_H(h);
+    TK_CHECK(h->have_sino && h->have_rec, TK_ERR_STATE,
+             "initialize before set_sinogram_properties / set_reconstruction_properties");
+    if (int rc = validate_geometry(&h->g)) return rc;
+    TK_CHECK(h->host_in, TK_ERR_INVALID, "initialize: no projection data");
+    TK_CUDA(cudaSetDevice(h->dev));
+    if (!h->stream) {
+        TK_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    if (!h->copy_stream) TK_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    for (auto &e : h->ev)
+        if (!e) TK_CUDA(cudaEventCreate(&e));
+    const tk_geometry &g = h->g;
+    const size_t n = (size_t)g.W * g.N * g.H;
+    const size_t in_bytes = n * (h->input_type == TK_INPUT_U16 ? 2 : 4);
+    if (int rc = ensure(&h->d_in, &h->d_in_cap, in_bytes)) return rc;
+    if (int rc = ensure(&h->d_ws, &h->d_ws_cap, tk_fdk_workspace_bytes(&g, h->precision))) return rc;
+    h->t_h2d = h->t_filter = h->t_bp = h->t_d2h = 0;
+    TK_CUDA(cudaEventRecord(h->ev[0], h->stream));
+    TK_CUDA(cudaMemcpyAsync(h->d_in, h->host_in, in_bytes, cudaMemcpyHostToDevice, h->stream));
+    if (h->input_type == TK_INPUT_U16) {
+        const size_t fb = (size_t)g.W * g.H * sizeof(float);
+        if (h->host_dark || h->host_flat) {
+            void *pd = h->d_dark, *pf = h->d_flat;
+            size_t cap = h->dfl_cap;
+            if (cap < fb) {
+                cudaFree(pd);
+                cudaFree(pf);
+                pd = pf = nullptr;
+                TK_CUDA(cudaMalloc(&pd, fb));
+                TK_CUDA(cudaMalloc(&pf, fb));
+                cap = fb;
+            }
+            h->d_dark = static_cast<float *>(pd);
+            h->d_flat = static_cast<float *>(pf);
+            h->dfl_cap = cap;
+        }
+        h->ff.dark = nullptr;
+        h->ff.flat = nullptr;
+        if (h->host_dark) {
+            TK_CUDA(cudaMemcpyAsync(h->d_dark, h->host_dark, fb, cudaMemcpyHostToDevice, h->stream));
+            h->ff.dark = h->d_dark;
+        }
+        if (h->host_flat) {
+            TK_CUDA(cudaMemcpyAsync(h->d_flat, h->host_flat, fb, cudaMemcpyHostToDevice, h->stream));
+            h->ff.flat = h->d_flat;
+        }
+    }
+    TK_CUDA(cudaEventRecord(h->ev[1], h->stream));
+    TK_CUDA(cudaStreamSynchronize(h->stream));  // the host buffer is only borrowed until we return
+    if (int rc = elapsed(h->ev[0], h->ev[1], &h->t_h2d)) return rc;
+    h->initialized = true;
+    h->filtered = false;
+    if (h->show) fprintf(stdout, "tk_fdk: %zu MiB of projections on GPU %d\n", in_bytes >> 20, h->dev);
+    return TK_OK;
+}
+
+static int run_filter(tk_fdk *h)
+{
+    if (h->filtered) return TK_OK;
+    float *d_scale = static_cast<float *>(h->d_ws);
+    void *d_q = static_cast<char *>(h->d_ws) + kWsHeader;
+    TK_CUDA(cudaEventRecord(h->ev[2], h->stream));
+    if (int rc = launch_filter(h->g, h->d_in, h->input_type, h->layout, &h->ff, h->window, d_q, h->precision, d_scale,
+                               h->stream))
+        return rc;
+    TK_CUDA(cudaEventRecord(h->ev[3], h->stream));
+    h->filtered = true;
+    return TK_OK;
+}
+
+static int check_device_flags(cudaStream_t st)
+{
+    unsigned *w = device_error_word();
+    TK_CHECK(w, TK_ERR_CUDA, "device error word unavailable");
+    unsigned v = 0;
+    TK_CUDA(cudaMemcpyAsync(&v, w, sizeof(v), cudaMemcpyDeviceToHost, st));
+    TK_CUDA(cudaStreamSynchronize(st));
+    if (v) {
+        cudaMemsetAsync(w, 0, sizeof(unsigned), st);
+        cudaStreamSynchronize(st);
+        set_error("kernel self-check failed (flags 0x%x)", v);
+        return TK_ERR_DEVICE;
+    }
+    return TK_OK;
+}
+
+// CalculateReconstruction (kernel.cu:804-897).
+extern "C" int tk_fdk_calculate_reconstruction(tk_fdk *h, tk_block_sink sink, void *user)
+{
+    TK_H(h);
+    TK_CHECK(h->initialized, TK_ERR_STATE, "calculate_reconstruction before initialize");
+    TK_CHECK(sink, TK_ERR_INVALID, "calculate_reconstruction: sink is NULL");
+    TK_CUDA(cudaSetDevice(h->dev));
+    const tk_geometry &g = h->g;
+    const int zb = h->zb;
+    const int nblk = tk_zblock_offsets(&g, zb, nullptr, 0);
+    std::vector<float> zoff((size_t)std::max(nblk, 1));
+    tk_zblock_offsets(&g, zb, zoff.data(), nblk);
+    const size_t slab = (size_t)g.X * g.Y;
+    const size_t block_bytes = slab * zb * sizeof(float);
+    if (h->block_cap < block_bytes || !h->d_block[0]) {
+        cudaFree(h->d_block[0]);
+        cudaFree(h->d_block[1]);
+        h->d_block[0] = h->d_block[1] = nullptr;
+        h->block_cap = 0;
+        TK_CUDA(cudaMalloc(&h->d_block[0], block_bytes));
+        TK_CUDA(cudaMalloc(&h->d_block[1], block_bytes));
+        h->block_cap = block_bytes;
+    }
+    if (int rc = run_filter(h)) return rc;
+    const float *d_scale = static_cast<const float *>(h->d_ws);
+    const void *d_q = static_cast<const char *>(h->d_ws) + kWsHeader;
+    cudaEvent_t bp_done[2] = {h->ev[4], h->ev[5]};
+    cudaEvent_t d2h_done[2] = {h->ev[6], h->ev[7]};
+    float *prev_host = nullptr;
+    for (int n = 0; n < nblk; ++n) {
+        const int k = n & 1;
+        // slices delivered for this block (kernel.cu:838-840)
+        int slices = zb;
+        if ((long long)(n + 1) * zb > g.Z) slices = g.Z - n * zb;
+        if (n >= 2) TK_CUDA(cudaStreamWaitEvent(h->stream, d2h_done[k], 0));  // block buffer k is free again
+        if (!h->collecting) {
+            if (int rc = launch_backproject(g, d_q, h->precision, d_scale, slices, zoff[n], h->d_block[k], 0,
+                                            h->stream))
+                return rc;
+            TK_CUDA(cudaEventRecord(bp_done[k], h->stream));
+        }
+        if (prev_host) TK_CUDA(cudaEventSynchronize(d2h_done[k ^ 1]));  // block n-1 has landed
+        float *host = sink(user, n, h->collecting);
+        TK_CHECK(host, TK_ERR_IO, "block sink returned NULL for block %d", n);
+        const size_t bytes = slab * (size_t)slices * sizeof(float);
+        if (h->collecting) {
+            // previous partial volume -> device, then vol = new + previous (kernel.cu:849-876)
+            TK_CUDA(cudaMemcpyAsync(h->d_block[k], host, bytes, cudaMemcpyHostToDevice, h->stream));
+            if (int rc = launch_backproject(g, d_q, h->precision, d_scale, slices, zoff[n], h->d_block[k], 1,
+                                            h->stream))
+                return rc;
+            TK_CUDA(cudaEventRecord(bp_done[k], h->stream));
+        }
+        TK_CUDA(cudaStreamWaitEvent(h->copy_stream, bp_done[k], 0));
+        TK_CUDA(cudaMemcpyAsync(host, h->d_block[k], bytes, cudaMemcpyDeviceToHost, h->copy_stream));
+        TK_CUDA(cudaEventRecord(d2h_done[k], h->copy_stream));
+        prev_host = host;
+    }
+    TK_CUDA(cudaStreamSynchronize(h->copy_stream));
+    TK_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->filtered) elapsed(h->ev[2], h->ev[3], &h->t_filter);
+    return check_device_flags(h->stream);
+}
+
+extern "C" int tk_fdk_reconstruct_device(tk_fdk *h, float *d_vol)
+{
+    TK_H(h);
+    TK_CHECK(h->initialized, TK_ERR_STATE, "reconstruct_device before initialize");
+    TK_CHECK(d_vol, TK_ERR_INVALID, "reconstruct_device: d_vol is NULL");
+    TK_CUDA(cudaSetDevice(h->dev));
+    const bool was = h->filtered;
+    if (int rc = run_filter(h)) return rc;
+    const float *d_scale = static_cast<const float *>(h->d_ws);
+    const void *d_q = static_cast<const char *>(h->d_ws) + kWsHeader;
+    TK_CUDA(cudaEventRecord(h->ev[4], h->stream));
+    if (int rc = launch_backproject(h->g, d_q, h->precision, d_scale, h->g.Z, tk_default_zoff(&h->g), d_vol, 0,
+                                    h->stream))
+        return rc;
+    TK_CUDA(cudaEventRecord(h->ev[5], h->stream));
+    TK_CUDA(cudaStreamSynchronize(h->stream));
+    if (!was) elapsed(h->ev[2], h->ev[3], &h->t_filter);
+    elapsed(h->ev[4], h->ev[5], &h->t_bp);
+    return check_device_flags(h->stream);
+}
+
+extern "C" int tk_fdk_get_timings(tk_fdk *h, float *filter_ms, float *bp_ms, float *h2d_ms, float *d2h_ms)
+{
+    TK_H(h);
+    if (filter_ms) *filter_ms = h->t_filter;
+    if (bp_ms) *bp_ms = h->t_bp;
+    if (h2d_ms) *h2d_ms = h->t_h2d;
+    if (d2h_ms) *d2h_ms = h->t_d2h;
+    return TK_OK;
+}

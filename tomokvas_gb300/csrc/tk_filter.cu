@@ -1,0 +1,424 @@
+// tk_filter.cu -- fused preprocessing + ramp filter for GB300 (sm_103a).
+//
+// Replaces three stages of the reference FDK (Lukas-kV/TomoKvas):
+//   * raw uint16 -> line integral, rsq::FlatFieldCorrection (FBPG/rsq_load.cpp:299-325);
+//   * cosine pre-weight, RB_comma3DKernel (FBPG/kernel.cu:179-201);
+//   * row-wise ramp filter, fConvolution (FBPG/kernel.cu:557-781): per detector
+//     row, zero-pad to p = 2*nextpow2(W), R2C, multiply by tau*|R2C(h)|, C2R
+//     unnormalised.
+//
+// GB300 design: one pass over HBM.  Each CTA streams pairs of detector rows
+// straight from the raw input, applies log + cosine weight while loading,
+// packs the two real rows as one complex signal z = a + i b, and runs a
+// radix-4/2 Stockham FFT in shared memory.  Because the filter spectrum is
+// real and even, IFFT(FFT(z) * Hf) = (a*k) + i (b*k), so one forward and one
+// inverse complex FFT filter two rows.  The inverse is computed as
+// conj(FFT(conj(Z) * Hf)).  Results are written once, projection-major, in
+// FP32/FP16/BF16.  No cuFFT, no staging copies, no per-row plans.
+#include "tk_common.cuh"
+#include "tk_internal.h"
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+namespace tk {
+
+constexpr int kMaxHf = 4097;  // p/2 + 1 for p <= 8192
+constexpr int kFiltThreads = 256;
+constexpr float kScaleTarget = 16384.f;  // bound of |stored value| for 16-bit storage
+
+struct LoadParams {
+    const void *in;
+    const float *dark, *flat;
+    float dark_v, flat_v, A, B, floor_counts;
+    int invert;
+    int W, N, H, layout, input_type;
+    float cX, cZ, D;
+};
+
+struct FiltParams {
+    LoadParams L;
+    void *out;
+    const float *q_scale;  // device storage scale (16-bit) or null (= 1)
+    long long nrows, npairs;
+    int Wp, p, lg, precision;
+    float Hf[kMaxHf];  // tau * |R2C_p(h)| * window, k = 0..p/2
+};
+
+// Element offset of the first sample of output row `row` (= b*H + r) in the input.
+__device__ __forceinline__ long long in_row_offset(const LoadParams &L, long long row, int &r)
+{
+    const long long b = row / L.H;
+    r = (int)(row - b * L.H);
+    return L.layout == TK_LAYOUT_SINOGRAM ? ((long long)r * L.N + b) * L.W : row * (long long)L.W;
+}
+
+// Preprocessed (log if raw, cosine weighted) sample x of a row.
+__device__ __forceinline__ float load_pre(const LoadParams &L, long long off, int r, int x)
+{
+    float val;
+    if (L.input_type == TK_INPUT_U16) {
+        const float I = (float)static_cast<const uint16_t *>(L.in)[off + x];
+        const size_t px = (size_t)r * L.W + x;
+        const float dk = L.dark ? L.dark[px] : L.dark_v;
+        const float fl = L.flat ? L.flat[px] : L.flat_v;
+        const float num = fmaxf(I - dk, L.floor_counts);
+        const float den = fmaxf(fl - dk, L.floor_counts);
+        val = L.A * logf(num / den) + L.B;
+        if (L.invert) val = -val;
+    } else {
+        val = static_cast<const float *>(L.in)[off + x];
+    }
+    // row[x] *= distance / sqrt(ce*ce + distance*distance + cs*cs)  (kernel.cu:195-199)
+    const float ce = (float)x - L.cX;
+    const float cs = (float)r - L.cZ;
+    return val * (L.D / sqrtf(ce * ce + L.D * L.D + cs * cs));
+}
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// One radix-4 Stockham pass (decimation in time, twiddle before butterfly):
+//   v[r] = x[j + r p/4] * w^(k r p/(4 Ns)),  k = j mod Ns,
+//   y[(j-k)*4 + k + s Ns] = DFT4(v)[s].
+__device__ __forceinline__ void radix4_pass(const float2 *__restrict__ x, float2 *__restrict__ y,
+                                            const float2 *__restrict__ tw, int p, int Ns, int t, int TPF)
+{
+    const int q = p >> 2;
+    const int tstep = p / (Ns << 2);
+    for (int j = t; j < q; j += TPF) {
+        const int k = j & (Ns - 1);
+        float2 v0 = x[j], v1 = x[j + q], v2 = x[j + 2 * q], v3 = x[j + 3 * q];
+        if (Ns > 1) {
+            const int e = k * tstep;
+            v1 = cmul(v1, tw[e]);
+            v2 = cmul(v2, tw[2 * e]);
+            v3 = cmul(v3, tw[3 * e]);
+        }
+        const float2 a = make_float2(v0.x + v2.x, v0.y + v2.y);
+        const float2 b = make_float2(v0.x - v2.x, v0.y - v2.y);
+        const float2 c = make_float2(v1.x + v3.x, v1.y + v3.y);
+        const float2 d = make_float2(v1.x - v3.x, v1.y - v3.y);
+        const int o = ((j - k) << 2) + k;
+        y[o] = make_float2(a.x + c.x, a.y + c.y);
+        y[o + Ns] = make_float2(b.x + d.y, b.y - d.x);
+        y[o + 2 * Ns] = make_float2(a.x - c.x, a.y - c.y);
+        y[o + 3 * Ns] = make_float2(b.x - d.y, b.y + d.x);
+    }
+}
+
+__device__ __forceinline__ void radix2_pass(const float2 *__restrict__ x, float2 *__restrict__ y,
+                                            const float2 *__restrict__ tw, int p, int Ns, int t, int TPF)
+{
+    const int q = p >> 1;
+    const int tstep = p / (Ns << 1);
+    for (int j = t; j < q; j += TPF) {
+        const int k = j & (Ns - 1);
+        const float2 v0 = x[j];
+        float2 v1 = x[j + q];
+        if (Ns > 1) v1 = cmul(v1, tw[k * tstep]);
+        const int o = ((j - k) << 1) + k;
+        y[o] = make_float2(v0.x + v1.x, v0.y + v1.y);
+        y[o + Ns] = make_float2(v0.x - v1.x, v0.y - v1.y);
+    }
+}
+
+// Forward FFT of length 2^lg; ping-pongs between a and b, returns the buffer
+// holding the result.  Every thread of the CTA calls it (barriers inside).
+__device__ __forceinline__ float2 *fft_forward(float2 *a, float2 *b, const float2 *tw, int p, int lg, int t, int TPF)
+{
+    int Ns = 1, l = 0;
+    for (; l + 2 <= lg; l += 2) {
+        radix4_pass(a, b, tw, p, Ns, t, TPF);
+        __syncthreads();
+        float2 *s = a;
+        a = b;
+        b = s;
+        Ns <<= 2;
+    }
+    if (l < lg) {
+        radix2_pass(a, b, tw, p, Ns, t, TPF);
+        __syncthreads();
+        float2 *s = a;
+        a = b;
+        b = s;
+    }
+    return a;
+}
+
+template <typename T> __device__ __forceinline__ T store_cvt(float v);
+template <> __device__ __forceinline__ float store_cvt<float>(float v) { return v; }
+template <> __device__ __forceinline__ __half store_cvt<__half>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 store_cvt<__nv_bfloat16>(float v)
+{
+    return __float2bfloat16_rn(v);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_constant__ FiltParams P)
+{
+    extern __shared__ __align__(16) float2 fsm[];
+    const int p = P.p;
+    const int TPF = min(kFiltThreads, p >> 2);
+    const int G = kFiltThreads / TPF;
+    const int grp = threadIdx.x / TPF, t = threadIdx.x - grp * TPF;
+    float2 *tw = fsm;  // exp(-2 pi i k / p), k < 3p/4 are used
+    float2 *bufA = fsm + p + (size_t)grp * 2 * p;
+    float2 *bufB = bufA + p;
+    for (int k = threadIdx.x; k < p; k += kFiltThreads) {
+        float s, c;
+        sincospif(-2.0f * (float)k / (float)p, &s, &c);
+        tw[k] = make_float2(c, s);
+    }
+    const float sigma = P.q_scale ? *P.q_scale : 1.f;
+    const int W = P.L.W;
+    T *out = static_cast<T *>(P.out);
+    __syncthreads();
+
+    for (long long pg = blockIdx.x; pg * G < P.npairs; pg += gridDim.x) {
+        const long long pair = pg * G + grp;
+        const bool valid = pair < P.npairs;
+        const long long ra = 2 * pair, rb = 2 * pair + 1;
+        const bool hasb = valid && rb < P.nrows;
+        if (valid) {
+            int r_a = 0, r_b = 0;
+            const long long oa = in_row_offset(P.L, ra, r_a);
+            const long long ob = hasb ? in_row_offset(P.L, rb, r_b) : 0;
+            for (int x = t; x < p; x += TPF) {
+                float a = 0.f, b = 0.f;
+                if (x < W) {
+                    a = load_pre(P.L, oa, r_a, x);
+                    if (hasb) b = load_pre(P.L, ob, r_b, x);
+                }
+                bufA[x] = make_float2(a, b);
+            }
+        }
+        __syncthreads();
+        float2 *R = fft_forward(bufA, bufB, tw, p, P.lg, t, TPF);
+        float2 *Sb = (R == bufA) ? bufB : bufA;
+        // conj(Z) * Hf (Hf real and even)
+        for (int k = t; k < p; k += TPF) {
+            const float h = P.Hf[k <= (p >> 1) ? k : p - k];
+            const float2 z = R[k];
+            R[k] = make_float2(z.x * h, -z.y * h);
+        }
+        __syncthreads();
+        float2 *Q = fft_forward(R, Sb, tw, p, P.lg, t, TPF);
+        if (valid) {
+            T *qa = out + ra * (long long)P.Wp;
+            for (int i = t; i < W; i += TPF) qa[i] = store_cvt<T>(Q[i].x * sigma);
+            if (hasb) {
+                T *qb = out + rb * (long long)P.Wp;
+                for (int i = t; i < W; i += TPF) qb[i] = store_cvt<T>(-Q[i].y * sigma);
+            }
+        }
+        __syncthreads();  // buffers are reused by the next pair group
+    }
+}
+
+// max |preprocessed sample| over the whole input, as float bits in *maxbits.
+__global__ void __launch_bounds__(256) prescan_kernel(const __grid_constant__ LoadParams L, long long nrows,
+                                                      unsigned *maxbits)
+{
+    float m = 0.f;
+    const long long total = nrows * L.W;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long row = i / L.W;
+        const int x = (int)(i - row * L.W);
+        int r;
+        const long long off = in_row_offset(L, row, r);
+        const float v = fabsf(load_pre(L, off, r, x));
+        if (v == v) m = fmaxf(m, v);  // NaN input leaves the bound unchanged
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float wm[8];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, wm[w]);
+        atomicMax(maxbits, __float_as_uint(m));
+    }
+}
+
+// Turns the bound into a power-of-two storage scale: |q| <= max * L1K.
+__global__ void scale_finalize_kernel(float *scale, double L1K)
+{
+    const float m = __uint_as_float(*reinterpret_cast<unsigned *>(scale));
+    float s = 1.f;
+    const double bound = (double)m * L1K;
+    if (bound > 0.0 && isfinite(bound)) {
+        int e = (int)floor(log2((double)kScaleTarget / bound));
+        e = max(-100, min(100, e));
+        s = (float)ldexp(1.0, e);
+    }
+    *scale = s;
+}
+
+__global__ void set_scale_kernel(float *scale, float v) { *scale = v; }
+
+// ---------------------------------------------------------------------------
+// host: filter spectrum (FP64), cached per (W, tau, window, p)
+
+struct Spectrum {
+    int p;
+    std::vector<float> Hf;  // p/2 + 1
+    double L1K;             // sum_n |K[n]|, K = unnormalised spatial kernel, |n| < W
+};
+
+// FilteredBackProjection::RamLak (kernel.cu:792-802), float result.
+static float ramlak_ref(int v, float sm)
+{
+    if (v == 0) return (float)(1. / (4. * sm * sm));
+    if ((v % 2) == 0) return 0.f;
+    return (float)(-1. / (v * v * M_PI * M_PI * sm * sm));
+}
+
+static double window_gain(int window, int k, int p)
+{
+    const double f = (double)k / (double)p;
+    if (window == TK_WINDOW_SHEPP_LOGAN) return k == 0 ? 1.0 : std::sin(M_PI * f) / (M_PI * f);
+    if (window == TK_WINDOW_HANN) return 0.5 * (1.0 + std::cos(2.0 * M_PI * f));
+    return 1.0;
+}
+
+static const Spectrum &spectrum(int W, float tau, int window, int p)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, uint32_t, int, int>, Spectrum> cache;
+    uint32_t tb;
+    std::memcpy(&tb, &tau, 4);
+    const auto key = std::make_tuple(W, tb, window, p);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    Spectrum sp;
+    sp.p = p;
+    // h[i] = RamLak(i - W/2)/2 for i < W, zero padded (FillFilter, kernel.cu:783-790)
+    std::vector<float> h(W);
+    for (int i = 0; i < W; ++i) h[i] = ramlak_ref(i - W / 2, tau) / 2;
+    std::vector<double> ct(p), st(p);
+    for (int m = 0; m < p; ++m) {
+        ct[m] = std::cos(2.0 * M_PI * m / p);
+        st[m] = std::sin(2.0 * M_PI * m / p);
+    }
+    std::vector<double> Hd(p / 2 + 1);
+    for (int k = 0; k <= p / 2; ++k) {
+        double sr = 0, si = 0;
+        for (int i = 0; i < W; ++i) {
+            const int m = (int)(((long long)k * i) % p);
+            sr += h[i] * ct[m];
+            si -= h[i] * st[m];
+        }
+        // AbsKernel: sampling * |X| (kernel.cu:55-64)
+        Hd[k] = (double)tau * std::sqrt(sr * sr + si * si) * window_gain(window, k, p);
+    }
+    sp.Hf.resize(p / 2 + 1);
+    for (int k = 0; k <= p / 2; ++k) sp.Hf[k] = (float)Hd[k];
+    double L1 = 0;
+    for (int n = 0; n < W; ++n) {
+        double s = Hd[0] + Hd[p / 2] * ((n & 1) ? -1.0 : 1.0);
+        for (int k = 1; k < p / 2; ++k) s += 2.0 * Hd[k] * ct[(int)(((long long)k * n) % p)];
+        L1 += (n == 0 ? 1.0 : 2.0) * std::fabs(s);
+    }
+    sp.L1K = L1;
+    return cache.emplace(key, std::move(sp)).first->second;
+}
+
+static int launch_filter_typed(const FiltParams &P, int p, cudaStream_t stream, int precision)
+{
+    const void *fn = precision == TK_F32   ? reinterpret_cast<const void *>(&filter_fft_kernel<float>)
+                     : precision == TK_F16 ? reinterpret_cast<const void *>(&filter_fft_kernel<__half>)
+                                           : reinterpret_cast<const void *>(&filter_fft_kernel<__nv_bfloat16>);
+    const int TPF = std::min(kFiltThreads, p >> 2);
+    const int G = kFiltThreads / TPF;
+    const size_t smem = (size_t)p * sizeof(float2) * (1 + 2 * (size_t)G);
+    TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "filter: pad length %d needs too much shared memory", p);
+    TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int dev = 0, sms = 0, per_sm = 0;
+    TK_CUDA(cudaGetDevice(&dev));
+    TK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    TK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kFiltThreads, smem));
+    if (per_sm < 1) per_sm = 1;
+    const long long groups = (P.npairs + G - 1) / G;
+    const long long grid = std::min<long long>(groups, (long long)sms * per_sm);
+    void *args[] = {const_cast<FiltParams *>(&P)};
+    TK_CUDA(cudaLaunchKernel(fn, dim3((unsigned)std::max<long long>(grid, 1)), dim3(kFiltThreads), args, smem,
+                             stream));
+    return TK_OK;
+}
+
+int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int layout, const tk_flatfield *ff,
+                  int window, void *d_q, int precision, float *d_q_scale, cudaStream_t stream)
+{
+    if (int rc = validate_geometry(&g)) return rc;
+    TK_CHECK(d_in && d_q, TK_ERR_INVALID, "filter: null device pointer");
+    TK_CHECK(input_type == TK_INPUT_F32 || input_type == TK_INPUT_U16, TK_ERR_INVALID, "filter: bad input type");
+    TK_CHECK(layout == TK_LAYOUT_SINOGRAM || layout == TK_LAYOUT_PROJECTION, TK_ERR_INVALID, "filter: bad layout");
+    TK_CHECK(window >= TK_WINDOW_RAMLAK && window <= TK_WINDOW_HANN, TK_ERR_INVALID, "filter: bad window");
+    TK_CHECK(precision >= TK_F32 && precision <= TK_BF16, TK_ERR_INVALID, "filter: bad precision");
+    TK_CHECK(precision == TK_F32 || d_q_scale, TK_ERR_INVALID, "filter: 16-bit storage needs d_q_scale");
+    TK_CHECK(input_type == TK_INPUT_F32 || ff, TK_ERR_INVALID, "filter: raw input needs flat-field parameters");
+    const int p = reference_pad_length(g.W);
+    TK_CHECK(p <= 2 * (kMaxHf - 1), TK_ERR_UNSUPPORTED, "filter: W = %d exceeds the supported 4096", g.W);
+
+    static thread_local FiltParams P;  // ~16 KB: keep off the stack
+    std::memset(&P, 0, sizeof(P));
+    LoadParams &L = P.L;
+    L.in = d_in;
+    L.W = g.W;
+    L.N = g.N;
+    L.H = g.H;
+    L.layout = layout;
+    L.input_type = input_type;
+    L.cX = g.cX;
+    L.cZ = g.cZ;
+    L.D = g.D;
+    L.A = 1.f;
+    if (input_type == TK_INPUT_U16) {
+        TK_CHECK(ff->floor_counts > 0.f, TK_ERR_INVALID, "filter: floor_counts must be > 0");
+        TK_CHECK(ff->flat || ff->flat_value > 0.f, TK_ERR_INVALID, "filter: flat field missing");
+        L.dark = ff->dark;
+        L.flat = ff->flat;
+        L.dark_v = ff->dark_value;
+        L.flat_v = ff->flat_value;
+        L.A = ff->A;
+        L.B = ff->B;
+        L.invert = ff->invert ? 1 : 0;
+        L.floor_counts = ff->floor_counts;
+    }
+    const Spectrum &sp = spectrum(g.W, g.tau, window, p);
+    P.out = d_q;
+    P.nrows = (long long)g.N * g.H;
+    P.npairs = (P.nrows + 1) / 2;
+    P.Wp = row_pitch(g.W);
+    P.p = p;
+    int lg = 0;
+    while ((1 << lg) < p) ++lg;
+    P.lg = lg;
+    P.precision = precision;
+    std::memcpy(P.Hf, sp.Hf.data(), sizeof(float) * sp.Hf.size());
+
+    if (precision == TK_F32) {
+        P.q_scale = nullptr;
+        if (d_q_scale) set_scale_kernel<<<1, 1, 0, stream>>>(d_q_scale, 1.f);
+    } else {
+        TK_CUDA(cudaMemsetAsync(d_q_scale, 0, sizeof(float), stream));
+        int dev = 0, sms = 0;
+        TK_CUDA(cudaGetDevice(&dev));
+        TK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        prescan_kernel<<<sms * 4, 256, 0, stream>>>(L, P.nrows, reinterpret_cast<unsigned *>(d_q_scale));
+        scale_finalize_kernel<<<1, 1, 0, stream>>>(d_q_scale, sp.L1K);
+        P.q_scale = d_q_scale;
+    }
+    TK_CUDA(cudaGetLastError());
+    return launch_filter_typed(P, p, stream, precision);
+}
+
+}  // namespace tk

@@ -1,0 +1,47 @@
+// tk_internal.h -- host-side interfaces shared by the library's translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/tk_fdk.h"
+
+namespace tk {
+
+void set_error(const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+// Row pitch (elements) of the device filtered-projection layout [N][H][Wp]:
+// rows start on 16-byte boundaries for every storage precision.
+inline int row_pitch(int W) { return (W + 7) & ~7; }
+inline size_t elem_size(int precision) { return precision == TK_F32 ? 4 : 2; }
+inline size_t filtered_bytes(const tk_geometry &g, int precision)
+{
+    return (size_t)g.N * (size_t)g.H * (size_t)row_pitch(g.W) * elem_size(precision);
+}
+
+int validate_geometry(const tk_geometry *g);
+int reference_pad_length(int W);
+
+// Angle tables exactly as CalcSinCos builds them (FBPG/kernel.cu:430-441).
+void build_trig(const tk_geometry &g, float *cos_out, float *sin_out);
+
+// Launchers (asynchronous on `stream`).
+int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int layout,
+                  const tk_flatfield *ff, int window, void *d_q, int precision, float *d_q_scale,
+                  cudaStream_t stream);
+int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale,
+                       int nz, float zoff, float *d_vol, int accumulate, cudaStream_t stream);
+int launch_phantom(const tk_geometry &g, const double *ell, int nell, int layout, float *d_out,
+                   cudaStream_t stream);
+
+// Device error word of the current device (allocated on first use).
+unsigned *device_error_word();
+
+// Backprojection tile configuration (chosen by the autotuner or defaults).
+struct BPConfig {
+    int variant;  // index into the compiled kernel table
+};
+
+}  // namespace tk

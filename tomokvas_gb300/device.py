@@ -1,0 +1,122 @@
+"""Stage API over device buffers (torch tensors used only as device memory).
+
+Thin wrappers of the C ABI entry points tk_filter_projections,
+tk_backproject, tk_fdk_device and tk_phantom_project.  All work runs in the
+CUDA library; torch provides allocation and the current stream.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, load
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _stream_ptr(stream=None) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _geom(g):
+    return g.to_c() if hasattr(g, "to_c") else g
+
+
+def row_pitch(W: int) -> int:
+    return (W + 7) & ~7
+
+
+_TDTYPE = {_lib.TK_F32: "float32", _lib.TK_F16: "float16", _lib.TK_BF16: "bfloat16"}
+
+
+def flatfield(flat=None, dark=None, flat_value=0.0, dark_value=0.0, A=1.0, B=0.0, invert=True, floor_counts=0.5):
+    """tk_flatfield; flat/dark may be device tensors [H][W] (float32) or None."""
+    ff = _lib.FlatField()
+    ff.flat = None if flat is None else flat.data_ptr()
+    ff.dark = None if dark is None else dark.data_ptr()
+    ff.flat_value, ff.dark_value = float(flat_value), float(dark_value)
+    ff.A, ff.B, ff.invert, ff.floor_counts = float(A), float(B), int(bool(invert)), float(floor_counts)
+    return ff
+
+
+def alloc_filtered(g, precision=_lib.TK_F32, device="cuda"):
+    torch = _torch()
+    dt = getattr(torch, _TDTYPE[precision])
+    q = torch.empty((g.N, g.H, row_pitch(g.W)), dtype=dt, device=device)
+    scale = torch.ones(1, dtype=torch.float32, device=device)
+    return q, scale
+
+
+def filter_projections(g, d_in, input_type=_lib.TK_INPUT_F32, layout=_lib.TK_LAYOUT_SINOGRAM, ff=None,
+                       window=_lib.TK_WINDOW_RAMLAK, precision=_lib.TK_F32, out=None, stream=None):
+    """Preprocess + ramp filter; returns (q [N][H][Wp], scale[1]) device tensors."""
+    L = load()
+    q, scale = out if out is not None else alloc_filtered(g, precision, d_in.device)
+    gc = _geom(g)
+    check(L.tk_filter_projections(ctypes.byref(gc), d_in.data_ptr(), input_type, layout,
+                                  None if ff is None else ctypes.byref(ff), window, q.data_ptr(), precision,
+                                  scale.data_ptr(), _stream_ptr(stream)))
+    return q, scale
+
+
+def backproject(g, q, scale, precision=_lib.TK_F32, vol=None, nz=None, zoff=None, accumulate=False, stream=None):
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    nz = g.Z if nz is None else nz
+    zoff = L.tk_default_zoff(ctypes.byref(gc)) if zoff is None else zoff
+    if vol is None:
+        vol = torch.empty((nz, g.Y, g.X), dtype=torch.float32, device=q.device)
+    check(L.tk_backproject(ctypes.byref(gc), q.data_ptr(), precision,
+                           None if scale is None else scale.data_ptr(), int(nz), float(zoff), vol.data_ptr(),
+                           int(bool(accumulate)), _stream_ptr(stream)))
+    return vol
+
+
+def workspace_bytes(g, precision=_lib.TK_F32) -> int:
+    gc = _geom(g)
+    return int(load().tk_fdk_workspace_bytes(ctypes.byref(gc), precision))
+
+
+def fdk_device(g, d_in, input_type=_lib.TK_INPUT_F32, layout=_lib.TK_LAYOUT_SINOGRAM, ff=None,
+               window=_lib.TK_WINDOW_RAMLAK, precision=_lib.TK_F32, workspace=None, vol=None, stream=None):
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    nb = workspace_bytes(g, precision)
+    if workspace is None:
+        workspace = torch.empty(nb, dtype=torch.uint8, device=d_in.device)
+    if vol is None:
+        vol = torch.empty((g.Z, g.Y, g.X), dtype=torch.float32, device=d_in.device)
+    check(L.tk_fdk_device(ctypes.byref(gc), d_in.data_ptr(), input_type, layout,
+                          None if ff is None else ctypes.byref(ff), window, precision, workspace.data_ptr(),
+                          workspace.numel(), vol.data_ptr(), _stream_ptr(stream)))
+    return vol
+
+
+def phantom_project(g, ell: np.ndarray, layout=_lib.TK_LAYOUT_SINOGRAM, out=None, device="cuda", stream=None):
+    """Analytic line integrals of ellipsoids on the GPU (FP32)."""
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    e = np.ascontiguousarray(ell, dtype=np.float64).reshape(-1, 16)
+    shape = (g.H, g.N, g.W) if layout == _lib.TK_LAYOUT_SINOGRAM else (g.N, g.H, g.W)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float32, device=device)
+    check(L.tk_phantom_project(ctypes.byref(gc), e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), e.shape[0],
+                               layout, out.data_ptr(), _stream_ptr(stream)))
+    return out
+
+
+def device_error_flags(clear=True) -> int:
+    v = ctypes.c_uint()
+    check(load().tk_device_error_flags(ctypes.byref(v), int(bool(clear))))
+    return v.value
