@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-rmse", action="store_true", help="skip the FP64 oracle accuracy check")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-bp", choices=["f32", "f16", "bf16"], default=None,
+                    help="small case for ncu: 180 x 1024^2 projections, a 64-slice slab of the 1024^2 volume; "
+                         "one untimed and two timed backprojection launches")
     return ap.parse_args()
 
 
@@ -391,8 +394,43 @@ def run_ours(args):
     return 0
 
 
+def run_profile_bp(args):
+    """Backprojection-only case small enough for an ncu capture (inputs > L2)."""
+    import torch
+
+    from tomokvas_gb300 import _build, _lib, device
+
+    _build.build()
+    torch.cuda.set_device(0)
+    g = workload().replace(N=180, dfi=float(np.float32(2.0 * np.pi / 180)))
+    prec = _lib.PRECISIONS[args.profile_bp]
+    line = device.phantom_project(g, phantom(g), _lib.TK_LAYOUT_PROJECTION)
+    q, scale = device.filter_projections(g, line, _lib.TK_INPUT_F32, _lib.TK_LAYOUT_PROJECTION,
+                                         window=_lib.TK_WINDOW_HANN, precision=prec)
+    del line
+    nz = 64
+    vol = torch.empty((nz, g.Y, g.X), dtype=torch.float32, device="cuda")
+    zoff = -(g.Z - 1) / 2.0 + (g.Z - nz) / 2.0  # the central slab
+    sc = scale if prec != _lib.TK_F32 else None
+    device.backproject(g, q, sc, prec, vol=vol, nz=nz, zoff=zoff)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(2):
+        device.backproject(g, q, sc, prec, vol=vol, nz=nz, zoff=zoff)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 2
+    upd = nz * g.X * g.Y * g.N
+    emit({"profile_bp": args.profile_bp, "ms_per_launch": ms, "gups": upd / (ms * 1e-3) / 1e9,
+          "updates_per_launch": upd, "flags": device.device_error_flags()})
+    return 0
+
+
 def main():
     args = parse()
+    if args.profile_bp:
+        return run_profile_bp(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

