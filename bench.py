@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-rmse", action="store_true", help="skip the FP64 oracle accuracy check")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--variant", type=int, default=-1, help="backprojection kernel variant (-1 = default)")
+    ap.add_argument("--sweep", action="store_true", help="with --profile-bp: time every variant of that precision")
     ap.add_argument("--profile-bp", choices=["f32", "f16", "bf16"], default=None,
                     help="small case for ncu: 180 x 1024^2 projections, a 64-slice slab of the 1024^2 volume; "
                          "one untimed and two timed backprojection launches")
@@ -412,18 +414,26 @@ def run_profile_bp(args):
     vol = torch.empty((nz, g.Y, g.X), dtype=torch.float32, device="cuda")
     zoff = -(g.Z - 1) / 2.0 + (g.Z - nz) / 2.0  # the central slab
     sc = scale if prec != _lib.TK_F32 else None
-    device.backproject(g, q, sc, prec, vol=vol, nz=nz, zoff=zoff)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(2):
-        device.backproject(g, q, sc, prec, vol=vol, nz=nz, zoff=zoff)
-    e1.record()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / 2
+    L = _lib.load()
+    variants = [args.variant]
+    if args.sweep:
+        variants = [i for i in range(L.tk_bp_variant_count()) if L.tk_bp_variant_precision(i) == prec]
     upd = nz * g.X * g.Y * g.N
-    emit({"profile_bp": args.profile_bp, "ms_per_launch": ms, "gups": upd / (ms * 1e-3) / 1e9,
-          "updates_per_launch": upd, "flags": device.device_error_flags()})
+    for vi in variants:
+        _lib.check(L.tk_bp_select_variant(vi))
+        device.backproject(g, q, sc, prec, vol=vol, nz=nz, zoff=zoff)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(2):
+            device.backproject(g, q, sc, prec, vol=vol, nz=nz, zoff=zoff)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 2
+        name = L.tk_bp_variant_name(vi).decode() if vi >= 0 else "default"
+        emit({"profile_bp": args.profile_bp, "variant": name, "ms_per_launch": ms,
+              "gups": upd / (ms * 1e-3) / 1e9, "updates_per_launch": upd, "flags": device.device_error_flags()})
+    _lib.check(L.tk_bp_select_variant(-1))
     return 0
 
 

@@ -146,6 +146,15 @@ int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_type, int la
                   const tk_flatfield *ff, int window, int precision,
                   void *d_workspace, size_t workspace_bytes, float *d_vol, void *stream);
 
+/* Backprojection kernel variants (tile shape, pipeline), for benchmarking
+ * and the autotuner; no counterpart in the reference, whose launch shape is
+ * fixed (kernel.cu:825-827).  tk_bp_select_variant(-1) restores the default
+ * choice; a selected variant applies to launches of its storage precision. */
+int tk_bp_variant_count(void);
+const char *tk_bp_variant_name(int i);
+int tk_bp_variant_precision(int i);
+int tk_bp_select_variant(int i);
+
 /* Analytic cone-beam line integrals of ellipsoids (seeded synthetic input).
  * ell: host array of nell records of 16 doubles: centre[3] (cm), semi-axes[3]
  * (cm), rotation world->local[9], density (1/cm).  Output device float

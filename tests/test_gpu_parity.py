@@ -95,6 +95,34 @@ def test_bp_stage_matches_oracle(orc, cuda, case):
     assert device.device_error_flags() == 0
 
 
+def test_every_bp_variant_matches_oracle(orc, cuda, case):
+    """All compiled backprojection variants (tile shape / pipeline) agree with the oracle."""
+    import torch
+
+    from tomokvas_gb300._lib import check, load
+
+    g, G, ell, sino = case
+    L = load()
+    v64 = orc.fdk_f64(sino, G)
+    v32 = orc.fdk_f32(sino, G)
+    d_in = to_dev(sino, torch)
+    try:
+        for i in range(L.tk_bp_variant_count()):
+            prec = L.tk_bp_variant_precision(i)
+            check(L.tk_bp_select_variant(i))
+            v = device.fdk_device(g, d_in, precision=prec)
+            torch.cuda.synchronize()
+            v = v.cpu().numpy()
+            name = L.tk_bp_variant_name(i).decode()
+            if prec == _lib.TK_F32:
+                assert rel_rmse(v, v32) < F32_RMSE, name
+            else:
+                assert rel_rmse(v, v64) < (F16_RMSE if prec == _lib.TK_F16 else BF16_RMSE), name
+            assert device.device_error_flags() == 0, name
+    finally:
+        check(L.tk_bp_select_variant(-1))
+
+
 def test_fdk_f32_matches_restatement_and_fp64(orc, cuda, case):
     import torch
 

@@ -404,6 +404,247 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 }
 
 // ---------------------------------------------------------------------------
+// Coefficient-pipeline backprojector.
+//
+// Every staged tile is expanded once into bilinear coefficients, so that an
+// update needs one shared load and four FMAs:
+//   FP32 storage:      float4 (Q, dU, dV, dUV)            LDS.128
+//   FP16/BF16 storage: uint2  {(Q, dV), (dU, dUV)} pairs   LDS.64 + HFMA2
+// The expansion of tile b+1 overlaps the updates of tile b: threads arrive on
+// the tile's mbarrier after expanding their share, update from tile b, and
+// only then wait for tile b+1, so no CTA-wide barrier stalls the loop.  Three
+// coefficient buffers make the reuse safe: a thread may only expand tile b+1
+// after passing the wait on tile b, and every thread arrives on tile b only
+// after finishing its updates of tile b-2.
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <typename S> struct CoefOf;
+template <> struct CoefOf<StoreF32> { using E = float4; };
+template <> struct CoefOf<StoreF16> { using E = uint2; };
+template <> struct CoefOf<StoreBF16> { using E = uint2; };
+
+// FP32 tile [BH][BW] -> float4 coefficients [BH-1][BW] (column BW-1 unused).
+// Work item = (quad of columns, band of rows); walking down the band reuses
+// the previous raw row.  The fifth column of the last quad is read one
+// element past the row (the next row or the stage padding) and only feeds
+// the unused last column.
+template <int NT>
+__device__ __forceinline__ void expand_f32(const float *__restrict__ raw, float4 *__restrict__ coef, int BW, int BH,
+                                           int tid)
+{
+    constexpr int kBand = 4;
+    const int nq = BW >> 2;
+    const int nrows = BH - 1;
+    const int nbands = (nrows + kBand - 1) / kBand;
+    for (int item = tid; item < nq * nbands; item += NT) {
+        const int cq = item % nq, band = item / nq;
+        const int r0 = band * kBand, r1 = min(r0 + kBand, nrows);
+        const int c0 = cq << 2;
+        float4 a = *reinterpret_cast<const float4 *>(raw + r0 * BW + c0);
+        float a4 = raw[r0 * BW + c0 + 4];
+        float4 dA = make_float4(a.y - a.x, a.z - a.y, a.w - a.z, a4 - a.w);
+        for (int r = r0; r < r1; ++r) {
+            const float4 b = *reinterpret_cast<const float4 *>(raw + (r + 1) * BW + c0);
+            const float b4 = raw[(r + 1) * BW + c0 + 4];
+            const float4 dB = make_float4(b.y - b.x, b.z - b.y, b.w - b.z, b4 - b.w);
+            float4 *o = coef + r * BW + c0;
+            o[0] = make_float4(a.x, dA.x, b.x - a.x, dB.x - dA.x);
+            o[1] = make_float4(a.y, dA.y, b.y - a.y, dB.y - dA.y);
+            o[2] = make_float4(a.z, dA.z, b.z - a.z, dB.z - dA.z);
+            o[3] = make_float4(a.w, dA.w, b.w - a.w, dB.w - dA.w);
+            a = b;
+            dA = dB;
+        }
+    }
+}
+
+template <typename S, int NT>
+__device__ __forceinline__ void expand_any(const typename S::T *raw, typename CoefOf<S>::E *coef, int BW, int BH,
+                                           int tid)
+{
+    if constexpr (S::kCoef)
+        expand_tile<typename S::T, typename Vec2Of<S>::type, NT>(raw, coef, BW, BH, tid);
+    else
+        expand_f32<NT>(raw, coef, BW, BH, tid);
+}
+
+template <typename S, int TZ, bool ALL_IN>
+__device__ __forceinline__ void update_column(const typename CoefOf<S>::E *__restrict__ cb, uint32_t cbase, uint32_t BW,
+                                              const float (&aZ)[TZ], float (&acc)[TZ], float U, float U2, float fu,
+                                              float cZ, float Hm1)
+{
+    using V2 = typename Vec2Of<S>::type;
+    [[maybe_unused]] V2 fu2;
+    if constexpr (S::kCoef) fu2 = splat<V2>(fu);
+#pragma unroll
+    for (int z = 0; z < TZ; ++z) {
+        const float v = aZ[z] * U + cZ;
+        const float fl = __fadd_rd(v, kMagic);
+        const float fv = v - (fl - kMagic);
+        const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
+        float A, B;
+        if constexpr (S::kCoef) {
+            const float2 ab = coef_eval<V2>(cb[o], fu2);
+            A = ab.x;
+            B = ab.y;
+        } else {
+            const float4 c = cb[o];
+            A = fmaf(fu, c.y, c.x);
+            B = fmaf(fu, c.w, c.z);
+        }
+        const float val = fmaf(fv, B, A);
+        if constexpr (ALL_IN) {
+            acc[z] = fmaf(U2, val, acc[z]);
+        } else {
+            const float w = (v >= 0.f && v <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
+            acc[z] = fmaf(w, val, acc[z]);
+        }
+    }
+}
+
+template <typename S, int TX, int TY, int TZ, int RS, int MINB>
+__global__ void __launch_bounds__(TX *TY, MINB)
+    bp_coef_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
+{
+    using T = typename S::T;
+    using E = typename CoefOf<S>::E;
+    constexpr int NT = TX * TY;
+    constexpr int NC = 3;
+    extern __shared__ __align__(128) unsigned char smem[];
+    T *raw = reinterpret_cast<T *>(smem);
+    E *coef = reinterpret_cast<E *>(smem + (size_t)RS * P.stage_elems * sizeof(T));
+    int2 *boxo = reinterpret_cast<int2 *>(coef + (size_t)NC * P.coef_stride);
+    uint64_t *rfull = reinterpret_cast<uint64_t *>(boxo + P.N);
+    uint64_t *cfull = rfull + RS;
+
+    const int tid = threadIdx.x;
+    const int tx = tid % TX, ty = tid / TX;
+    const int x0 = (blockIdx.x % P.tilesX) * TX, y0 = (blockIdx.x / P.tilesX) * TY;
+    const int z0 = blockIdx.y * TZ;
+    const int x = x0 + tx, y = y0 + ty;
+    const float aX = flip(P.scale * ((float)x + P.dX), P.dirx);
+    const float aY = flip(P.scale * ((float)y + P.dY), P.diry);
+    const bool inside = (x < P.X) && (y < P.Y);
+    const bool active = inside && (sqrtf(aX * aX + aY * aY) < P.halfW);
+
+    if (!__syncthreads_or(active)) {  // tile entirely outside the FOV cylinder
+        if (inside) {
+            for (int z = 0; z < TZ && z0 + z < P.nz; ++z) {
+                float *dst = P.vol + (size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x;
+                *dst = P.accumulate ? 0.f + *dst : 0.f;
+            }
+        }
+        return;
+    }
+
+    for (int b = tid; b < P.N; b += NT) boxo[b] = footprint_origin<TX, TY, TZ, S::kAlign>(P, b, x0, y0, z0);
+    if (tid == 0) {
+        for (int s = 0; s < RS; ++s) mbar_init(&rfull[s], 1);
+        for (int k = 0; k < NC; ++k) mbar_init(&cfull[k], NT);
+        fence_mbar_init();
+        prefetch_tensormap(&tmap);
+    }
+    __syncthreads();
+    const uint32_t stage_bytes = (uint32_t)(P.BW * P.BH * sizeof(T));
+    int issued = 0;  // raw tiles requested (meaningful in thread 0)
+    auto issue = [&](int tile) {
+        const int s = tile % RS;
+        mbar_arrive_expect_tx(&rfull[s], stage_bytes);
+        tma_load_3d(raw + (size_t)s * P.stage_elems, &tmap, boxo[tile].x, boxo[tile].y, tile, &rfull[s]);
+        issued = tile + 1;
+    };
+    if (tid == 0)
+        for (int t = 0; t < RS && t < P.N; ++t) issue(t);
+
+    // Slices past the end of the slab repeat the last one (see the note in
+    // bp_tma_kernel): their footprint stays inside the staged box.
+    float aZ[TZ];
+#pragma unroll
+    for (int z = 0; z < TZ; ++z) aZ[z] = flip(P.scale * ((float)min(z0 + z, P.nz - 1) + P.zoff), P.dirz);
+    float acc[TZ];
+#pragma unroll
+    for (int z = 0; z < TZ; ++z) acc[z] = 0.f;
+
+    bool ok = mbar_wait_bounded(&rfull[0], 0u, kWaitLimitNs);
+    int consumed = 1;
+    if (ok) expand_any<S, NT>(raw, coef, P.BW, P.BH, tid);
+    mbar_arrive(&cfull[0]);
+    ok = ok && mbar_wait_bounded(&cfull[0], 0u, kWaitLimitNs);
+    if (tid == 0 && ok && RS < P.N) issue(RS);
+
+    const float cZ = P.cZ, Hm1 = P.Hm1;
+    const uint32_t BW = (uint32_t)P.BW;
+    for (int b = 0; b < P.N && ok; ++b) {
+        const int nb = b + 1;
+        if (nb < P.N) {
+            ok = mbar_wait_bounded(&rfull[nb % RS], (uint32_t)(nb / RS) & 1u, kWaitLimitNs);
+            consumed = nb + 1;
+            if (ok) expand_any<S, NT>(raw + (size_t)(nb % RS) * P.stage_elems, coef + (size_t)(nb % NC) * P.coef_stride,
+                                      P.BW, P.BH, tid);
+            mbar_arrive(&cfull[nb % NC]);
+        }
+        if (active && ok) {
+            const float2 cs = P.trig[b];
+            const float Sd = aX * cs.x + aY * cs.y;
+            const float Td = aY * cs.x - aX * cs.y;
+            const float U = P.D / (P.D - Sd);
+            const float u = Td * U + P.cX;
+            if (u >= 0.f && u <= P.Wm1) {  // column inside the detector (kernel.cu:127-128)
+                const int bx0 = boxo[b].x, by0 = boxo[b].y;
+                const float U2 = U * U;
+                const float fla = __fadd_rd(u, kMagic);
+                const int col = __float_as_int(fla) - kMagicBits - bx0;
+                const float fu = u - (fla - kMagic);
+                const float vA = aZ[0] * U + cZ, vB = aZ[TZ - 1] * U + cZ;
+                const float vlo = fminf(vA, vB), vhi = fmaxf(vA, vB);
+                const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) + 1 - by0;
+                if (col >= 0 && col + 1 < P.BW && rlo >= 0 && rhi < P.BH) {
+                    const uint32_t cbase = (uint32_t)col - (uint32_t)(kMagicBits + by0) * BW;
+                    const E *cb = coef + (size_t)(b % NC) * P.coef_stride;
+                    if (vlo >= 0.f && vhi <= Hm1)
+                        update_column<S, TZ, true>(cb, cbase, BW, aZ, acc, U, U2, fu, cZ, Hm1);
+                    else
+                        update_column<S, TZ, false>(cb, cbase, BW, aZ, acc, U, U2, fu, cZ, Hm1);
+                } else {
+                    atomicOr(P.err, ERR_BOX_OVERFLOW);
+                }
+            }
+        }
+        if (nb < P.N && ok) {
+            ok = mbar_wait_bounded(&cfull[nb % NC], (uint32_t)(nb / NC) & 1u, kWaitLimitNs);
+            // every thread has expanded tile nb: its raw stage is free again
+            if (tid == 0 && ok && nb + RS < P.N) issue(nb + RS);
+        }
+    }
+
+    if (!ok) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        // Leave no copy in flight into shared memory this CTA gives back.
+        if (tid == 0)
+            for (int k = consumed; k < issued; ++k)
+                mbar_wait_bounded(&rfull[k % RS], (uint32_t)(k / RS) & 1u, 100000000ull);
+        return;
+    }
+
+    if (inside) {
+        const float fs = P.q_scale ? P.fscale / *P.q_scale : P.fscale;
+#pragma unroll
+        for (int z = 0; z < TZ; ++z) {
+            if (z0 + z < P.nz) {
+                float r = 0.f;
+                if (active) r = acc[z] * fs;
+                float *dst = P.vol + (size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x;
+                *dst = P.accumulate ? r + *dst : r;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 
 static PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
@@ -423,19 +664,32 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
 struct BPVariant {
     const void *fn;
     int precision, TX, TY, TZ, STAGES;
+    bool coef;  // coefficient pipeline (bp_coef_kernel) or direct FP32 gathers (bp_tma_kernel)
+    const char *name;
 };
 
-#define TK_BP_VARIANT(S, P, TX, TY, TZ, ST, MB) \
-    {reinterpret_cast<const void *>(&bp_tma_kernel<S, TX, TY, TZ, ST, MB>), P, TX, TY, TZ, ST}
+#define TK_BP_DIRECT(S, P, TX, TY, TZ, ST, MB) \
+    {reinterpret_cast<const void *>(&bp_tma_kernel<S, TX, TY, TZ, ST, MB>), P, TX, TY, TZ, ST, false, \
+     "direct<" #S "," #TX "," #TY "," #TZ "," #ST ">"}
+#define TK_BP_COEF(S, P, TX, TY, TZ, ST, MB) \
+    {reinterpret_cast<const void *>(&bp_coef_kernel<S, TX, TY, TZ, ST, MB>), P, TX, TY, TZ, ST, true, \
+     "coef<" #S "," #TX "," #TY "," #TZ "," #ST ">"}
 
+// The first entry of each precision is the default.
 static const BPVariant kVariants[] = {
-    TK_BP_VARIANT(StoreF32, TK_F32, 16, 16, 32, 4, 2),
-    TK_BP_VARIANT(StoreF16, TK_F16, 16, 16, 32, 4, 2),
-    TK_BP_VARIANT(StoreBF16, TK_BF16, 16, 16, 32, 4, 2),
+    TK_BP_COEF(StoreF32, TK_F32, 16, 16, 32, 3, 2),
+    TK_BP_COEF(StoreF16, TK_F16, 16, 16, 32, 3, 2),
+    TK_BP_COEF(StoreBF16, TK_BF16, 16, 16, 32, 3, 2),
+    TK_BP_DIRECT(StoreF32, TK_F32, 16, 16, 32, 4, 2),
+    TK_BP_DIRECT(StoreF16, TK_F16, 16, 16, 32, 4, 2),
 };
+
+static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
 
 static const BPVariant *pick_variant(int precision)
 {
+    if (g_variant_override >= 0 && kVariants[g_variant_override].precision == precision)
+        return &kVariants[g_variant_override];
     for (const auto &v : kVariants)
         if (v.precision == precision) return &v;
     return nullptr;
@@ -549,8 +803,11 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
 
         size_t smem = (size_t)v->STAGES * P.stage_elems * esz;
-        if (precision != TK_F32) smem += 2 * (size_t)P.coef_stride * sizeof(uint2);
-        smem += (size_t)nb * sizeof(int2) + (size_t)v->STAGES * sizeof(uint64_t) + 16;
+        if (v->coef)
+            smem += 3 * (size_t)P.coef_stride * (precision == TK_F32 ? sizeof(float4) : sizeof(uint2));
+        else if (precision != TK_F32)
+            smem += 2 * (size_t)P.coef_stride * sizeof(uint2);
+        smem += (size_t)nb * sizeof(int2) + (size_t)(v->STAGES + 3) * sizeof(uint64_t) + 16;
         TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "backproject: %zu B of shared memory needed", smem);
         TK_CUDA(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         dim3 grid((unsigned)(tilesX * tilesY), (unsigned)zchunks, 1);
@@ -562,3 +819,30 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
 }
 
 }  // namespace tk
+
+// ---------------------------------------------------------------------------
+// variant selection (benchmarking and the autotuner)
+
+extern "C" int tk_bp_variant_count(void) { return (int)(sizeof(tk::kVariants) / sizeof(tk::kVariants[0])); }
+
+extern "C" const char *tk_bp_variant_name(int i)
+{
+    if (i < 0 || i >= tk_bp_variant_count()) return "";
+    return tk::kVariants[i].name;
+}
+
+extern "C" int tk_bp_variant_precision(int i)
+{
+    if (i < 0 || i >= tk_bp_variant_count()) return -1;
+    return tk::kVariants[i].precision;
+}
+
+extern "C" int tk_bp_select_variant(int i)
+{
+    if (i < -1 || i >= tk_bp_variant_count()) {
+        tk::set_error("no backprojection variant %d", i);
+        return TK_ERR_INVALID;
+    }
+    tk::g_variant_override = i;
+    return TK_OK;
+}
