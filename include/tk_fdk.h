@@ -45,10 +45,22 @@ typedef enum tk_window {   /* ramp filter apodisation */
     TK_WINDOW_HANN = 2
 } tk_window;
 
-typedef enum tk_precision {  /* storage of filtered projections; math stays FP32 */
+/* Storage of the filtered projections between filter and backprojection;
+ * all arithmetic stays FP32.
+ *   TK_F32       raw FP32 samples, [N][H][Wp], Wp = (W + 7) & ~7         4 B
+ *   TK_F16       FP16 bilinear coefficient image, [N][H][Wc],
+ *                Wc = (W + 1) & ~1, entry {(Q, dV), (dU, dUV)} as half2 x2  8 B
+ *   TK_BF16      the same in bfloat16                                       8 B
+ *   TK_F32_COEF  FP32 coefficient image, [N][H][W], entry (Q, dU, dV, dUV) 16 B
+ * where for sample q[r][c]: Q = q[r][c], dU = q[r][c+1] - Q,
+ * dV = q[r+1][c] - Q, dUV = q[r+1][c+1] - q[r+1][c] - dU (samples outside
+ * the detector are zero), so bilinear interpolation inside cell (r, c) is
+ * Q + fu dU + fv (dV + fu dUV). */
+typedef enum tk_precision {
     TK_F32 = 0,
     TK_F16 = 1,
-    TK_BF16 = 2
+    TK_BF16 = 2,
+    TK_F32_COEF = 3
 } tk_precision;
 
 typedef enum tk_layout {
@@ -117,12 +129,13 @@ int tk_device_error_flags(unsigned *flags_out, int clear);
 /* Preprocessing + ramp filter: fuses the uint16 log transform
  * (rsq_load.cpp:299-325), the cosine pre-weight (RB_comma3DKernel,
  * kernel.cu:179-201) and the row-wise ramp filter (fConvolution,
- * kernel.cu:557-781).  Output d_q is projection-major [N][H][Wp] with row
- * pitch Wp = (W + 7) & ~7 elements, in `precision`, equal to the reference's
- * unnormalised C2R output times the storage scale s.  For TK_F32, s = 1 and
- * d_q_scale may be NULL.  For 16-bit storage, s is a power of two chosen on
- * the device from the data so that values stay well inside the format's
- * range; it is written to the device float *d_q_scale. */
+ * kernel.cu:557-781).  Output d_q is projection-major in the storage format
+ * `precision` (see tk_precision), with sample values equal to the reference's
+ * unnormalised C2R output times the storage scale s.  For the FP32 formats
+ * s = 1 and d_q_scale may be NULL.  For 16-bit storage, s is a power of two
+ * chosen on the device from the data so that values stay well inside the
+ * format's range; it is written to the device float *d_q_scale.  The
+ * coefficient formats support W <= 2048. */
 int tk_filter_projections(const tk_geometry *g, const void *d_in, int input_type, int layout,
                           const tk_flatfield *ff, int window, void *d_q, int precision,
                           float *d_q_scale, void *stream);
@@ -136,6 +149,8 @@ int tk_filter_projections(const tk_geometry *g, const void *d_in, int input_type
 int tk_backproject(const tk_geometry *g, const void *d_q, int precision, const float *d_q_scale,
                    int nz, float zoff, float *d_vol, int accumulate, void *stream);
 
+/* Bytes of the filtered projections in a storage format. */
+size_t tk_filtered_bytes(const tk_geometry *g, int precision);
 /* Device bytes tk_fdk_device needs as workspace (filtered projections plus
  * a 256-byte header holding the storage scale). */
 size_t tk_fdk_workspace_bytes(const tk_geometry *g, int precision);

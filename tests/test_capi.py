@@ -93,8 +93,13 @@ def test_stage_argument_checks(tklib):
 def test_workspace_bytes(tklib):
     g = small_geometry(W=60, N=10, H=7)
     gc = g.to_c()
-    assert tklib.tk_fdk_workspace_bytes(ctypes.byref(gc), 0) == 256 + 10 * 7 * 64 * 4
-    assert tklib.tk_fdk_workspace_bytes(ctypes.byref(gc), 1) == 256 + 10 * 7 * 64 * 2
+    assert tklib.tk_fdk_workspace_bytes(ctypes.byref(gc), 0) == 256 + 10 * 7 * 64 * 4   # FP32 samples
+    assert tklib.tk_fdk_workspace_bytes(ctypes.byref(gc), 1) == 256 + 10 * 7 * 60 * 8   # FP16 coefficients
+    assert tklib.tk_fdk_workspace_bytes(ctypes.byref(gc), 2) == 256 + 10 * 7 * 60 * 8   # BF16 coefficients
+    assert tklib.tk_fdk_workspace_bytes(ctypes.byref(gc), 3) == 256 + 10 * 7 * 60 * 16  # FP32 coefficients
+    assert tklib.tk_fdk_workspace_bytes(ctypes.byref(gc), 4) == 0
+    g2 = small_geometry(W=61, N=3, H=5).to_c()
+    assert tklib.tk_filtered_bytes(ctypes.byref(g2), 1) == 3 * 5 * 62 * 8
 
 
 def test_handle_setters_and_state_errors(tklib):

@@ -79,6 +79,49 @@ def test_filter_stage_matches_oracle(orc, cuda, case, window, layout):
     assert rel_rmse(qd, np.transpose(q_ref, (1, 0, 2))) < 2e-6
 
 
+def coefficients_from_samples(q):
+    """(Q, dU, dV, dUV) of every cell of q[N][H][W], samples outside are 0."""
+    qp = np.zeros((q.shape[0], q.shape[1] + 1, q.shape[2] + 1), dtype=np.float64)
+    qp[:, :-1, :-1] = q
+    Q = qp[:, :-1, :-1]
+    dU = qp[:, :-1, 1:] - Q
+    dV = qp[:, 1:, :-1] - Q
+    dUV = qp[:, 1:, 1:] - qp[:, 1:, :-1] - dU
+    return np.stack([Q, dU, dV, dUV], axis=-1)
+
+
+@pytest.mark.parametrize("precision", ["f32c", "f16", "bf16"])
+@pytest.mark.parametrize("H", [64, 130])  # 130: a work unit boundary inside the detector and a short last unit
+def test_filter_writes_coefficient_image(orc, cuda, precision, H):
+    import torch
+
+    g = small_geometry(W=60, N=7, H=H, vol=(32, 32, 32))
+    G = orc.geom_from(g)
+    rng = np.random.default_rng(9)
+    sino = rng.normal(size=(g.H, g.N, g.W)).astype(np.float32)
+    q_ref = np.transpose(orc.filter_f32(orc.weight_f32(sino, G), G), (1, 0, 2)).astype(np.float64)
+    exp = coefficients_from_samples(q_ref)  # [N][H][W][4]
+    prec = _lib.PRECISIONS[precision]
+    q, s = device.filter_projections(g, to_dev(sino, torch), precision=prec)
+    torch.cuda.synchronize()
+    raw = q.cpu().numpy().view(np.uint8)
+    if prec == _lib.TK_F32_COEF:
+        got = raw.view(np.float32).reshape(g.N, g.H, g.W, 4).astype(np.float64)
+        tol = 2e-6
+    else:
+        Wc = (g.W + 1) & ~1
+        h = raw.view(np.uint16).reshape(g.N, g.H, Wc, 4)[:, :, :g.W]
+        if prec == _lib.TK_F16:
+            vals = h.view(np.float16).astype(np.float64)
+        else:
+            vals = (h.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
+        got = vals[..., [0, 2, 1, 3]] / float(s.item())  # stored as (Q, dV), (dU, dUV)
+        tol = 2e-3 if prec == _lib.TK_F16 else 1.5e-2
+    for k in range(4):
+        scale = np.sqrt(np.mean(exp[..., 0] ** 2))
+        assert np.sqrt(np.mean((got[..., k] - exp[..., k]) ** 2)) < tol * scale, (precision, k)
+
+
 def test_bp_stage_matches_oracle(orc, cuda, case):
     import torch
 
@@ -114,7 +157,7 @@ def test_every_bp_variant_matches_oracle(orc, cuda, case):
             torch.cuda.synchronize()
             v = v.cpu().numpy()
             name = L.tk_bp_variant_name(i).decode()
-            if prec == _lib.TK_F32:
+            if prec in (_lib.TK_F32, _lib.TK_F32_COEF):
                 assert rel_rmse(v, v32) < F32_RMSE, name
             else:
                 assert rel_rmse(v, v64) < (F16_RMSE if prec == _lib.TK_F16 else BF16_RMSE), name
@@ -136,8 +179,8 @@ def test_fdk_f32_matches_restatement_and_fp64(orc, cuda, case):
     assert rel_rmse(v, v64) < F32_RMSE
 
 
-@pytest.mark.parametrize("precision,tol", [("f16", F16_RMSE), ("bf16", BF16_RMSE)])
-def test_fdk_16bit_storage_vs_fp64(orc, cuda, case, precision, tol):
+@pytest.mark.parametrize("precision,tol", [("f16", F16_RMSE), ("bf16", BF16_RMSE), ("f32c", F32_RMSE)])
+def test_fdk_storage_formats_vs_fp64(orc, cuda, case, precision, tol):
     import torch
 
     g, G, ell, sino = case
@@ -257,7 +300,7 @@ def test_reconstruct_to_device_and_precisions(orc, cuda, case):
 
     g, G, ell, sino = case
     v64 = orc.fdk_f64(sino, G)
-    for prec, tol in [("f32", F32_RMSE), ("f16", F16_RMSE)]:
+    for prec, tol in [("f32", F32_RMSE), ("f16", F16_RMSE), ("f32c", F32_RMSE)]:
         fbp = FilteredBackProjection(raise_on_error=True)
         fbp.SetSinogramProperties(sino, g.W, g.cX, g.N, g.H, g.cZ, g.dfi, g.D, g.tau)
         fbp.SetReconstructionProperties(None, g.X, g.cx, g.Y, g.cy, g.Z, g.cz, g.rot)
@@ -298,7 +341,8 @@ def test_full_size_1024_sampled_slices(orc, cuda):
         return (num / sum(float(np.sum(r ** 2)) for r in refs)) ** 0.5
 
     rest_err = grouped(rest)
-    for prec, tol in [(_lib.TK_F32, noisy_tol(rest_err)), (_lib.TK_F16, F16_RMSE)]:
+    for prec, tol in [(_lib.TK_F32, noisy_tol(rest_err)), (_lib.TK_F32_COEF, noisy_tol(rest_err)),
+                      (_lib.TK_F16, F16_RMSE)]:
         vol = device.fdk_device(g, raw, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff,
                                 window=_lib.TK_WINDOW_HANN, precision=prec)
         torch.cuda.synchronize()

@@ -13,19 +13,19 @@ from ._build import LIB
 
 TK_OK, TK_ERR_INVALID, TK_ERR_CUDA, TK_ERR_OOM, TK_ERR_STATE, TK_ERR_IO, TK_ERR_DEVICE, TK_ERR_UNSUPPORTED = range(8)
 TK_WINDOW_RAMLAK, TK_WINDOW_SHEPP_LOGAN, TK_WINDOW_HANN = 0, 1, 2
-TK_F32, TK_F16, TK_BF16 = 0, 1, 2
+TK_F32, TK_F16, TK_BF16, TK_F32_COEF = 0, 1, 2, 3
 TK_LAYOUT_SINOGRAM, TK_LAYOUT_PROJECTION = 0, 1
 TK_INPUT_F32, TK_INPUT_U16 = 0, 1
 
 WINDOWS = {"ramlak": TK_WINDOW_RAMLAK, "shepp_logan": TK_WINDOW_SHEPP_LOGAN, "hann": TK_WINDOW_HANN}
-PRECISIONS = {"f32": TK_F32, "f16": TK_F16, "bf16": TK_BF16}
+PRECISIONS = {"f32": TK_F32, "f16": TK_F16, "bf16": TK_BF16, "f32c": TK_F32_COEF}
 LAYOUTS = {"sinogram": TK_LAYOUT_SINOGRAM, "projection": TK_LAYOUT_PROJECTION}
 
 # Every symbol include/tk_fdk.h declares (checked by the CPU test-suite).
 EXPORTS = [
     "tk_version", "tk_last_error", "tk_get_free_mem_info", "tk_pad_length", "tk_default_zoff",
     "tk_zblock_offsets", "tk_device_error_flags", "tk_filter_projections", "tk_backproject",
-    "tk_fdk_workspace_bytes", "tk_fdk_device", "tk_phantom_project", "tk_bp_variant_count",
+    "tk_filtered_bytes", "tk_fdk_workspace_bytes", "tk_fdk_device", "tk_phantom_project", "tk_bp_variant_count",
     "tk_bp_variant_name", "tk_bp_variant_precision", "tk_bp_select_variant", "tk_fdk_create", "tk_fdk_destroy",
     "tk_fdk_set_gpu_id", "tk_fdk_set_block_size", "tk_fdk_set_allocation_limit", "tk_fdk_set_collecting",
     "tk_fdk_set_show_info", "tk_fdk_set_axis_direction", "tk_fdk_set_sinogram_properties",
@@ -99,6 +99,8 @@ def _declare(L):
     L.tk_device_error_flags.argtypes = [ctypes.POINTER(ctypes.c_uint), ip]
     L.tk_filter_projections.argtypes = [G, vp, ip, ip, ctypes.POINTER(FlatField), ip, vp, ip, vp, vp]
     L.tk_backproject.argtypes = [G, vp, ip, vp, ip, fp, vp, ip, vp]
+    L.tk_filtered_bytes.argtypes = [G, ip]
+    L.tk_filtered_bytes.restype = ctypes.c_size_t
     L.tk_fdk_workspace_bytes.argtypes = [G, ip]
     L.tk_fdk_workspace_bytes.restype = ctypes.c_size_t
     L.tk_fdk_device.argtypes = [G, vp, ip, ip, ctypes.POINTER(FlatField), ip, ip, vp, ctypes.c_size_t, vp, vp]

@@ -44,7 +44,6 @@ struct BPParams {
     int X, Y, nz, N;
     int BW, BH;              // staged box (elements)
     int stage_elems;         // elements per raw stage (>= BW*BH, padded)
-    int coef_stride;         // coefficient entries per coefficient buffer
     int tilesX;
     int accumulate;
     float cX, cZ, D;
@@ -68,17 +67,6 @@ struct StoreF32 {
     static constexpr int kAlign = 4;  // TMA x coordinate granularity (16 B)
     static constexpr bool kCoef = false;
 };
-struct StoreF16 {
-    using T = __half;
-    static constexpr int kAlign = 8;
-    static constexpr bool kCoef = true;
-};
-struct StoreBF16 {
-    using T = __nv_bfloat16;
-    static constexpr int kAlign = 8;
-    static constexpr bool kCoef = true;
-};
-
 // Bounding box origin of the footprint of tile (x0,y0,z0) in projection b.
 template <int TX, int TY, int TZ, int ALIGN>
 __device__ __forceinline__ int2 footprint_origin(const BPParams &P, int b, int x0, int y0, int z0)
@@ -114,106 +102,19 @@ __device__ __forceinline__ int2 footprint_origin(const BPParams &P, int b, int x
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: a TMA stage never takes this long
 
 // ---------------------------------------------------------------------------
-// Expansion of a staged 16-bit tile into bilinear coefficient pairs.
-// Entry (r, c): lo = (Q, dV), hi = (dU, dUV) with
-//   Q = q[r][c], dU = q[r][c+1]-Q, dV = q[r+1][c]-Q, dUV = q[r+1][c+1]-q[r+1][c]-dU,
-// so that [top, bot-top] = hi * fu + lo.
-template <typename V2>
-__device__ __forceinline__ V2 v2_shift(V2 a, V2 b)  // (a.y, b.x)
-{
-    uint32_t ua = *reinterpret_cast<uint32_t *>(&a), ub = *reinterpret_cast<uint32_t *>(&b);
-    uint32_t r = __byte_perm(ua, ub, 0x5432);
-    return *reinterpret_cast<V2 *>(&r);
-}
-template <typename V2>
-__device__ __forceinline__ uint32_t v2_bits(V2 a) { return *reinterpret_cast<uint32_t *>(&a); }
-
-template <typename T, typename V2, int NT>
-__device__ __forceinline__ void expand_tile(const T *__restrict__ raw, uint2 *__restrict__ coef, int BW, int BH,
-                                            int tid)
-{
-    // Work item = (column pair, band of kBand coefficient rows); walking down
-    // the band reuses the previous raw row.
-    constexpr int kBand = 4;
-    const int npairs = BW >> 1;
-    const int nrows = BH - 1;
-    const int nbands = (nrows + kBand - 1) / kBand;
-    const V2 *raw2 = reinterpret_cast<const V2 *>(raw);
-    const int w2 = BW >> 1;  // pairs per raw row
-    for (int item = tid; item < npairs * nbands; item += NT) {
-        const int pr = item % npairs, band = item / npairs;
-        const int r0 = band * kBand;
-        const int r1 = min(r0 + kBand, nrows);
-        // row r0: columns (2pr, 2pr+1) and (2pr+2, 2pr+3); the second pair of
-        // the last column pair lies one element past the row and is never used.
-        V2 a0 = raw2[r0 * w2 + pr];
-        V2 a1 = raw2[r0 * w2 + pr + 1];
-        V2 dU0 = __hsub2(v2_shift(a0, a1), a0);
-        for (int r = r0; r < r1; ++r) {
-            const V2 b0 = raw2[(r + 1) * w2 + pr];
-            const V2 b1 = raw2[(r + 1) * w2 + pr + 1];
-            const V2 dU1 = __hsub2(v2_shift(b0, b1), b0);
-            const V2 dV = __hsub2(b0, a0);
-            const V2 dUV = __hsub2(dU1, dU0);
-            // entry (r, 2pr): lo=(a0.x, dV.x) hi=(dU0.x, dUV.x); entry (r, 2pr+1): .y halves
-            uint4 out;
-            out.x = __byte_perm(v2_bits(a0), v2_bits(dV), 0x5410);
-            out.y = __byte_perm(v2_bits(dU0), v2_bits(dUV), 0x5410);
-            out.z = __byte_perm(v2_bits(a0), v2_bits(dV), 0x7632);
-            out.w = __byte_perm(v2_bits(dU0), v2_bits(dUV), 0x7632);
-            *reinterpret_cast<uint4 *>(coef + r * BW + 2 * pr) = out;
-            a0 = b0;
-            dU0 = dU1;
-        }
-    }
-}
-
-template <typename V2>
-__device__ __forceinline__ float2 coef_eval(uint2 c, V2 fu2);
-
-template <>
-__device__ __forceinline__ float2 coef_eval<__half2>(uint2 c, __half2 fu2)
-{
-    const __half2 lo = *reinterpret_cast<__half2 *>(&c.x);
-    const __half2 hi = *reinterpret_cast<__half2 *>(&c.y);
-    return __half22float2(__hfma2(hi, fu2, lo));
-}
-
-template <>
-__device__ __forceinline__ float2 coef_eval<__nv_bfloat162>(uint2 c, __nv_bfloat162 fu2)
-{
-    const __nv_bfloat162 lo = *reinterpret_cast<__nv_bfloat162 *>(&c.x);
-    const __nv_bfloat162 hi = *reinterpret_cast<__nv_bfloat162 *>(&c.y);
-    return __bfloat1622float2(__hfma2(hi, fu2, lo));
-}
-
-template <typename V2> __device__ __forceinline__ V2 splat(float f);
-template <> __device__ __forceinline__ __half2 splat<__half2>(float f) { return __float2half2_rn(f); }
-template <> __device__ __forceinline__ __nv_bfloat162 splat<__nv_bfloat162>(float f)
-{
-    return __float2bfloat162_rn(f);
-}
-
-template <typename S> struct Vec2Of;
-template <> struct Vec2Of<StoreF16> { using type = __half2; };
-template <> struct Vec2Of<StoreBF16> { using type = __nv_bfloat162; };
-template <> struct Vec2Of<StoreF32> { using type = float2; };
-
-// ---------------------------------------------------------------------------
+// Direct FP32 backprojector: bilinear gathers straight from the staged
+// sample tile (four LDS.32 per update).
 template <typename S, int TX, int TY, int TZ, int STAGES, int MINB>
 __global__ void __launch_bounds__(TX *TY, MINB)
     bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
     using T = typename S::T;
-    using V2 = typename Vec2Of<S>::type;
+    static_assert(sizeof(T) == 4, "direct kernel: FP32 samples only");
     constexpr int NT = TX * TY;
     extern __shared__ __align__(128) unsigned char smem[];
 
     T *stages = reinterpret_cast<T *>(smem);
-    // coefficient buffers (16-bit storage only), 16-byte aligned
-    uint2 *coef = reinterpret_cast<uint2 *>(smem + (size_t)STAGES * P.stage_elems * sizeof(T));
-    int2 *boxo = reinterpret_cast<int2 *>(reinterpret_cast<unsigned char *>(coef) +
-                                          (S::kCoef ? 2 * (size_t)P.coef_stride * sizeof(uint2) : 0));
+    int2 *boxo = reinterpret_cast<int2 *>(smem + (size_t)STAGES * P.stage_elems * sizeof(T));
     uint64_t *full = reinterpret_cast<uint64_t *>(boxo + P.N);
     volatile int &s_abort = *reinterpret_cast<int *>(full + STAGES);
 
@@ -276,18 +177,6 @@ __global__ void __launch_bounds__(TX *TY, MINB)
             s_abort = 1;
         }
         const int bx0 = boxo[b].x, by0 = boxo[b].y;
-        const uint2 *cb_tile = coef + (size_t)(b & 1) * P.coef_stride;
-        if constexpr (S::kCoef) {
-            if (got) expand_tile<T, V2, NT>(stages + (size_t)s * P.stage_elems, const_cast<uint2 *>(cb_tile),
-                                            P.BW, P.BH, tid);
-            __syncthreads();
-            if (s_abort) break;
-            if (tid == 0 && b + STAGES < P.N) {  // raw stage s is free again
-                mbar_arrive_expect_tx(&full[s], stage_bytes);
-                tma_load_3d(stages + (size_t)s * P.stage_elems, &tmap, boxo[b + STAGES].x, boxo[b + STAGES].y,
-                            b + STAGES, &full[s]);
-            }
-        }
         if (active && got) {
             const float2 cs = P.trig[b];
             const float dcos = cs.x, dsin = cs.y;
@@ -307,7 +196,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                 if (col >= 0 && col + 1 < P.BW && rlo >= 0 && rhi < P.BH) {
                     const uint32_t cbase = (uint32_t)col - (uint32_t)(kMagicBits + by0) * BW;
                     const bool all_in = (vlo >= 0.f) && (vhi <= Hm1);
-                    if constexpr (!S::kCoef) {
+                    {
                         const float *st = reinterpret_cast<const float *>(stages) + (size_t)s * P.stage_elems;
                         if (all_in) {
 #pragma unroll
@@ -337,44 +226,18 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                                 acc[z] = fmaf(w, fmaf(fv, bot - top, top), acc[z]);
                             }
                         }
-                    } else {
-                        const V2 fu2 = splat<V2>(fu);
-                        if (all_in) {
-#pragma unroll
-                            for (int z = 0; z < TZ; ++z) {
-                                const float v = aZ[z] * U + cZ;
-                                const float fl = __fadd_rd(v, kMagic);
-                                const float fv = v - (fl - kMagic);
-                                const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
-                                const float2 tb = coef_eval<V2>(cb_tile[o], fu2);
-                                acc[z] = fmaf(U2, fmaf(fv, tb.y, tb.x), acc[z]);
-                            }
-                        } else {
-#pragma unroll
-                            for (int z = 0; z < TZ; ++z) {
-                                const float v = aZ[z] * U + cZ;
-                                const float fl = __fadd_rd(v, kMagic);
-                                const float fv = v - (fl - kMagic);
-                                const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
-                                const float2 tb = coef_eval<V2>(cb_tile[o], fu2);
-                                const float w = (v >= 0.f && v <= Hm1) ? U2 : 0.f;
-                                acc[z] = fmaf(w, fmaf(fv, tb.y, tb.x), acc[z]);
-                            }
-                        }
                     }
                 } else {
                     atomicOr(P.err, ERR_BOX_OVERFLOW);
                 }
             }
         }
-        if constexpr (!S::kCoef) {
-            __syncthreads();  // every thread is done with stage s
-            if (s_abort) break;
-            if (tid == 0 && b + STAGES < P.N) {
-                mbar_arrive_expect_tx(&full[s], stage_bytes);
-                tma_load_3d(stages + (size_t)s * P.stage_elems, &tmap, boxo[b + STAGES].x, boxo[b + STAGES].y,
-                            b + STAGES, &full[s]);
-            }
+        __syncthreads();  // every thread is done with stage s
+        if (s_abort) break;
+        if (tid == 0 && b + STAGES < P.N) {
+            mbar_arrive_expect_tx(&full[s], stage_bytes);
+            tma_load_3d(stages + (size_t)s * P.stage_elems, &tmap, boxo[b + STAGES].x, boxo[b + STAGES].y,
+                        b + STAGES, &full[s]);
         }
     }
 
@@ -404,99 +267,110 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 }
 
 // ---------------------------------------------------------------------------
-// Coefficient-pipeline backprojector.
+// Coefficient-image backprojector.
 //
-// Every staged tile is expanded once into bilinear coefficients, so that an
-// update needs one shared load and four FMAs:
-//   FP32 storage:      float4 (Q, dU, dV, dUV)            LDS.128
-//   FP16/BF16 storage: uint2  {(Q, dV), (dU, dUV)} pairs   LDS.64 + HFMA2
-// The expansion of tile b+1 overlaps the updates of tile b: threads arrive on
-// the tile's mbarrier after expanding their share, update from tile b, and
-// only then wait for tile b+1, so no CTA-wide barrier stalls the loop.  Three
-// coefficient buffers make the reuse safe: a thread may only expand tile b+1
-// after passing the wait on tile b, and every thread arrives on tile b only
-// after finishing its updates of tile b-2.
+// The filter writes each projection as an image of bilinear coefficient
+// entries (see tk_precision): entry (r, c) covers the detector cell
+// [r, r+1] x [c, c+1], so an update is one shared load of one entry and
+//   A = Q + fu dU,  B = dV + fu dUV,  acc += U^2 (A + fv B)
+// (FP16/BF16: A and B come from one packed HFMA2).  The staged box holds
+// entries, one row/column smaller than a sample box.  v is walked linearly,
+// v_z = v0 + z dv with dv = scale * U, which frees the per-slice registers
+// for a 64-voxel z column.  Loads use 32-bit shared addresses (inline PTX)
+// so the address of an update is one IMAD.
 
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+template <int PREC> struct Cimg;
+template <> struct Cimg<TK_F32_COEF> {
+    static constexpr int kBytes = 16, kAlign = 1;
+    static __device__ __forceinline__ float2 eval(uint32_t addr, float fu, float2)
+    {
+        float q, du, dv, duv;
+        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(q), "=f"(du), "=f"(dv), "=f"(duv) : "r"(addr));
+        return make_float2(fmaf(fu, du, q), fmaf(fu, duv, dv));
+    }
+};
+template <> struct Cimg<TK_F16> {
+    static constexpr int kBytes = 8, kAlign = 2;
+    static __device__ __forceinline__ float2 eval(uint32_t addr, float, float2 fu2raw)
+    {
+        uint32_t lo, hi;
+        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(lo), "=r"(hi) : "r"(addr));
+        const __half2 h = __hfma2(*reinterpret_cast<const __half2 *>(&hi),
+                                  *reinterpret_cast<const __half2 *>(&fu2raw.x),
+                                  *reinterpret_cast<const __half2 *>(&lo));
+        return __half22float2(h);
+    }
+};
+template <> struct Cimg<TK_BF16> {
+    static constexpr int kBytes = 8, kAlign = 2;
+    static __device__ __forceinline__ float2 eval(uint32_t addr, float, float2 fu2raw)
+    {
+        uint32_t lo, hi;
+        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(lo), "=r"(hi) : "r"(addr));
+        const __nv_bfloat162 h = __hfma2(*reinterpret_cast<const __nv_bfloat162 *>(&hi),
+                                         *reinterpret_cast<const __nv_bfloat162 *>(&fu2raw.x),
+                                         *reinterpret_cast<const __nv_bfloat162 *>(&lo));
+        return __bfloat1622float2(h);
+    }
+};
+
+// fu packed for the 16-bit HFMA2 (carried in the bits of a float2.x).
+template <int PREC> __device__ __forceinline__ float2 pack_fu(float fu)
 {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+    float2 r = make_float2(0.f, 0.f);
+    if constexpr (PREC == TK_F16) {
+        const __half2 h = __float2half2_rn(fu);
+        r.x = *reinterpret_cast<const float *>(&h);
+    } else if constexpr (PREC == TK_BF16) {
+        const __nv_bfloat162 h = __float2bfloat162_rn(fu);
+        r.x = *reinterpret_cast<const float *>(&h);
+    }
+    return r;
 }
 
-template <typename S> struct CoefOf;
-template <> struct CoefOf<StoreF32> { using E = float4; };
-template <> struct CoefOf<StoreF16> { using E = uint2; };
-template <> struct CoefOf<StoreBF16> { using E = uint2; };
-
-// FP32 tile [BH][BW] -> float4 coefficients [BH-1][BW] (column BW-1 unused).
-// Work item = (quad of columns, band of rows); walking down the band reuses
-// the previous raw row.  The fifth column of the last quad is read one
-// element past the row (the next row or the stage padding) and only feeds
-// the unused last column.
-template <int NT>
-__device__ __forceinline__ void expand_f32(const float *__restrict__ raw, float4 *__restrict__ coef, int BW, int BH,
-                                           int tid)
+// Bounding-box origin (entries) of a tile's footprint; the z range is
+// [z0, z1] in slab slices.
+template <int TX, int TY, int ALIGN>
+__device__ __forceinline__ int2 footprint_origin_z(const BPParams &P, int b, int x0, int y0, int z0, int z1)
 {
-    constexpr int kBand = 4;
-    const int nq = BW >> 2;
-    const int nrows = BH - 1;
-    const int nbands = (nrows + kBand - 1) / kBand;
-    for (int item = tid; item < nq * nbands; item += NT) {
-        const int cq = item % nq, band = item / nq;
-        const int r0 = band * kBand, r1 = min(r0 + kBand, nrows);
-        const int c0 = cq << 2;
-        float4 a = *reinterpret_cast<const float4 *>(raw + r0 * BW + c0);
-        float a4 = raw[r0 * BW + c0 + 4];
-        float4 dA = make_float4(a.y - a.x, a.z - a.y, a.w - a.z, a4 - a.w);
-        for (int r = r0; r < r1; ++r) {
-            const float4 b = *reinterpret_cast<const float4 *>(raw + (r + 1) * BW + c0);
-            const float b4 = raw[(r + 1) * BW + c0 + 4];
-            const float4 dB = make_float4(b.y - b.x, b.z - b.y, b.w - b.z, b4 - b.w);
-            float4 *o = coef + r * BW + c0;
-            o[0] = make_float4(a.x, dA.x, b.x - a.x, dB.x - dA.x);
-            o[1] = make_float4(a.y, dA.y, b.y - a.y, dB.y - dA.y);
-            o[2] = make_float4(a.z, dA.z, b.z - a.z, dB.z - dA.z);
-            o[3] = make_float4(a.w, dA.w, b.w - a.w, dB.w - dA.w);
-            a = b;
-            dA = dB;
+    const float2 cs = P.trig[b];
+    const int xs[2] = {x0, min(x0 + TX - 1, P.X - 1)};
+    const int ys[2] = {y0, min(y0 + TY - 1, P.Y - 1)};
+    const float aZ0 = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
+    const float aZ1 = flip(P.scale * ((float)z1 + P.zoff), P.dirz);
+    float umin = 3.0e38f, vmin = 3.0e38f;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float aX = flip(P.scale * ((float)xs[i] + P.dX), P.dirx);
+            const float aY = flip(P.scale * ((float)ys[j] + P.dY), P.diry);
+            const float S = aX * cs.x + aY * cs.y;
+            const float T = aY * cs.x - aX * cs.y;
+            const float U = P.D / (P.D - S);
+            umin = fminf(umin, T * U + P.cX);
+            vmin = fminf(vmin, fminf(aZ0 * U + P.cZ, aZ1 * U + P.cZ));
         }
     }
+    int bx = (int)floorf(umin) - 1;
+    bx &= ~(ALIGN - 1);
+    return make_int2(bx, (int)floorf(vmin) - 1);
 }
 
-template <typename S, int NT>
-__device__ __forceinline__ void expand_any(const typename S::T *raw, typename CoefOf<S>::E *coef, int BW, int BH,
-                                           int tid)
+template <int PREC, int TZ, bool ALL_IN, bool PARTIAL>
+__device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu,
+                                            float U2, float Hm1, int zlast, float (&acc)[TZ])
 {
-    if constexpr (S::kCoef)
-        expand_tile<typename S::T, typename Vec2Of<S>::type, NT>(raw, coef, BW, BH, tid);
-    else
-        expand_f32<NT>(raw, coef, BW, BH, tid);
-}
-
-template <typename S, int TZ, bool ALL_IN>
-__device__ __forceinline__ void update_column(const typename CoefOf<S>::E *__restrict__ cb, uint32_t cbase, uint32_t BW,
-                                              const float (&aZ)[TZ], float (&acc)[TZ], float U, float U2, float fu,
-                                              float cZ, float Hm1)
-{
-    using V2 = typename Vec2Of<S>::type;
-    [[maybe_unused]] V2 fu2;
-    if constexpr (S::kCoef) fu2 = splat<V2>(fu);
+    const float2 fu2 = pack_fu<PREC>(fu);
 #pragma unroll
     for (int z = 0; z < TZ; ++z) {
-        const float v = aZ[z] * U + cZ;
+        if (PARTIAL && z > zlast) break;
+        const float v = fmaf((float)z, dv, v0);
         const float fl = __fadd_rd(v, kMagic);
         const float fv = v - (fl - kMagic);
-        const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
-        float A, B;
-        if constexpr (S::kCoef) {
-            const float2 ab = coef_eval<V2>(cb[o], fu2);
-            A = ab.x;
-            B = ab.y;
-        } else {
-            const float4 c = cb[o];
-            A = fmaf(fu, c.y, c.x);
-            B = fmaf(fu, c.w, c.z);
-        }
-        const float val = fmaf(fv, B, A);
+        const uint32_t addr = (uint32_t)__float_as_int(fl) * row_bytes + sbase;
+        const float2 ab = Cimg<PREC>::eval(addr, fu, fu2);
+        const float val = fmaf(fv, ab.y, ab.x);
         if constexpr (ALL_IN) {
             acc[z] = fmaf(U2, val, acc[z]);
         } else {
@@ -506,25 +380,25 @@ __device__ __forceinline__ void update_column(const typename CoefOf<S>::E *__res
     }
 }
 
-template <typename S, int TX, int TY, int TZ, int RS, int MINB>
-__global__ void __launch_bounds__(TX *TY, MINB)
-    bp_coef_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
+template <int PREC, int TX, int TY, int TZ, int STAGES, bool PARTIAL>
+__global__ void __launch_bounds__(TX *TY, 2)
+    bp_cimg_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
-    using T = typename S::T;
-    using E = typename CoefOf<S>::E;
     constexpr int NT = TX * TY;
-    constexpr int NC = 3;
+    constexpr int ES = Cimg<PREC>::kBytes;
     extern __shared__ __align__(128) unsigned char smem[];
-    T *raw = reinterpret_cast<T *>(smem);
-    E *coef = reinterpret_cast<E *>(smem + (size_t)RS * P.stage_elems * sizeof(T));
-    int2 *boxo = reinterpret_cast<int2 *>(coef + (size_t)NC * P.coef_stride);
-    uint64_t *rfull = reinterpret_cast<uint64_t *>(boxo + P.N);
-    uint64_t *cfull = rfull + RS;
+    int2 *boxo = reinterpret_cast<int2 *>(smem + (size_t)STAGES * P.stage_elems * ES);
+    uint64_t *full = reinterpret_cast<uint64_t *>(boxo + P.N);
+    volatile int &s_abort = *reinterpret_cast<int *>(full + STAGES);
 
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX;
     const int x0 = (blockIdx.x % P.tilesX) * TX, y0 = (blockIdx.x / P.tilesX) * TY;
-    const int z0 = blockIdx.y * TZ;
+    // Full chunks: the last one is moved down to end at nz and stores only
+    // the slices no earlier chunk owns.  PARTIAL handles nz < TZ.
+    const int zc = blockIdx.y * TZ;
+    const int z0 = PARTIAL ? zc : min(zc, P.nz - TZ);
+    const int zlast = PARTIAL ? P.nz - 1 - z0 : TZ - 1;
     const int x = x0 + tx, y = y0 + ty;
     const float aX = flip(P.scale * ((float)x + P.dX), P.dirx);
     const float aY = flip(P.scale * ((float)y + P.dY), P.diry);
@@ -533,7 +407,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 
     if (!__syncthreads_or(active)) {  // tile entirely outside the FOV cylinder
         if (inside) {
-            for (int z = 0; z < TZ && z0 + z < P.nz; ++z) {
+            for (int z = max(zc - z0, 0); z <= zlast; ++z) {
                 float *dst = P.vol + (size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x;
                 *dst = P.accumulate ? 0.f + *dst : 0.f;
             }
@@ -541,53 +415,42 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         return;
     }
 
-    for (int b = tid; b < P.N; b += NT) boxo[b] = footprint_origin<TX, TY, TZ, S::kAlign>(P, b, x0, y0, z0);
+    for (int b = tid; b < P.N; b += NT) boxo[b] = footprint_origin_z<TX, TY, Cimg<PREC>::kAlign>(P, b, x0, y0, z0, z0 + zlast);
     if (tid == 0) {
-        for (int s = 0; s < RS; ++s) mbar_init(&rfull[s], 1);
-        for (int k = 0; k < NC; ++k) mbar_init(&cfull[k], NT);
+        s_abort = 0;
+        for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
         fence_mbar_init();
         prefetch_tensormap(&tmap);
     }
     __syncthreads();
-    const uint32_t stage_bytes = (uint32_t)(P.BW * P.BH * sizeof(T));
-    int issued = 0;  // raw tiles requested (meaningful in thread 0)
-    auto issue = [&](int tile) {
-        const int s = tile % RS;
-        mbar_arrive_expect_tx(&rfull[s], stage_bytes);
-        tma_load_3d(raw + (size_t)s * P.stage_elems, &tmap, boxo[tile].x, boxo[tile].y, tile, &rfull[s]);
-        issued = tile + 1;
-    };
-    if (tid == 0)
-        for (int t = 0; t < RS && t < P.N; ++t) issue(t);
+    const uint32_t stage_bytes = (uint32_t)(P.BW * P.BH * ES);
+    const uint32_t smem0 = smem_u32(smem);
+    // the tensor map's innermost dimension counts floats: ES/4 per entry
+    if (tid == 0) {
+        for (int s = 0; s < STAGES && s < P.N; ++s) {
+            mbar_arrive_expect_tx(&full[s], stage_bytes);
+            tma_load_3d(smem + (size_t)s * P.stage_elems * ES, &tmap, boxo[s].x * (ES / 4), boxo[s].y, s, &full[s]);
+        }
+    }
 
-    // Slices past the end of the slab repeat the last one (see the note in
-    // bp_tma_kernel): their footprint stays inside the staged box.
-    float aZ[TZ];
-#pragma unroll
-    for (int z = 0; z < TZ; ++z) aZ[z] = flip(P.scale * ((float)min(z0 + z, P.nz - 1) + P.zoff), P.dirz);
+    const float aZ0 = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
+    const float daZ = flip(P.scale, P.dirz);
     float acc[TZ];
 #pragma unroll
     for (int z = 0; z < TZ; ++z) acc[z] = 0.f;
 
-    bool ok = mbar_wait_bounded(&rfull[0], 0u, kWaitLimitNs);
-    int consumed = 1;
-    if (ok) expand_any<S, NT>(raw, coef, P.BW, P.BH, tid);
-    mbar_arrive(&cfull[0]);
-    ok = ok && mbar_wait_bounded(&cfull[0], 0u, kWaitLimitNs);
-    if (tid == 0 && ok && RS < P.N) issue(RS);
-
     const float cZ = P.cZ, Hm1 = P.Hm1;
-    const uint32_t BW = (uint32_t)P.BW;
-    for (int b = 0; b < P.N && ok; ++b) {
-        const int nb = b + 1;
-        if (nb < P.N) {
-            ok = mbar_wait_bounded(&rfull[nb % RS], (uint32_t)(nb / RS) & 1u, kWaitLimitNs);
-            consumed = nb + 1;
-            if (ok) expand_any<S, NT>(raw + (size_t)(nb % RS) * P.stage_elems, coef + (size_t)(nb % NC) * P.coef_stride,
-                                      P.BW, P.BH, tid);
-            mbar_arrive(&cfull[nb % NC]);
+    const uint32_t row_bytes = (uint32_t)P.BW * ES;
+    int b = 0;
+    for (; b < P.N; ++b) {
+        const int s = b % STAGES;
+        const uint32_t parity = (uint32_t)(b / STAGES) & 1u;
+        const bool got = mbar_wait_bounded(&full[s], parity, kWaitLimitNs);
+        if (!got) {
+            atomicOr(P.err, ERR_WAIT_TIMEOUT);
+            s_abort = 1;
         }
-        if (active && ok) {
+        if (active && got) {
             const float2 cs = P.trig[b];
             const float Sd = aX * cs.x + aY * cs.y;
             const float Td = aY * cs.x - aX * cs.y;
@@ -595,38 +458,43 @@ __global__ void __launch_bounds__(TX *TY, MINB)
             const float u = Td * U + P.cX;
             if (u >= 0.f && u <= P.Wm1) {  // column inside the detector (kernel.cu:127-128)
                 const int bx0 = boxo[b].x, by0 = boxo[b].y;
-                const float U2 = U * U;
                 const float fla = __fadd_rd(u, kMagic);
                 const int col = __float_as_int(fla) - kMagicBits - bx0;
                 const float fu = u - (fla - kMagic);
-                const float vA = aZ[0] * U + cZ, vB = aZ[TZ - 1] * U + cZ;
-                const float vlo = fminf(vA, vB), vhi = fmaxf(vA, vB);
-                const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) + 1 - by0;
-                if (col >= 0 && col + 1 < P.BW && rlo >= 0 && rhi < P.BH) {
-                    const uint32_t cbase = (uint32_t)col - (uint32_t)(kMagicBits + by0) * BW;
-                    const E *cb = coef + (size_t)(b % NC) * P.coef_stride;
+                const float v0 = aZ0 * U + cZ;
+                const float dv = daZ * U;
+                const float vL = fmaf((float)zlast, dv, v0);
+                const float vlo = fminf(v0, vL), vhi = fmaxf(v0, vL);
+                const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) - by0;
+                if (col >= 0 && col < P.BW && rlo >= 0 && rhi < P.BH) {
+                    const uint32_t sbase = smem0 + (uint32_t)s * P.stage_elems * ES + (uint32_t)col * ES -
+                                           (uint32_t)(kMagicBits + by0) * row_bytes;
+                    const float U2 = U * U;
                     if (vlo >= 0.f && vhi <= Hm1)
-                        update_column<S, TZ, true>(cb, cbase, BW, aZ, acc, U, U2, fu, cZ, Hm1);
+                        update_cimg<PREC, TZ, true, PARTIAL>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                     else
-                        update_column<S, TZ, false>(cb, cbase, BW, aZ, acc, U, U2, fu, cZ, Hm1);
+                        update_cimg<PREC, TZ, false, PARTIAL>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                 } else {
                     atomicOr(P.err, ERR_BOX_OVERFLOW);
                 }
             }
         }
-        if (nb < P.N && ok) {
-            ok = mbar_wait_bounded(&cfull[nb % NC], (uint32_t)(nb / NC) & 1u, kWaitLimitNs);
-            // every thread has expanded tile nb: its raw stage is free again
-            if (tid == 0 && ok && nb + RS < P.N) issue(nb + RS);
+        __syncthreads();  // every thread is done with stage s
+        if (s_abort) break;
+        if (tid == 0 && b + STAGES < P.N) {
+            mbar_arrive_expect_tx(&full[s], stage_bytes);
+            tma_load_3d(smem + (size_t)s * P.stage_elems * ES, &tmap, boxo[b + STAGES].x * (ES / 4),
+                        boxo[b + STAGES].y, b + STAGES, &full[s]);
         }
     }
 
-    if (!ok) {
-        atomicOr(P.err, ERR_WAIT_TIMEOUT);
-        // Leave no copy in flight into shared memory this CTA gives back.
-        if (tid == 0)
-            for (int k = consumed; k < issued; ++k)
-                mbar_wait_bounded(&rfull[k % RS], (uint32_t)(k / RS) & 1u, 100000000ull);
+    if (s_abort) {
+        if (tid == 0) {
+            const int issued = min(P.N, b + STAGES);
+            for (int k = b; k < issued; ++k)
+                mbar_wait_bounded(&full[k % STAGES], (uint32_t)(k / STAGES) & 1u, 100000000ull);
+        }
+        __syncthreads();
         return;
     }
 
@@ -634,7 +502,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         const float fs = P.q_scale ? P.fscale / *P.q_scale : P.fscale;
 #pragma unroll
         for (int z = 0; z < TZ; ++z) {
-            if (z0 + z < P.nz) {
+            if (z <= zlast && z0 + z >= zc) {
                 float r = 0.f;
                 if (active) r = acc[z] * fs;
                 float *dst = P.vol + (size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x;
@@ -663,25 +531,28 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
 
 struct BPVariant {
     const void *fn;
+    const void *fn_partial;  // nz < TZ (coefficient kernels only)
     int precision, TX, TY, TZ, STAGES;
-    bool coef;  // coefficient pipeline (bp_coef_kernel) or direct FP32 gathers (bp_tma_kernel)
+    bool coef;  // coefficient image (bp_cimg_kernel) or raw FP32 samples (bp_tma_kernel)
     const char *name;
 };
 
-#define TK_BP_DIRECT(S, P, TX, TY, TZ, ST, MB) \
-    {reinterpret_cast<const void *>(&bp_tma_kernel<S, TX, TY, TZ, ST, MB>), P, TX, TY, TZ, ST, false, \
-     "direct<" #S "," #TX "," #TY "," #TZ "," #ST ">"}
-#define TK_BP_COEF(S, P, TX, TY, TZ, ST, MB) \
-    {reinterpret_cast<const void *>(&bp_coef_kernel<S, TX, TY, TZ, ST, MB>), P, TX, TY, TZ, ST, true, \
-     "coef<" #S "," #TX "," #TY "," #TZ "," #ST ">"}
+#define TK_BP_DIRECT(TX, TY, TZ, ST) \
+    {reinterpret_cast<const void *>(&bp_tma_kernel<StoreF32, TX, TY, TZ, ST, 2>), nullptr, TK_F32, TX, TY, TZ, ST, \
+     false, "direct<f32," #TX "," #TY "," #TZ "," #ST ">"}
+#define TK_BP_CIMG(P, PN, TX, TY, TZ, ST) \
+    {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false>), \
+     reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true>), P, TX, TY, TZ, ST, true, \
+     "cimg<" PN "," #TX "," #TY "," #TZ "," #ST ">"}
 
-// The first entry of each precision is the default.
+// The first entry of each storage format is its default.
 static const BPVariant kVariants[] = {
-    TK_BP_COEF(StoreF32, TK_F32, 16, 16, 32, 3, 2),
-    TK_BP_COEF(StoreF16, TK_F16, 16, 16, 32, 3, 2),
-    TK_BP_COEF(StoreBF16, TK_BF16, 16, 16, 32, 3, 2),
-    TK_BP_DIRECT(StoreF32, TK_F32, 16, 16, 32, 4, 2),
-    TK_BP_DIRECT(StoreF16, TK_F16, 16, 16, 32, 4, 2),
+    TK_BP_DIRECT(16, 16, 32, 4),
+    TK_BP_CIMG(TK_F16, "f16", 16, 16, 64, 3),
+    TK_BP_CIMG(TK_BF16, "bf16", 16, 16, 64, 3),
+    TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3),
+    TK_BP_CIMG(TK_F16, "f16", 16, 16, 32, 4),
+    TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 64, 2),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
@@ -712,9 +583,13 @@ static int box_dims(const tk_geometry &g, int nz, float zoff, const BPVariant &v
     const double azmax = s * std::fmax(std::fabs((double)zoff), std::fabs((double)(nz - 1) + zoff)) + 1.0;
     const double du = dxy * Umax + R * dU * dxy;
     const double dv = s * (v.TZ - 1) * Umax + azmax * dU * dxy;
-    int bw = (int)std::floor(du) + 9 + align;
+    // Sample boxes need columns floor(umin)-1 .. floor(umax)+1 plus the rounding
+    // of the origin to the TMA granularity; coefficient entries cover a cell,
+    // so their box is one column and one row smaller.  One extra of each
+    // absorbs FP32-vs-FP64 differences of the device's corner evaluation.
+    int bw = (int)std::floor(du) + (v.coef ? 4 : 5) + align;
     bw = (bw + align - 1) / align * align;
-    int bh = (int)std::floor(dv) + 7;
+    int bh = (int)std::floor(dv) + (v.coef ? 5 : 7);
     TK_CHECK(bw <= 256 && bh <= 256, TK_ERR_UNSUPPORTED,
              "tile footprint %dx%d exceeds the 256x256 TMA box", bw, bh);
     *BW = bw;
@@ -728,16 +603,21 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     if (int rc = validate_geometry(&g)) return rc;
     TK_CHECK(d_q && d_vol, TK_ERR_INVALID, "backproject: null device pointer");
     TK_CHECK(nz >= 0, TK_ERR_INVALID, "backproject: nz < 0");
-    TK_CHECK(precision == TK_F32 || d_q_scale, TK_ERR_INVALID, "backproject: 16-bit storage needs its scale");
+    TK_CHECK(valid_precision(precision), TK_ERR_INVALID, "backproject: unknown precision %d", precision);
+    TK_CHECK((precision != TK_F16 && precision != TK_BF16) || d_q_scale, TK_ERR_INVALID,
+             "backproject: 16-bit storage needs its scale");
     if (nz == 0) return TK_OK;
     const BPVariant *v = pick_variant(precision);
     TK_CHECK(v, TK_ERR_INVALID, "backproject: unknown precision %d", precision);
     auto encode = get_encode_fn();
     TK_CHECK(encode, TK_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
 
-    const int align = precision == TK_F32 ? 4 : 8;
+    // TMA x-coordinate granularity in entries: 16 bytes
+    const int ES = (int)entry_size(precision);
+    const int align = v->coef ? (ES >= 16 ? 1 : 16 / ES) : 4;
     int BW, BH;
     if (int rc = box_dims(g, nz, zoff, *v, align, &BW, &BH)) return rc;
+    TK_CHECK(!v->coef || BW * ES / 4 <= 256, TK_ERR_UNSUPPORTED, "tile footprint of %d entries too wide", BW);
 
     std::vector<float> cs(g.N), sn(g.N);
     build_trig(g, cs.data(), sn.data());
@@ -748,8 +628,7 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     TK_CHECK((long long)tilesX * tilesY < (1ll << 31) && zchunks < 65536, TK_ERR_UNSUPPORTED,
              "volume too large for one launch");
 
-    const size_t esz = elem_size(precision);
-    const int Wp = row_pitch(g.W);
+    const int pitch = storage_pitch(g.W, precision);
     static thread_local BPParams P;  // ~26 KB: keep off the stack
     std::memset(&P, 0, sizeof(P));
     P.err = device_error_word();
@@ -761,8 +640,8 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     P.nz = nz;
     P.BW = BW;
     P.BH = BH;
-    P.stage_elems = (BW * BH + 63) / 64 * 64;  // 128-byte aligned stages for any element size
-    P.coef_stride = (BW * (BH - 1) + 15) / 16 * 16;
+    P.stage_elems = v->coef ? (BW * BH + 15) / 16 * 16   // 128-byte aligned stages
+                            : (BW * BH + 63) / 64 * 64;
     P.tilesX = tilesX;
     P.accumulate = accumulate ? 1 : 0;
     P.cX = g.cX;
@@ -780,40 +659,37 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     P.halfW = g.W / 2.;
     // result *= delta_f * scaling, with scaling = 1/p (kernel.cu:113, 575)
     P.fscale = g.dfi * (1.f / (float)p);
-    P.q_scale = d_q_scale;
+    P.q_scale = (precision == TK_F16 || precision == TK_BF16) ? d_q_scale : nullptr;
 
+    const bool partial = v->coef && nz < v->TZ;
+    const void *fn = partial ? v->fn_partial : v->fn;
     for (int b0 = 0; b0 < g.N; b0 += kMaxParamProj) {
         const int nb = std::min(kMaxParamProj, g.N - b0);
         P.N = nb;
         for (int b = 0; b < nb; ++b) P.trig[b] = make_float2(cs[b0 + b], sn[b0 + b]);
         P.accumulate = (accumulate || b0 > 0) ? 1 : 0;
 
+        // Samples are FP32 elements; coefficient entries are viewed as ES/4 floats.
+        const int fpe = v->coef ? ES / 4 : 1;
         CUtensorMap tmap;
-        const char *base = static_cast<const char *>(d_q) + (size_t)b0 * g.H * Wp * esz;
-        cuuint64_t dims[3] = {(cuuint64_t)g.W, (cuuint64_t)g.H, (cuuint64_t)nb};
-        cuuint64_t strides[2] = {(cuuint64_t)Wp * esz, (cuuint64_t)Wp * g.H * esz};
-        cuuint32_t box[3] = {(cuuint32_t)BW, (cuuint32_t)BH, 1};
+        const char *base = static_cast<const char *>(d_q) + (size_t)b0 * g.H * pitch * ES;
+        cuuint64_t dims[3] = {(cuuint64_t)g.W * fpe, (cuuint64_t)g.H, (cuuint64_t)nb};
+        cuuint64_t strides[2] = {(cuuint64_t)pitch * ES, (cuuint64_t)pitch * g.H * ES};
+        cuuint32_t box[3] = {(cuuint32_t)(BW * fpe), (cuuint32_t)BH, 1};
         cuuint32_t estr[3] = {1, 1, 1};
-        CUtensorMapDataType dt = precision == TK_F32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
-                                 : precision == TK_F16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
-                                                       : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-        CUresult cr = encode(&tmap, dt, 3, const_cast<char *>(base), dims, strides, box, estr,
-                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        CUresult cr = encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<char *>(base), dims, strides, box,
+                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
 
-        size_t smem = (size_t)v->STAGES * P.stage_elems * esz;
-        if (v->coef)
-            smem += 3 * (size_t)P.coef_stride * (precision == TK_F32 ? sizeof(float4) : sizeof(uint2));
-        else if (precision != TK_F32)
-            smem += 2 * (size_t)P.coef_stride * sizeof(uint2);
-        smem += (size_t)nb * sizeof(int2) + (size_t)(v->STAGES + 3) * sizeof(uint64_t) + 16;
+        size_t smem = (size_t)v->STAGES * P.stage_elems * ES;
+        smem += (size_t)nb * sizeof(int2) + (size_t)v->STAGES * sizeof(uint64_t) + 16;
         TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "backproject: %zu B of shared memory needed", smem);
-        TK_CUDA(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        dim3 grid((unsigned)(tilesX * tilesY), (unsigned)zchunks, 1);
+        TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        dim3 grid((unsigned)(tilesX * tilesY), partial ? 1u : (unsigned)zchunks, 1);
         dim3 block((unsigned)(v->TX * v->TY), 1, 1);
         void *args[] = {&tmap, &P};
-        TK_CUDA(cudaLaunchKernel(v->fn, grid, block, args, smem, stream));
+        TK_CUDA(cudaLaunchKernel(fn, grid, block, args, smem, stream));
     }
     return TK_OK;
 }

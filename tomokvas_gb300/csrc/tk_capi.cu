@@ -162,9 +162,15 @@ extern "C" int tk_backproject(const tk_geometry *g, const void *d_q, int precisi
 
 static constexpr size_t kWsHeader = 256;
 
+extern "C" size_t tk_filtered_bytes(const tk_geometry *g, int precision)
+{
+    if (!g || !valid_precision(precision)) return 0;
+    return filtered_bytes(*g, precision);
+}
+
 extern "C" size_t tk_fdk_workspace_bytes(const tk_geometry *g, int precision)
 {
-    if (!g || precision < TK_F32 || precision > TK_BF16) return 0;
+    if (!g || !valid_precision(precision)) return 0;
     return kWsHeader + filtered_bytes(*g, precision);
 }
 
@@ -173,7 +179,7 @@ extern "C" int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_t
                              size_t workspace_bytes, float *d_vol, void *stream)
 {
     if (int rc = validate_geometry(g)) return rc;
-    TK_CHECK(precision >= TK_F32 && precision <= TK_BF16, TK_ERR_INVALID, "bad precision %d", precision);
+    TK_CHECK(valid_precision(precision), TK_ERR_INVALID, "bad precision %d", precision);
     const size_t need = tk_fdk_workspace_bytes(g, precision);
     TK_CHECK(d_workspace && workspace_bytes >= need, TK_ERR_INVALID, "workspace of %zu B needed, %zu given", need,
              workspace_bytes);
@@ -403,7 +409,7 @@ extern "C" int tk_fdk_set_filter(tk_fdk *h, int window)
 extern "C" int tk_fdk_set_precision(tk_fdk *h, int precision)
 {
     TK_H(h);
-    TK_CHECK(precision >= TK_F32 && precision <= TK_BF16, TK_ERR_INVALID, "bad precision %d", precision);
+    TK_CHECK(valid_precision(precision), TK_ERR_INVALID, "bad precision %d", precision);
     h->precision = precision;
     h->filtered = false;
     return TK_OK;

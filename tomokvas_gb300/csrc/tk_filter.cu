@@ -46,6 +46,8 @@ struct FiltParams {
     const float *q_scale;  // device storage scale (16-bit) or null (= 1)
     long long nrows, npairs;
     int Wp, p, lg, precision;
+    int rc, nchunks;        // coefficient image: rows per work unit, units per projection
+    long long nunits;
     float Hf[kMaxHf];  // tau * |R2C_p(h)| * window, k = 0..p/2
 };
 
@@ -222,6 +224,153 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
     }
 }
 
+// ---------------------------------------------------------------------------
+// Filter straight into a bilinear coefficient image.
+//
+// A work unit is RC consecutive detector rows of one projection.  The group
+// filters the unit's rows two at a time (plus the first row of the next unit,
+// which the last coefficient row needs) and keeps the previous filtered row in
+// shared memory, so every coefficient row r is formed from filtered rows r
+// and r+1 without another pass over HBM.  Samples outside the detector are 0.
+
+template <int MODE> struct CoefStore;
+template <> struct CoefStore<TK_F32_COEF> {
+    static __device__ __forceinline__ void put(void *img, size_t idx, float Q, float dU, float dV, float dUV)
+    {
+        static_cast<float4 *>(img)[idx] = make_float4(Q, dU, dV, dUV);
+    }
+};
+template <> struct CoefStore<TK_F16> {
+    static __device__ __forceinline__ void put(void *img, size_t idx, float Q, float dU, float dV, float dUV)
+    {
+        const __half2 lo = __floats2half2_rn(Q, dV), hi = __floats2half2_rn(dU, dUV);
+        uint2 e;
+        e.x = *reinterpret_cast<const uint32_t *>(&lo);
+        e.y = *reinterpret_cast<const uint32_t *>(&hi);
+        static_cast<uint2 *>(img)[idx] = e;
+    }
+};
+template <> struct CoefStore<TK_BF16> {
+    static __device__ __forceinline__ void put(void *img, size_t idx, float Q, float dU, float dV, float dUV)
+    {
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(Q, dV), hi = __floats2bfloat162_rn(dU, dUV);
+        uint2 e;
+        e.x = *reinterpret_cast<const uint32_t *>(&lo);
+        e.y = *reinterpret_cast<const uint32_t *>(&hi);
+        static_cast<uint2 *>(img)[idx] = e;
+    }
+};
+
+// Row accessors over the FFT result (row a = Re * s, row b = -Im * s) and
+// the kept previous row; index W reads as 0.
+struct RowRe {
+    const float2 *q; float s; int W;
+    __device__ __forceinline__ float operator()(int c) const { return c < W ? q[c].x * s : 0.f; }
+};
+struct RowNegIm {
+    const float2 *q; float s; int W;
+    __device__ __forceinline__ float operator()(int c) const { return c < W ? -q[c].y * s : 0.f; }
+};
+struct RowBuf {
+    const float *q; int W;
+    __device__ __forceinline__ float operator()(int c) const { return c < W ? q[c] : 0.f; }
+};
+struct RowZero {
+    __device__ __forceinline__ float operator()(int) const { return 0.f; }
+};
+
+template <int MODE, typename RA, typename RB>
+__device__ __forceinline__ void emit_coef_row(void *img, size_t row_base, int W, int t, int TPF, RA a, RB b)
+{
+    for (int c = t; c < W; c += TPF) {
+        const float a0 = a(c), a1 = a(c + 1), b0 = b(c), b1 = b(c + 1);
+        const float dU = a1 - a0;
+        CoefStore<MODE>::put(img, row_base + c, a0, dU, b0 - a0, (b1 - b0) - dU);
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_constant__ FiltParams P)
+{
+    extern __shared__ __align__(16) float2 fsm[];
+    const int p = P.p;
+    const int TPF = min(kFiltThreads, p >> 2);
+    const int G = kFiltThreads / TPF;
+    const int grp = threadIdx.x / TPF, t = threadIdx.x - grp * TPF;
+    float2 *tw = fsm;
+    float2 *bufA = fsm + p + (size_t)grp * 3 * p;
+    float2 *bufB = bufA + p;
+    float *prev = reinterpret_cast<float *>(bufB + p);  // W floats
+    for (int k = threadIdx.x; k < p; k += kFiltThreads) {
+        float sn, cs;
+        sincospif(-2.0f * (float)k / (float)p, &sn, &cs);
+        tw[k] = make_float2(cs, sn);
+    }
+    const float sigma = P.q_scale ? *P.q_scale : 1.f;
+    const int W = P.L.W, H = P.L.H, RC = P.rc;
+    const int Wc = MODE == TK_F32_COEF ? W : ((W + 1) & ~1);
+    __syncthreads();
+
+    for (long long ug = blockIdx.x; ug * G < P.nunits; ug += gridDim.x) {
+        const long long unit = ug * G + grp;
+        const bool valid = unit < P.nunits;
+        const long long b = valid ? unit / P.nchunks : 0;
+        const int r0 = valid ? (int)(unit - b * P.nchunks) * RC : 0;
+        const int r1 = min(r0 + RC, H);         // coefficient rows [r0, r1)
+        const int rend = min(r0 + RC, H - 1);   // last filtered row (includes the next unit's first)
+        const int npair = valid ? (rend - r0 + 2) / 2 : 0;
+        // every group runs the same number of pair steps (CTA-wide barriers inside)
+        const int steps = (min(RC, H - 1) + 2) / 2;
+        for (int k = 0; k < steps; ++k) {
+            const bool live = valid && k < npair;
+            const int ra = r0 + 2 * k, rb = ra + 1;
+            const bool hasb = live && rb <= rend;
+            if (live) {
+                int rr;
+                const long long oa = in_row_offset(P.L, b * H + ra, rr);
+                const long long ob = hasb ? in_row_offset(P.L, b * H + rb, rr) : 0;
+                for (int x = t; x < p; x += TPF) {
+                    float va = 0.f, vb = 0.f;
+                    if (x < W) {
+                        va = load_pre(P.L, oa, ra, x);
+                        if (hasb) vb = load_pre(P.L, ob, rb, x);
+                    }
+                    bufA[x] = make_float2(va, vb);
+                }
+            }
+            __syncthreads();
+            float2 *R = fft_forward(bufA, bufB, tw, p, P.lg, t, TPF);
+            float2 *Sb = (R == bufA) ? bufB : bufA;
+            for (int kk = t; kk < p; kk += TPF) {
+                const float h = P.Hf[kk <= (p >> 1) ? kk : p - kk];
+                const float2 z = R[kk];
+                R[kk] = make_float2(z.x * h, -z.y * h);
+            }
+            __syncthreads();
+            const float2 *Q = fft_forward(R, Sb, tw, p, P.lg, t, TPF);
+            if (live) {
+                const size_t base = (size_t)b * H;
+                const RowRe rowa{Q, sigma, W};
+                const RowNegIm rowb{Q, sigma, W};
+                if (ra - 1 >= r0)  // prev = row ra-1, next = row ra
+                    emit_coef_row<MODE>(P.out, (base + ra - 1) * Wc, W, t, TPF, RowBuf{prev, W}, rowa);
+                if (ra < r1) {
+                    if (hasb)
+                        emit_coef_row<MODE>(P.out, (base + ra) * Wc, W, t, TPF, rowa, rowb);
+                    else  // row ra is the detector's last row
+                        emit_coef_row<MODE>(P.out, (base + ra) * Wc, W, t, TPF, rowa, RowZero{});
+                }
+                if (hasb && rb < r1 && rb == rend)  // detector's last row, nothing follows
+                    emit_coef_row<MODE>(P.out, (base + rb) * Wc, W, t, TPF, rowb, RowZero{});
+            }
+            __syncthreads();
+            if (live && hasb)
+                for (int c = t; c < W; c += TPF) prev[c] = -Q[c].y * sigma;
+            __syncthreads();
+        }
+    }
+}
+
 // max |preprocessed sample| over the whole input, as float bits in *maxbits.
 __global__ void __launch_bounds__(256) prescan_kernel(const __grid_constant__ LoadParams L, long long nrows,
                                                       unsigned *maxbits)
@@ -333,12 +482,17 @@ static const Spectrum &spectrum(int W, float tau, int window, int p)
 
 static int launch_filter_typed(const FiltParams &P, int p, cudaStream_t stream, int precision)
 {
-    const void *fn = precision == TK_F32   ? reinterpret_cast<const void *>(&filter_fft_kernel<float>)
-                     : precision == TK_F16 ? reinterpret_cast<const void *>(&filter_fft_kernel<__half>)
-                                           : reinterpret_cast<const void *>(&filter_fft_kernel<__nv_bfloat16>);
+    const void *fn = nullptr;
+    size_t per_group = 2;  // complex buffers of p per FFT group
+    switch (precision) {
+    case TK_F32: fn = reinterpret_cast<const void *>(&filter_fft_kernel<float>); break;
+    case TK_F16: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_F16>); per_group = 3; break;
+    case TK_BF16: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_BF16>); per_group = 3; break;
+    default: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_F32_COEF>); per_group = 3; break;
+    }
     const int TPF = std::min(kFiltThreads, p >> 2);
     const int G = kFiltThreads / TPF;
-    const size_t smem = (size_t)p * sizeof(float2) * (1 + 2 * (size_t)G);
+    const size_t smem = (size_t)p * sizeof(float2) * (1 + per_group * (size_t)G);
     TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "filter: pad length %d needs too much shared memory", p);
     TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, sms = 0, per_sm = 0;
@@ -346,7 +500,8 @@ static int launch_filter_typed(const FiltParams &P, int p, cudaStream_t stream, 
     TK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     TK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kFiltThreads, smem));
     if (per_sm < 1) per_sm = 1;
-    const long long groups = (P.npairs + G - 1) / G;
+    const long long work = is_coef(precision) ? P.nunits : P.npairs;
+    const long long groups = (work + G - 1) / G;
     const long long grid = std::min<long long>(groups, (long long)sms * per_sm);
     void *args[] = {const_cast<FiltParams *>(&P)};
     TK_CUDA(cudaLaunchKernel(fn, dim3((unsigned)std::max<long long>(grid, 1)), dim3(kFiltThreads), args, smem,
@@ -362,11 +517,14 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     TK_CHECK(input_type == TK_INPUT_F32 || input_type == TK_INPUT_U16, TK_ERR_INVALID, "filter: bad input type");
     TK_CHECK(layout == TK_LAYOUT_SINOGRAM || layout == TK_LAYOUT_PROJECTION, TK_ERR_INVALID, "filter: bad layout");
     TK_CHECK(window >= TK_WINDOW_RAMLAK && window <= TK_WINDOW_HANN, TK_ERR_INVALID, "filter: bad window");
-    TK_CHECK(precision >= TK_F32 && precision <= TK_BF16, TK_ERR_INVALID, "filter: bad precision");
-    TK_CHECK(precision == TK_F32 || d_q_scale, TK_ERR_INVALID, "filter: 16-bit storage needs d_q_scale");
+    TK_CHECK(valid_precision(precision), TK_ERR_INVALID, "filter: bad precision");
+    const bool sixteen = precision == TK_F16 || precision == TK_BF16;
+    TK_CHECK(!sixteen || d_q_scale, TK_ERR_INVALID, "filter: 16-bit storage needs d_q_scale");
     TK_CHECK(input_type == TK_INPUT_F32 || ff, TK_ERR_INVALID, "filter: raw input needs flat-field parameters");
     const int p = reference_pad_length(g.W);
     TK_CHECK(p <= 2 * (kMaxHf - 1), TK_ERR_UNSUPPORTED, "filter: W = %d exceeds the supported 4096", g.W);
+    TK_CHECK(!is_coef(precision) || p <= 4096, TK_ERR_UNSUPPORTED,
+             "filter: coefficient storage supports W <= 2048 (W = %d)", g.W);
 
     static thread_local FiltParams P;  // ~16 KB: keep off the stack
     std::memset(&P, 0, sizeof(P));
@@ -403,9 +561,12 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     while ((1 << lg) < p) ++lg;
     P.lg = lg;
     P.precision = precision;
+    P.rc = 64;
+    P.nchunks = (g.H + P.rc - 1) / P.rc;
+    P.nunits = (long long)g.N * P.nchunks;
     std::memcpy(P.Hf, sp.Hf.data(), sizeof(float) * sp.Hf.size());
 
-    if (precision == TK_F32) {
+    if (!sixteen) {
         P.q_scale = nullptr;
         if (d_q_scale) set_scale_kernel<<<1, 1, 0, stream>>>(d_q_scale, 1.f);
     } else {

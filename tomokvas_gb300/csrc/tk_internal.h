@@ -15,11 +15,22 @@ int cuda_fail(cudaError_t e, const char *what);
 // Row pitch (elements) of the device filtered-projection layout [N][H][Wp]:
 // rows start on 16-byte boundaries for every storage precision.
 inline int row_pitch(int W) { return (W + 7) & ~7; }
-inline size_t elem_size(int precision) { return precision == TK_F32 ? 4 : 2; }
+// Coefficient-image row pitch (entries): even, so rows start on 16 bytes.
+inline int coef_pitch(int W) { return (W + 1) & ~1; }
+inline bool is_coef(int precision) { return precision != TK_F32; }
+inline size_t entry_size(int precision)
+{
+    return precision == TK_F32 ? 4 : precision == TK_F32_COEF ? 16 : 8;
+}
+inline int storage_pitch(int W, int precision)
+{
+    return precision == TK_F32 ? row_pitch(W) : precision == TK_F32_COEF ? W : coef_pitch(W);
+}
 inline size_t filtered_bytes(const tk_geometry &g, int precision)
 {
-    return (size_t)g.N * (size_t)g.H * (size_t)row_pitch(g.W) * elem_size(precision);
+    return (size_t)g.N * (size_t)g.H * (size_t)storage_pitch(g.W, precision) * entry_size(precision);
 }
+inline bool valid_precision(int p) { return p >= TK_F32 && p <= TK_F32_COEF; }
 
 int validate_geometry(const tk_geometry *g);
 int reference_pad_length(int W);

@@ -34,9 +34,6 @@ def row_pitch(W: int) -> int:
     return (W + 7) & ~7
 
 
-_TDTYPE = {_lib.TK_F32: "float32", _lib.TK_F16: "float16", _lib.TK_BF16: "bfloat16"}
-
-
 def flatfield(flat=None, dark=None, flat_value=0.0, dark_value=0.0, A=1.0, B=0.0, invert=True, floor_counts=0.5):
     """tk_flatfield; flat/dark may be device tensors [H][W] (float32) or None."""
     ff = _lib.FlatField()
@@ -48,10 +45,19 @@ def flatfield(flat=None, dark=None, flat_value=0.0, dark_value=0.0, A=1.0, B=0.0
     return ff
 
 
+def filtered_bytes(g, precision=_lib.TK_F32) -> int:
+    gc = _geom(g)
+    return int(load().tk_filtered_bytes(ctypes.byref(gc), precision))
+
+
 def alloc_filtered(g, precision=_lib.TK_F32, device="cuda"):
+    """Device buffer for filtered projections in a storage format (see tk_precision)
+    and its storage-scale word."""
     torch = _torch()
-    dt = getattr(torch, _TDTYPE[precision])
-    q = torch.empty((g.N, g.H, row_pitch(g.W)), dtype=dt, device=device)
+    if precision == _lib.TK_F32:
+        q = torch.empty((g.N, g.H, row_pitch(g.W)), dtype=torch.float32, device=device)
+    else:
+        q = torch.empty(filtered_bytes(g, precision), dtype=torch.uint8, device=device)
     scale = torch.ones(1, dtype=torch.float32, device=device)
     return q, scale
 
