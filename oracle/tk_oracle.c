@@ -5,6 +5,11 @@
  * and bench.py's CPU-baseline leg use it.  The shipped library never links,
  * loads or calls it.
  *
+ * Parity unpinned: the reference ships no tests, fixtures or sample data,
+ * and its own code cannot be run where these tests run, so no reference
+ * output pins this restatement; tests/test_oracle.py pins it with closed-form
+ * consequences of the reference's code instead.
+ *
  * Every function below restates one step of the reference
  * (Lukas-kV/TomoKvas, FBPG/kernel.cu and FBPG/rsq_load.cpp); the reference
  * line each one follows is cited beside it.  Build with -ffp-contract=off so

@@ -11,6 +11,11 @@
  *             backprojection kernel.cu:68-177).
  *   - *_f64: the same discretisation in double precision (the FP64 oracle).
  *
+ * Parity unpinned: the reference ships no tests, fixtures or sample data,
+ * and its own code cannot be run where these tests run, so no reference
+ * output pins this restatement; tests/test_oracle.py pins it with closed-form
+ * consequences of the reference's code instead.
+ *
  * Sinogram layout is the reference's sinogram-major [H][N][W]
  * (detector row, angle, column), FBPG/mucat_file.cpp:244-249.
  * Volume layout is [z][y][x] float, FBPG/kernel.cu:116-117.
