@@ -161,6 +161,23 @@ int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_type, int la
                   const tk_flatfield *ff, int window, int precision,
                   void *d_workspace, size_t workspace_bytes, float *d_vol, void *stream);
 
+/* Whole FDK on device buffers for callers that cannot allocate device memory:
+ * a service that reserves a fixed device-memory budget at start-up and may
+ * not grow it, or code inside a callback or timing-critical loop where
+ * cudaMalloc's implicit device synchronisation and possible failure are not
+ * acceptable.  Same work and results as tk_fdk_device, but the workspace is a
+ * static device array of 64 MiB inside the library, so the problem must fit
+ * it: tk_fdk_workspace_bytes(g, precision) <= 64 MiB (for example 180
+ * projections of 256 x 256 in TK_F32); larger problems are rejected with
+ * TK_ERR_UNSUPPORTED and a message.  The caller still passes the input and
+ * the output volume.  Every GPU that loads the library holds the array until
+ * the process exits.  The first call on a device looks the array up (with
+ * that device current), so make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised.
+ * Allocates nothing.  No counterpart in the reference. */
+int tk_fdk_device_noalloc(const tk_geometry *g, const void *d_in, int input_type, int layout,
+                          const tk_flatfield *ff, int window, int precision, float *d_vol, void *stream);
+
 /* Backprojection kernel variants (tile shape, pipeline), for benchmarking
  * and the autotuner; no counterpart in the reference, whose launch shape is
  * fixed (kernel.cu:825-827).  tk_bp_select_variant(-1) restores the default

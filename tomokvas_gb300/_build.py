@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "libtk_fdk.so")
-SOURCES = ["tk_capi.cu", "tk_filter.cu", "tk_bp.cu", "tk_phantom.cu"]
+SOURCES = ["tk_capi.cu", "tk_filter.cu", "tk_bp.cu", "tk_phantom.cu", "tk_noalloc.cu"]
 HEADERS = ["tk_common.cuh", "tk_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
