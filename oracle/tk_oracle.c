@@ -5,10 +5,11 @@
  * and bench.py's CPU-baseline leg use it.  The shipped library never links,
  * loads or calls it.
  *
- * Parity unpinned: the reference ships no tests, fixtures or sample data,
- * and its own code cannot be run where these tests run, so no reference
- * output pins this restatement; tests/test_oracle.py pins it with closed-form
- * consequences of the reference's code instead.
+ * Pinned against the reference itself: tests/golden/ref_*.npz hold outputs of
+ * the reference's own FBPG/kernel.cu kernels with cuFFT on a GB300
+ * (oracle/ref_build.py, oracle/tk_refrun.cpp, tests/golden/make_golden.py);
+ * tests/test_golden_reference.py checks both restatements against them, and
+ * tests/test_oracle.py adds closed-form consequences of the reference's code.
  *
  * Every function below restates one step of the reference
  * (Lukas-kV/TomoKvas, FBPG/kernel.cu and FBPG/rsq_load.cpp); the reference

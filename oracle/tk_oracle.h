@@ -11,10 +11,11 @@
  *             backprojection kernel.cu:68-177).
  *   - *_f64: the same discretisation in double precision (the FP64 oracle).
  *
- * Parity unpinned: the reference ships no tests, fixtures or sample data,
- * and its own code cannot be run where these tests run, so no reference
- * output pins this restatement; tests/test_oracle.py pins it with closed-form
- * consequences of the reference's code instead.
+ * Pinned against the reference itself: tests/golden/ref_*.npz hold outputs of
+ * the reference's own FBPG/kernel.cu kernels with cuFFT on a GB300
+ * (oracle/ref_build.py, oracle/tk_refrun.cpp, tests/golden/make_golden.py);
+ * tests/test_golden_reference.py checks both restatements against them, and
+ * tests/test_oracle.py adds closed-form consequences of the reference's code.
  *
  * Sinogram layout is the reference's sinogram-major [H][N][W]
  * (detector row, angle, column), FBPG/mucat_file.cpp:244-249.

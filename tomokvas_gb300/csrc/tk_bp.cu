@@ -380,8 +380,8 @@ __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, 
     }
 }
 
-template <int PREC, int TX, int TY, int TZ, int STAGES, bool PARTIAL>
-__global__ void __launch_bounds__(TX *TY, 2)
+template <int PREC, int TX, int TY, int TZ, int STAGES, bool PARTIAL, int MINB>
+__global__ void __launch_bounds__(TX *TY, MINB)
     bp_cimg_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
     constexpr int NT = TX * TY;
@@ -540,19 +540,22 @@ struct BPVariant {
 #define TK_BP_DIRECT(TX, TY, TZ, ST) \
     {reinterpret_cast<const void *>(&bp_tma_kernel<StoreF32, TX, TY, TZ, ST, 2>), nullptr, TK_F32, TX, TY, TZ, ST, \
      false, "direct<f32," #TX "," #TY "," #TZ "," #ST ">"}
-#define TK_BP_CIMG(P, PN, TX, TY, TZ, ST) \
-    {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false>), \
-     reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true>), P, TX, TY, TZ, ST, true, \
-     "cimg<" PN "," #TX "," #TY "," #TZ "," #ST ">"}
+#define TK_BP_CIMG(P, PN, TX, TY, TZ, ST, MB) \
+    {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB>), \
+     reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB>), P, TX, TY, TZ, ST, true, \
+     "cimg<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
 // The first entry of each storage format is its default.
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT(16, 16, 32, 4),
-    TK_BP_CIMG(TK_F16, "f16", 16, 16, 64, 3),
-    TK_BP_CIMG(TK_BF16, "bf16", 16, 16, 64, 3),
-    TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3),
-    TK_BP_CIMG(TK_F16, "f16", 16, 16, 32, 4),
-    TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 64, 2),
+    TK_BP_CIMG(TK_F16, "f16", 16, 16, 64, 3, 2),
+    TK_BP_CIMG(TK_BF16, "bf16", 16, 16, 64, 3, 2),
+    TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
+    TK_BP_CIMG(TK_F16, "f16", 16, 16, 32, 3, 3),
+    TK_BP_CIMG(TK_F16, "f16", 32, 8, 64, 3, 2),
+    TK_BP_CIMG(TK_F16, "f16", 16, 16, 48, 3, 2),
+    TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
+    TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant

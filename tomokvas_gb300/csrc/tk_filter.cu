@@ -569,6 +569,16 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     if (!sixteen) {
         P.q_scale = nullptr;
         if (d_q_scale) set_scale_kernel<<<1, 1, 0, stream>>>(d_q_scale, 1.f);
+    } else if (input_type == TK_INPUT_U16 && !ff->dark && !ff->flat) {
+        // Scalar flat/dark: |A log(num/den) + B| is bounded without looking at the
+        // data, since num in [floor, 65535] and den = max(flat - dark, floor).
+        const double fl = ff->floor_counts, den = std::fmax((double)ff->flat_value - ff->dark_value, fl);
+        const double lg = std::fmax(std::fabs(std::log(fl / den)), std::fabs(std::log(65535.0 / fl)));
+        const double bound = (std::fabs((double)ff->A) * lg + std::fabs((double)ff->B)) * sp.L1K;
+        int e = bound > 0 ? (int)std::floor(std::log2((double)kScaleTarget / bound)) : 0;
+        e = std::max(-100, std::min(100, e));
+        set_scale_kernel<<<1, 1, 0, stream>>>(d_q_scale, (float)std::ldexp(1.0, e));
+        P.q_scale = d_q_scale;
     } else {
         TK_CUDA(cudaMemsetAsync(d_q_scale, 0, sizeof(float), stream));
         int dev = 0, sms = 0;
