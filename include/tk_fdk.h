@@ -161,6 +161,31 @@ int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_type, int la
                   const tk_flatfield *ff, int window, int precision,
                   void *d_workspace, size_t workspace_bytes, float *d_vol, void *stream);
 
+/* ------------------------------------------------ adjoint (differentiation)
+ * The FDK A = B F W is linear in the line integrals: W the cosine weight
+ * (diagonal), F the ramp filter (symmetric Toeplitz: its spectrum is real and
+ * even), B the backprojection.  Its transpose A^T = W F B^T gives gradients
+ * with respect to the projections.  No counterpart in the reference. */
+
+/* B^T: exact transpose of tk_backproject for TK_F32 storage (same masks,
+ * bilinear weights and scale dfi/p).  Scatters d_vol[nz][Y][X] (slices at
+ * aZ = scale*(z + zoff)) into d_qbar [N][H][Wp] FP32; accumulate = 0 clears
+ * d_qbar first.  FP32 atomics: results are deterministic to rounding only. */
+int tk_forward_project(const tk_geometry *g, const float *d_vol, int nz, float zoff, float *d_qbar,
+                       int accumulate, void *stream);
+/* (F W)^T = W F: filters d_qbar [N][H][Wp] with the ramp of `window` and
+ * multiplies by the cosine weight; writes d_pbar FP32 in `layout`. */
+int tk_filter_transpose(const tk_geometry *g, const float *d_qbar, int window, float *d_pbar, int layout,
+                        void *stream);
+/* A: line integrals (FP32, `layout`) -> volume [Z][Y][X]; tk_fdk_device with
+ * TK_F32 storage. */
+int tk_fdk_forward(const tk_geometry *g, const float *d_proj, int layout, int window, void *d_workspace,
+                   size_t workspace_bytes, float *d_vol, void *stream);
+/* A^T: volume gradient [Z][Y][X] -> gradient with respect to the line
+ * integrals (FP32, `layout`).  Workspace: tk_fdk_workspace_bytes(g, TK_F32). */
+int tk_fdk_backward(const tk_geometry *g, const float *d_vol_grad, int layout, int window, void *d_workspace,
+                    size_t workspace_bytes, float *d_proj_grad, void *stream);
+
 /* Whole FDK on device buffers for callers that cannot allocate device memory:
  * a service that reserves a fixed device-memory budget at start-up and may
  * not grow it, or code inside a callback or timing-critical loop where

@@ -89,6 +89,7 @@ def _declare(L):
     L.orc_bp_f64.argtypes = [f64p, gp, i32p, ctypes.c_int, f64p, ctypes.c_int, ctypes.c_int]
     L.orc_fdk_f64.argtypes = [f32p, gp, ctypes.c_int, i32p, ctypes.c_int, f64p, ctypes.c_int]
     L.orc_rows_needed.argtypes = [gp, i32p, ctypes.c_int, i32p, i32p]
+    L.orc_fdk_adjoint_f64.argtypes = [f32p, gp, ctypes.c_int, f64p, ctypes.c_int]
     d = ctypes.c_double
     L.orc_fdk_u16_f32_sampled.argtypes = [P(ctypes.c_uint16), d, d, d, d, ctypes.c_int, d, gp, ctypes.c_int,
                                           i32p, ctypes.c_int, f32p, ctypes.c_int]
@@ -183,6 +184,18 @@ def fdk_u16_f32_sampled(raw: np.ndarray, g: Geom, flat: float, dark: float = 0.0
     if rc:
         raise MemoryError("oracle fdk_u16_f32_sampled failed")
     return vol
+
+
+def fdk_adjoint_f64(vol: np.ndarray, g: Geom, window="ramlak", nthreads=0) -> np.ndarray:
+    """FP64 transpose of the FDK (volume [Z][Y][X] -> line-integral gradient [H][N][W])."""
+    v = np.ascontiguousarray(vol, dtype=np.float32)
+    assert v.shape == (g.Z, g.Y, g.X), v.shape
+    out = np.empty((g.H, g.N, g.W), dtype=np.float64)
+    win = WINDOWS[window] if isinstance(window, str) else int(window)
+    if lib().orc_fdk_adjoint_f64(_ptr(v, ctypes.c_float), ctypes.byref(g), win, _ptr(out, ctypes.c_double),
+                                 _threads(nthreads)):
+        raise MemoryError("oracle adjoint failed")
+    return out
 
 
 def rows_needed(g: Geom, zlist):

@@ -630,6 +630,110 @@ int orc_fdk_f64(const float *sino, const orc_geom *g, int window,
     return 0;
 }
 
+/* adjoint: scatter every voxel into the filtered-sample gradient, one
+ * projection per task (no races), then filter and weight each row */
+typedef struct {
+    const float *vol;
+    const orc_geom *g;
+    double *qbar; /* [N][H][W] */
+    const double *sn, *cs;
+} orc_adj_ctx;
+
+static void orc_adj_proj(void *vctx, long b)
+{
+    orc_adj_ctx *c = (orc_adj_ctx *)vctx;
+    const orc_geom *g = c->g;
+    double *q = c->qbar + (size_t)b * g->H * g->W;
+    double s = g->scale, D = g->D;
+    for (int z = 0; z < g->Z; ++z) {
+        double aZ = s * ((double)z - (g->Z - 1) / 2.0 - g->cz);
+        if (g->dirz) aZ = -aZ;
+        for (int y = 0; y < g->Y; ++y) {
+            double aY = s * ((double)y - g->cy);
+            if (g->diry) aY = -aY;
+            for (int x = 0; x < g->X; ++x) {
+                double aX = s * ((double)x - g->cx);
+                if (g->dirx) aX = -aX;
+                if (!(sqrt(aX * aX + aY * aY) < g->W / 2.0)) continue;
+                double val = c->vol[((size_t)z * g->Y + y) * g->X + x];
+                if (val == 0) continue;
+                double S = aX * c->cs[b] + aY * c->sn[b];
+                double T = aY * c->cs[b] - aX * c->sn[b];
+                double U = D / (D - S);
+                double u = T * U + g->cX, v = aZ * U + g->cZ;
+                if (u < 0 || u > g->W - 1 || v < 0 || v > g->H - 1) continue;
+                int a = (int)floor(u), r = (int)floor(v);
+                double fu = u - a, fv = v - r;
+                double w = (double)g->dfi * U * U * val;
+                int a1 = a + 1 < g->W ? a + 1 : a, r1 = r + 1 < g->H ? r + 1 : r;
+                q[(size_t)r * g->W + a] += w * (1 - fu) * (1 - fv);
+                q[(size_t)r * g->W + a1] += w * fu * (1 - fv);
+                q[(size_t)r1 * g->W + a] += w * (1 - fu) * fv;
+                q[(size_t)r1 * g->W + a1] += w * fu * fv;
+            }
+        }
+    }
+}
+
+typedef struct {
+    const double *qbar;
+    double *out;
+    const orc_geom *g;
+    const double *Hf, *tw;
+    int p;
+} orc_adjf_ctx;
+
+static void orc_adj_filter_row(void *vctx, long i)
+{
+    orc_adjf_ctx *c = (orc_adjf_ctx *)vctx;
+    const orc_geom *g = c->g;
+    int p = c->p, W = g->W;
+    int b = (int)(i / g->H), r = (int)(i % g->H);
+    double *re = (double *)malloc(sizeof(double) * 2 * (size_t)p);
+    double *im = re + p;
+    const double *src = c->qbar + (size_t)i * W;
+    for (int x = 0; x < p; ++x) { re[x] = x < W ? src[x] : 0; im[x] = 0; }
+    orc_fft_f64(re, im, p, c->tw, -1);
+    for (int k = 0; k < p; ++k) {
+        double h = c->Hf[k <= p / 2 ? k : p - k];
+        re[k] *= h;
+        im[k] *= h;
+    }
+    orc_fft_f64(re, im, p, c->tw, +1);
+    double D = g->D, cs = (double)r - g->cZ;
+    double *dst = c->out + ((size_t)r * g->N + b) * W;
+    for (int x = 0; x < W; ++x) {
+        double ce = (double)x - g->cX;
+        dst[x] = re[x] / (double)p * (D / sqrt(ce * ce + D * D + cs * cs));
+    }
+    free(re);
+}
+
+int orc_fdk_adjoint_f64(const float *vol, const orc_geom *g, int window, double *out, int nthreads)
+{
+    size_t nq = (size_t)g->N * g->H * g->W;
+    double *qbar = (double *)calloc(nq, sizeof(double));
+    double *sn = (double *)malloc(sizeof(double) * 2 * (size_t)g->N);
+    if (!qbar || !sn) { free(qbar); free(sn); return -1; }
+    double *cs = sn + g->N;
+    for (int b = 0; b < g->N; ++b) {
+        double a = orc_angle(g, b);
+        sn[b] = sin(a);
+        cs[b] = cos(a);
+    }
+    orc_adj_ctx c = {vol, g, qbar, sn, cs};
+    orc_parallel_for(g->N, nthreads, orc_adj_proj, &c);
+    int p = orc_pad_length(g->W);
+    double *Hf = (double *)malloc(sizeof(double) * (size_t)(p / 2 + 1));
+    double *tw = (double *)malloc(sizeof(double) * (size_t)p);
+    orc_spectrum_f64(g->W, g->tau, window, p, Hf);
+    orc_twiddles_f64(tw, p);
+    orc_adjf_ctx f = {qbar, out, g, Hf, tw, p};
+    orc_parallel_for((long)g->N * g->H, nthreads, orc_adj_filter_row, &f);
+    free(qbar); free(sn); free(Hf); free(tw);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* raw uint16 -> line integral (rsq::FlatFieldCorrection, rsq_load.cpp:299-325) */
 

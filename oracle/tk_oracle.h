@@ -94,6 +94,11 @@ void orc_bp_f64(const double *q64, const orc_geom *g, const int *zlist, int nz, 
                 int row_lo, int nthreads);
 int orc_fdk_f64(const float *sino, const orc_geom *g, int window,
                 const int *zlist, int nz, double *vol, int nthreads);
+/* FP64 adjoint of the FDK A = B F W (line integrals -> volume, exact slice
+ * centring): out = W F B^T vol, with B^T the transpose of the bilinear
+ * backprojection (same masks and weights) and F the symmetric ramp filter.
+ * vol [Z][Y][X], out [H][N][W] (double). */
+int orc_fdk_adjoint_f64(const float *vol, const orc_geom *g, int window, double *out, int nthreads);
 /* Detector rows [lo, hi] that slices zlist can touch (for sampled oracles). */
 void orc_rows_needed(const orc_geom *g, const int *zlist, int nz, int *lo, int *hi);
 

@@ -165,3 +165,16 @@ def test_u16_counts_roundtrip(orc, phantom_case):
     p = orc.log_u16(raw, np.float32(60000.0))
     # Poisson noise at I0 = 60000 is small relative to the line integrals
     assert np.sqrt(np.mean((p - sino) ** 2)) < 0.02
+
+
+def test_fp64_adjoint_is_exact_transpose(orc):
+    """<A x, y> = <x, A^T y> for the FP64 FDK and its FP64 adjoint."""
+    g = small_geometry(W=48, N=40, H=40, vol=(32, 32, 32), rot=0.2, dirx=1)
+    G = orc.geom_from(g)
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=(g.H, g.N, g.W)).astype(np.float32)
+    y = rng.normal(size=(g.Z, g.Y, g.X)).astype(np.float32)
+    for window in ("ramlak", "hann"):
+        lhs = float(np.sum(orc.fdk_f64(x, G, window) * y))
+        rhs = float(np.sum(x.astype(np.float64) * orc.fdk_adjoint_f64(y, G, window)))
+        assert abs(lhs - rhs) <= 1e-12 * abs(lhs)

@@ -513,6 +513,122 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 }
 
 // ---------------------------------------------------------------------------
+// Forward projector: the exact transpose of the bilinear backprojector.
+//
+// For every voxel v in the FOV, projection b and voxel value g[v], the
+// backprojection reads q_b at (u, v') with bilinear weights and adds
+// fscale * U^2 * interp to the voxel; the transpose adds
+// fscale * U^2 * g[v] * weight to each of the four samples.  Masks are the
+// same: u in [0, W-1], v' in [0, H-1] (kernel.cu:127-131), FOV (kernel.cu:100).
+// A CTA scatters its voxel tile's contributions for one projection into a
+// shared-memory box with shared atomics, then adds the box to the global
+// gradient with one TMA reduce (cp.reduce.async.bulk.tensor ... .add).  Two
+// boxes alternate; a box is cleared only after the reduce that read it.
+// Reduces never start at a negative coordinate: the box origin is clamped
+// to >= 0, which only drops samples outside the detector (weight 0 anyway).
+template <int TX, int TY, int TZ, bool PARTIAL>
+__global__ void __launch_bounds__(TX *TY, 2)
+    fp_scatter_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P,
+                      const float *__restrict__ vin)
+{
+    constexpr int NT = TX * TY;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float *boxes = reinterpret_cast<float *>(smem);
+    int2 *boxo = reinterpret_cast<int2 *>(boxes + 2 * (size_t)P.stage_elems);
+
+    const int tid = threadIdx.x;
+    const int tx = tid % TX, ty = tid / TX;
+    const int x0 = (blockIdx.x % P.tilesX) * TX, y0 = (blockIdx.x / P.tilesX) * TY;
+    const int zc = blockIdx.y * TZ;
+    const int z0 = PARTIAL ? zc : min(zc, P.nz - TZ);
+    const int zlast = PARTIAL ? P.nz - 1 - z0 : TZ - 1;
+    const int x = x0 + tx, y = y0 + ty;
+    const float aX = flip(P.scale * ((float)x + P.dX), P.dirx);
+    const float aY = flip(P.scale * ((float)y + P.dY), P.diry);
+    const bool inside = (x < P.X) && (y < P.Y);
+    const bool active = inside && (sqrtf(aX * aX + aY * aY) < P.halfW);
+    if (!__syncthreads_or(active)) return;  // nothing in this tile projects
+
+    for (int b = tid; b < P.N; b += NT) {
+        int2 o = footprint_origin_z<TX, TY, 4>(P, b, x0, y0, z0, z0 + zlast);
+        o.x = max(o.x, 0);  // still a multiple of 4
+        o.y = max(o.y, 0);
+        boxo[b] = o;
+    }
+    // this thread's voxel values, scaled; slices owned by another chunk are 0
+    float g[TZ];
+#pragma unroll
+    for (int z = 0; z < TZ; ++z) {
+        g[z] = 0.f;
+        if (active && z <= zlast && z0 + z >= zc)
+            g[z] = P.fscale * vin[(size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x];
+    }
+    const float aZ0 = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
+    const float daZ = flip(P.scale, P.dirz);
+    const float cZ = P.cZ, Hm1 = P.Hm1;
+    const int BW = P.BW;
+    __syncthreads();
+
+    for (int b = 0; b < P.N; ++b) {
+        float *box = boxes + (size_t)(b & 1) * P.stage_elems;
+        if (tid == 0 && b >= 2) bulk_wait_group_read<1>();  // the reduce of b-2 has read this box
+        __syncthreads();
+        for (int i = tid; i < P.BW * P.BH; i += NT) box[i] = 0.f;
+        __syncthreads();
+        const int bx0 = boxo[b].x, by0 = boxo[b].y;
+        if (active) {
+            const float2 cs = P.trig[b];
+            const float Sd = aX * cs.x + aY * cs.y;
+            const float Td = aY * cs.x - aX * cs.y;
+            const float U = P.D / (P.D - Sd);
+            const float u = Td * U + P.cX;
+            if (u >= 0.f && u <= P.Wm1) {
+                const float fla = __fadd_rd(u, kMagic);
+                const int col = __float_as_int(fla) - kMagicBits - bx0;
+                const float fu = u - (fla - kMagic);
+                const float U2 = U * U;
+                const float v0 = aZ0 * U + cZ;
+                const float dv = daZ * U;
+                const float vL = fmaf((float)zlast, dv, v0);
+                const float vlo = fmaxf(fminf(v0, vL), 0.f), vhi = fminf(fmaxf(v0, vL), Hm1);
+                if (vlo <= vhi) {
+                    const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) + 1 - by0;
+                    if (col >= 0 && col + 1 < BW && rlo >= 0 && rhi < P.BH) {
+                        float *base = box + col;
+#pragma unroll
+                        for (int z = 0; z < TZ; ++z) {
+                            if (PARTIAL && z > zlast) break;
+                            const float v = fmaf((float)z, dv, v0);
+                            if (g[z] != 0.f && v >= 0.f && v <= Hm1) {
+                                const float fl = __fadd_rd(v, kMagic);
+                                const float fv = v - (fl - kMagic);
+                                const int row = __float_as_int(fl) - kMagicBits - by0;
+                                const float w = U2 * g[z];
+                                const float w1 = w * fu, w0 = w - w1;  // columns col, col+1
+                                float *r0 = base + row * BW;
+                                atomicAdd(r0, w0 - w0 * fv);
+                                atomicAdd(r0 + 1, w1 - w1 * fv);
+                                atomicAdd(r0 + BW, w0 * fv);
+                                atomicAdd(r0 + BW + 1, w1 * fv);
+                            }
+                        }
+                    } else {
+                        atomicOr(P.err, ERR_BOX_OVERFLOW);
+                    }
+                }
+            }
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            if (bx0 < (int)P.Wm1 + 1 && by0 < (int)P.Hm1 + 1) tma_reduce_add_3d(&tmap, bx0, by0, b, box);
+            bulk_commit_group();  // one group per projection, empty when the box misses the detector
+        }
+    }
+    if (tid == 0) bulk_wait_group_all();
+}
+
+// ---------------------------------------------------------------------------
 // host side
 
 static PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
@@ -693,6 +809,86 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
         dim3 block((unsigned)(v->TX * v->TY), 1, 1);
         void *args[] = {&tmap, &P};
         TK_CUDA(cudaLaunchKernel(fn, grid, block, args, smem, stream));
+    }
+    return TK_OK;
+}
+
+int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, float zoff, float *d_qbar,
+                           int accumulate, cudaStream_t stream)
+{
+    constexpr int TX = 16, TY = 16, TZ = 32;
+    if (int rc = validate_geometry(&g)) return rc;
+    TK_CHECK(d_vol && d_qbar, TK_ERR_INVALID, "forward project: null device pointer");
+    TK_CHECK(nz >= 0, TK_ERR_INVALID, "forward project: nz < 0");
+    auto encode = get_encode_fn();
+    TK_CHECK(encode, TK_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    const int Wp = row_pitch(g.W);
+    if (!accumulate)
+        TK_CUDA(cudaMemsetAsync(d_qbar, 0, (size_t)g.N * g.H * Wp * sizeof(float), stream));
+    if (nz == 0) return TK_OK;
+
+    const BPVariant shape = {nullptr, nullptr, TK_F32, TX, TY, TZ, 2, false, "fp"};
+    int BW, BH;
+    if (int rc = box_dims(g, nz, zoff, shape, 4, &BW, &BH)) return rc;
+    std::vector<float> cs(g.N), sn(g.N);
+    build_trig(g, cs.data(), sn.data());
+    const int p = reference_pad_length(g.W);
+    const int tilesX = (g.X + TX - 1) / TX, tilesY = (g.Y + TY - 1) / TY;
+    const int zchunks = (nz + TZ - 1) / TZ;
+    TK_CHECK((long long)tilesX * tilesY < (1ll << 31) && zchunks < 65536, TK_ERR_UNSUPPORTED,
+             "volume too large for one launch");
+    const bool partial = nz < TZ;
+    const void *fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, TZ, true>)
+                             : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, TZ, false>);
+
+    static thread_local BPParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.err = device_error_word();
+    TK_CHECK(P.err, TK_ERR_CUDA, "device error word unavailable");
+    P.slice_stride = (long long)g.X * g.Y;
+    P.X = g.X;
+    P.Y = g.Y;
+    P.nz = nz;
+    P.BW = BW;
+    P.BH = BH;
+    P.stage_elems = (BW * BH + 31) / 32 * 32;  // 128-byte aligned boxes
+    P.tilesX = tilesX;
+    P.cX = g.cX;
+    P.cZ = g.cZ;
+    P.D = g.D;
+    P.dX = -g.cx;
+    P.dY = -g.cy;
+    P.zoff = zoff;
+    P.scale = g.scale;
+    P.dirx = g.dirx ? 0x80000000u : 0u;
+    P.diry = g.diry ? 0x80000000u : 0u;
+    P.dirz = g.dirz ? 0x80000000u : 0u;
+    P.Wm1 = (float)(g.W - 1);
+    P.Hm1 = (float)(g.H - 1);
+    P.halfW = g.W / 2.;
+    P.fscale = g.dfi * (1.f / (float)p);  // the backprojection's scale, transposed
+
+    for (int b0 = 0; b0 < g.N; b0 += kMaxParamProj) {
+        const int nb = std::min(kMaxParamProj, g.N - b0);
+        P.N = nb;
+        for (int b = 0; b < nb; ++b) P.trig[b] = make_float2(cs[b0 + b], sn[b0 + b]);
+        CUtensorMap tmap;
+        char *base = reinterpret_cast<char *>(d_qbar) + (size_t)b0 * g.H * Wp * sizeof(float);
+        cuuint64_t dims[3] = {(cuuint64_t)g.W, (cuuint64_t)g.H, (cuuint64_t)nb};
+        cuuint64_t strides[2] = {(cuuint64_t)Wp * 4, (cuuint64_t)Wp * g.H * 4};
+        cuuint32_t box[3] = {(cuuint32_t)BW, (cuuint32_t)BH, 1};
+        cuuint32_t estr[3] = {1, 1, 1};
+        CUresult cr = encode(&tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
+        const size_t smem = 2 * (size_t)P.stage_elems * sizeof(float) + (size_t)nb * sizeof(int2) + 16;
+        TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "forward project: %zu B of shared memory needed", smem);
+        TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        dim3 grid((unsigned)(tilesX * tilesY), partial ? 1u : (unsigned)zchunks, 1);
+        const float *vin = d_vol;
+        void *args[] = {&tmap, &P, &vin};
+        TK_CUDA(cudaLaunchKernel(fn, grid, dim3(TX * TY), args, smem, stream));
     }
     return TK_OK;
 }

@@ -192,6 +192,43 @@ extern "C" int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_t
     return launch_backproject(*g, d_q, precision, d_scale, g->Z, tk_default_zoff(g), d_vol, 0, st);
 }
 
+// ------------------------------------------------------------- adjoint pair
+extern "C" int tk_forward_project(const tk_geometry *g, const float *d_vol, int nz, float zoff, float *d_qbar,
+                                  int accumulate, void *stream)
+{
+    if (int rc = validate_geometry(g)) return rc;
+    return launch_forward_project(*g, d_vol, nz, zoff, d_qbar, accumulate, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tk_filter_transpose(const tk_geometry *g, const float *d_qbar, int window, float *d_pbar, int layout,
+                                   void *stream)
+{
+    if (int rc = validate_geometry(g)) return rc;
+    return launch_filter_transpose(*g, d_qbar, window, d_pbar, layout, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tk_fdk_forward(const tk_geometry *g, const float *d_proj, int layout, int window, void *d_workspace,
+                              size_t workspace_bytes, float *d_vol, void *stream)
+{
+    return tk_fdk_device(g, d_proj, TK_INPUT_F32, layout, nullptr, window, TK_F32, d_workspace, workspace_bytes, d_vol,
+                         stream);
+}
+
+extern "C" int tk_fdk_backward(const tk_geometry *g, const float *d_vol_grad, int layout, int window,
+                               void *d_workspace, size_t workspace_bytes, float *d_proj_grad, void *stream)
+{
+    if (int rc = validate_geometry(g)) return rc;
+    const size_t need = tk_fdk_workspace_bytes(g, TK_F32);
+    TK_CHECK(d_workspace && workspace_bytes >= need, TK_ERR_INVALID, "workspace of %zu B needed, %zu given", need,
+             workspace_bytes);
+    TK_CHECK((reinterpret_cast<uintptr_t>(d_workspace) & 255) == 0, TK_ERR_INVALID,
+             "workspace must be 256-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    float *qbar = reinterpret_cast<float *>(static_cast<char *>(d_workspace) + kWsHeader);
+    if (int rc = launch_forward_project(*g, d_vol_grad, g->Z, tk_default_zoff(g), qbar, 0, st)) return rc;
+    return launch_filter_transpose(*g, qbar, window, d_proj_grad, layout, st);
+}
+
 extern "C" int tk_phantom_project(const tk_geometry *g, const double *ell, int nell, int layout, float *d_out,
                                   void *stream)
 {

@@ -37,6 +37,8 @@ struct LoadParams {
     float dark_v, flat_v, A, B, floor_counts;
     int invert;
     int W, N, H, layout, input_type;
+    int in_pitch;   // elements between consecutive input rows of one layout line (W, or Wp)
+    int weight_in;  // apply the cosine weight while loading (forward); 0 for the transpose
     float cX, cZ, D;
 };
 
@@ -48,6 +50,8 @@ struct FiltParams {
     int Wp, p, lg, precision;
     int rc, nchunks;        // coefficient image: rows per work unit, units per projection
     long long nunits;
+    int out_layout;         // raw output: TK_LAYOUT_PROJECTION [N][H][Wp] or TK_LAYOUT_SINOGRAM [H][N][Wp]
+    int weight_out;         // multiply the output by the cosine weight (the filter's transpose)
     float Hf[kMaxHf];  // tau * |R2C_p(h)| * window, k = 0..p/2
 };
 
@@ -56,7 +60,15 @@ __device__ __forceinline__ long long in_row_offset(const LoadParams &L, long lon
 {
     const long long b = row / L.H;
     r = (int)(row - b * L.H);
-    return L.layout == TK_LAYOUT_SINOGRAM ? ((long long)r * L.N + b) * L.W : row * (long long)L.W;
+    return L.layout == TK_LAYOUT_SINOGRAM ? ((long long)r * L.N + b) * L.in_pitch : row * (long long)L.in_pitch;
+}
+
+// row[x] *= distance / sqrt(ce*ce + distance*distance + cs*cs)  (kernel.cu:195-199)
+__device__ __forceinline__ float cosine_weight(const LoadParams &L, int r, int x)
+{
+    const float ce = (float)x - L.cX;
+    const float cs = (float)r - L.cZ;
+    return L.D / sqrtf(ce * ce + L.D * L.D + cs * cs);
 }
 
 // Preprocessed (log if raw, cosine weighted) sample x of a row.
@@ -75,10 +87,8 @@ __device__ __forceinline__ float load_pre(const LoadParams &L, long long off, in
     } else {
         val = static_cast<const float *>(L.in)[off + x];
     }
-    // row[x] *= distance / sqrt(ce*ce + distance*distance + cs*cs)  (kernel.cu:195-199)
-    const float ce = (float)x - L.cX;
-    const float cs = (float)r - L.cZ;
-    return val * (L.D / sqrtf(ce * ce + L.D * L.D + cs * cs));
+    if (!L.weight_in) return val;
+    return val * cosine_weight(L, r, x);
 }
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
@@ -162,6 +172,14 @@ template <> __device__ __forceinline__ __nv_bfloat16 store_cvt<__nv_bfloat16>(fl
     return __float2bfloat16_rn(v);
 }
 
+// Element offset of output row `row` (= b*H + r) of the raw-sample output.
+__device__ __forceinline__ long long out_row_offset(const FiltParams &P, long long row, int &r)
+{
+    const long long b = row / P.L.H;
+    r = (int)(row - b * P.L.H);
+    return P.out_layout == TK_LAYOUT_SINOGRAM ? ((long long)r * P.L.N + b) * P.Wp : row * (long long)P.Wp;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_constant__ FiltParams P)
 {
@@ -213,11 +231,18 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
         __syncthreads();
         float2 *Q = fft_forward(R, Sb, tw, p, P.lg, t, TPF);
         if (valid) {
-            T *qa = out + ra * (long long)P.Wp;
-            for (int i = t; i < W; i += TPF) qa[i] = store_cvt<T>(Q[i].x * sigma);
+            int r_a, r_b;
+            T *qa = out + out_row_offset(P, ra, r_a);
+            for (int i = t; i < W; i += TPF) {
+                const float w = P.weight_out ? cosine_weight(P.L, r_a, i) : 1.f;
+                qa[i] = store_cvt<T>(Q[i].x * sigma * w);
+            }
             if (hasb) {
-                T *qb = out + rb * (long long)P.Wp;
-                for (int i = t; i < W; i += TPF) qb[i] = store_cvt<T>(-Q[i].y * sigma);
+                T *qb = out + out_row_offset(P, rb, r_b);
+                for (int i = t; i < W; i += TPF) {
+                    const float w = P.weight_out ? cosine_weight(P.L, r_b, i) : 1.f;
+                    qb[i] = store_cvt<T>(-Q[i].y * sigma * w);
+                }
             }
         }
         __syncthreads();  // buffers are reused by the next pair group
@@ -535,6 +560,8 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     L.H = g.H;
     L.layout = layout;
     L.input_type = input_type;
+    L.in_pitch = g.W;
+    L.weight_in = 1;
     L.cX = g.cX;
     L.cZ = g.cZ;
     L.D = g.D;
@@ -553,6 +580,8 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     }
     const Spectrum &sp = spectrum(g.W, g.tau, window, p);
     P.out = d_q;
+    P.out_layout = TK_LAYOUT_PROJECTION;
+    P.weight_out = 0;
     P.nrows = (long long)g.N * g.H;
     P.npairs = (P.nrows + 1) / 2;
     P.Wp = row_pitch(g.W);
@@ -590,6 +619,52 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     }
     TK_CUDA(cudaGetLastError());
     return launch_filter_typed(P, p, stream, precision);
+}
+
+// Transpose of the filter stage for the adjoint: the ramp filter is a
+// symmetric Toeplitz operator (its spectrum is real and even) and the cosine
+// weight is diagonal, so (F W)^T = W F.  Reads a [N][H][Wp] FP32 gradient,
+// filters each row with the same spectrum and unnormalised scale, multiplies
+// by the cosine weight and writes FP32 in `layout` with row pitch W.
+int launch_filter_transpose(const tk_geometry &g, const float *d_qbar, int window, float *d_pbar, int layout,
+                            cudaStream_t stream)
+{
+    if (int rc = validate_geometry(&g)) return rc;
+    TK_CHECK(d_qbar && d_pbar, TK_ERR_INVALID, "filter transpose: null device pointer");
+    TK_CHECK(layout == TK_LAYOUT_SINOGRAM || layout == TK_LAYOUT_PROJECTION, TK_ERR_INVALID, "bad layout");
+    TK_CHECK(window >= TK_WINDOW_RAMLAK && window <= TK_WINDOW_HANN, TK_ERR_INVALID, "bad window");
+    const int p = reference_pad_length(g.W);
+    TK_CHECK(p <= 2 * (kMaxHf - 1), TK_ERR_UNSUPPORTED, "filter: W = %d exceeds the supported 4096", g.W);
+    static thread_local FiltParams P;
+    std::memset(&P, 0, sizeof(P));
+    LoadParams &L = P.L;
+    L.in = d_qbar;
+    L.W = g.W;
+    L.N = g.N;
+    L.H = g.H;
+    L.layout = TK_LAYOUT_PROJECTION;
+    L.input_type = TK_INPUT_F32;
+    L.in_pitch = row_pitch(g.W);
+    L.weight_in = 0;
+    L.cX = g.cX;
+    L.cZ = g.cZ;
+    L.D = g.D;
+    L.A = 1.f;
+    const Spectrum &sp = spectrum(g.W, g.tau, window, p);
+    P.out = d_pbar;
+    P.out_layout = layout;
+    P.weight_out = 1;
+    P.q_scale = nullptr;
+    P.nrows = (long long)g.N * g.H;
+    P.npairs = (P.nrows + 1) / 2;
+    P.Wp = g.W;  // dense output rows
+    P.p = p;
+    int lg = 0;
+    while ((1 << lg) < p) ++lg;
+    P.lg = lg;
+    P.precision = TK_F32;
+    std::memcpy(P.Hf, sp.Hf.data(), sizeof(float) * sp.Hf.size());
+    return launch_filter_typed(P, p, stream, TK_F32);
 }
 
 }  // namespace tk

@@ -44,6 +44,10 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
                   cudaStream_t stream);
 int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale,
                        int nz, float zoff, float *d_vol, int accumulate, cudaStream_t stream);
+int launch_filter_transpose(const tk_geometry &g, const float *d_qbar, int window, float *d_pbar, int layout,
+                            cudaStream_t stream);
+int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, float zoff, float *d_qbar,
+                           int accumulate, cudaStream_t stream);
 int launch_phantom(const tk_geometry &g, const double *ell, int nell, int layout, float *d_out,
                    cudaStream_t stream);
 

@@ -109,6 +109,49 @@ def fdk_device(g, d_in, input_type=_lib.TK_INPUT_F32, layout=_lib.TK_LAYOUT_SINO
     return vol
 
 
+def forward_project(g, vol, nz=None, zoff=None, out=None, accumulate=False, stream=None):
+    """B^T: transpose of the backprojection; returns [N][H][Wp] FP32."""
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    nz = g.Z if nz is None else nz
+    zoff = L.tk_default_zoff(ctypes.byref(gc)) if zoff is None else zoff
+    if out is None:
+        out = torch.empty((g.N, g.H, row_pitch(g.W)), dtype=torch.float32, device=vol.device)
+    check(L.tk_forward_project(ctypes.byref(gc), vol.data_ptr(), int(nz), float(zoff), out.data_ptr(),
+                               int(bool(accumulate)), _stream_ptr(stream)))
+    return out
+
+
+def filter_transpose(g, qbar, window=_lib.TK_WINDOW_RAMLAK, layout=_lib.TK_LAYOUT_SINOGRAM, out=None, stream=None):
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    shape = (g.H, g.N, g.W) if layout == _lib.TK_LAYOUT_SINOGRAM else (g.N, g.H, g.W)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float32, device=qbar.device)
+    check(L.tk_filter_transpose(ctypes.byref(gc), qbar.data_ptr(), window, out.data_ptr(), layout,
+                                _stream_ptr(stream)))
+    return out
+
+
+def fdk_backward(g, vol_grad, window=_lib.TK_WINDOW_RAMLAK, layout=_lib.TK_LAYOUT_SINOGRAM, workspace=None,
+                 out=None, stream=None):
+    """A^T: gradient of a volume loss with respect to the line integrals."""
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    nb = workspace_bytes(g, _lib.TK_F32)
+    if workspace is None:
+        workspace = torch.empty(nb, dtype=torch.uint8, device=vol_grad.device)
+    shape = (g.H, g.N, g.W) if layout == _lib.TK_LAYOUT_SINOGRAM else (g.N, g.H, g.W)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float32, device=vol_grad.device)
+    check(L.tk_fdk_backward(ctypes.byref(gc), vol_grad.data_ptr(), layout, window, workspace.data_ptr(),
+                            workspace.numel(), out.data_ptr(), _stream_ptr(stream)))
+    return out
+
+
 def phantom_project(g, ell: np.ndarray, layout=_lib.TK_LAYOUT_SINOGRAM, out=None, device="cuda", stream=None):
     """Analytic line integrals of ellipsoids on the GPU (FP32)."""
     torch = _torch()
