@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--no-rmse", action="store_true", help="skip the FP64 oracle accuracy check")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--variant", type=int, default=-1, help="backprojection kernel variant (-1 = default)")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="differentiation workload: 512^3 (scale 1.5) from 360 x 768^2 FP32 projections, "
+                         "time A (FDK) and A^T (transpose) and check the dot-product test")
     ap.add_argument("--sweep", action="store_true", help="with --profile-bp: time every variant of that precision")
     ap.add_argument("--profile-bp", choices=["f32", "f16", "bf16", "f32c"], default=None,
                     help="small case for ncu: 180 x 1024^2 projections, a 64-slice slab of the 1024^2 volume; "
@@ -445,8 +448,56 @@ def run_profile_bp(args):
     return 0
 
 
+def run_adjoint(args):
+    """A and A^T on the 512^3 / 360 x 768^2 differentiation workload."""
+    import torch
+
+    from tomokvas_gb300 import _build, _lib, device
+    from tomokvas_gb300.geometry import config
+    from tomokvas_gb300.phantom import random_ellipsoids
+
+    _build.build()
+    torch.cuda.set_device(0)
+    g = config("c4")
+    ell = random_ellipsoids(20, g.fov_radius_cm, g.Z * g.voxel_cm / 2, seed=4)
+    p = device.phantom_project(g, ell, _lib.TK_LAYOUT_SINOGRAM)
+    gen = torch.Generator(device="cuda").manual_seed(9)
+    p += 0.01 * float(p.max().item()) * torch.randn(p.shape, device="cuda", generator=gen)
+    y = torch.randn((g.Z, g.Y, g.X), device="cuda", generator=gen)
+    ws = torch.empty(device.workspace_bytes(g, _lib.TK_F32), dtype=torch.uint8, device="cuda")
+    vol = torch.empty((g.Z, g.Y, g.X), device="cuda")
+    grad = torch.empty_like(p)
+
+    def fwd():
+        device.fdk_device(g, p, workspace=ws, vol=vol)
+
+    def bwd():
+        device.fdk_backward(g, y, workspace=ws, out=grad)
+
+    res = {}
+    for name, fn in (("forward", fwd), ("backward", bwd)):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res[name] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
+    lhs = float(torch.sum(vol.double() * y.double()).item())
+    rhs = float(torch.sum(p.double() * grad.double()).item())
+    emit({"workload": "fdk_adjoint_512cube_scale1.5_from_360x768sq_f32", "updates": g.updates, **res,
+          "dot_product_rel_err": abs(lhs - rhs) / abs(lhs), "flags": device.device_error_flags()})
+    return 0
+
+
 def main():
     args = parse()
+    if args.adjoint:
+        return run_adjoint(args)
     if args.profile_bp:
         return run_profile_bp(args)
     if args.impl == "reference":
