@@ -513,7 +513,8 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 }
 
 // ---------------------------------------------------------------------------
-// Forward projector: the exact transpose of the bilinear backprojector.
+// Forward projector: the exact transpose of the bilinear backprojector
+// (bp_tma_kernel, the FP32-sample storage that tk_fdk_forward uses).
 //
 // For every voxel v in the FOV, projection b and voxel value g[v], the
 // backprojection reads q_b at (u, v') with bilinear weights and adds
@@ -563,8 +564,12 @@ __global__ void __launch_bounds__(TX *TY, 2)
         if (active && z <= zlast && z0 + z >= zc)
             g[z] = P.fscale * vin[(size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x];
     }
-    const float aZ0 = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
-    const float daZ = flip(P.scale, P.dirz);
+    // v is formed per voxel exactly as bp_tma_kernel forms it, so the masks
+    // v in [0, H-1] agree voxel by voxel and this is the transpose of that
+    // kernel to FP32 rounding of the weights.
+    float aZ[TZ];
+#pragma unroll
+    for (int z = 0; z < TZ; ++z) aZ[z] = flip(P.scale * ((float)min(z0 + z, P.nz - 1) + P.zoff), P.dirz);
     const float cZ = P.cZ, Hm1 = P.Hm1;
     const int BW = P.BW;
     __syncthreads();
@@ -587,9 +592,8 @@ __global__ void __launch_bounds__(TX *TY, 2)
                 const int col = __float_as_int(fla) - kMagicBits - bx0;
                 const float fu = u - (fla - kMagic);
                 const float U2 = U * U;
-                const float v0 = aZ0 * U + cZ;
-                const float dv = daZ * U;
-                const float vL = fmaf((float)zlast, dv, v0);
+                const float v0 = aZ[0] * U + cZ;
+                const float vL = aZ[TZ - 1] * U + cZ;  // slices past zlast repeat zlast
                 const float vlo = fmaxf(fminf(v0, vL), 0.f), vhi = fminf(fmaxf(v0, vL), Hm1);
                 if (vlo <= vhi) {
                     const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) + 1 - by0;
@@ -598,7 +602,7 @@ __global__ void __launch_bounds__(TX *TY, 2)
 #pragma unroll
                         for (int z = 0; z < TZ; ++z) {
                             if (PARTIAL && z > zlast) break;
-                            const float v = fmaf((float)z, dv, v0);
+                            const float v = aZ[z] * U + cZ;
                             if (g[z] != 0.f && v >= 0.f && v <= Hm1) {
                                 const float fl = __fadd_rd(v, kMagic);
                                 const float fv = v - (fl - kMagic);
