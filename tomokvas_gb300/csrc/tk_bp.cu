@@ -523,21 +523,31 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // same: u in [0, W-1], v' in [0, H-1] (kernel.cu:127-131), FOV (kernel.cu:100).
 // A CTA scatters its voxel tile's contributions for one projection into a
 // shared-memory box with shared atomics, then adds the box to the global
-// gradient with one TMA reduce (cp.reduce.async.bulk.tensor ... .add).  Two
-// boxes alternate; a box is cleared only after the reduce that read it.
-// Reduces never start at a negative coordinate: the box origin is clamped
-// to >= 0, which only drops samples outside the detector (weight 0 anyway).
-template <int TX, int TY, int TZ, bool PARTIAL>
+// gradient with one TMA reduce (cp.reduce.async.bulk.tensor ... .add).
+// Conflicts: in a warp the lanes that share a detector column would hit the
+// same cell at every z (rays along x put all 16 x-lanes on one column), so
+// lane l handles slice (k + l) mod 32 at step k; lanes then sit on different
+// rows, and the accumulation box has an odd row pitch (BW + 1) so that
+// different rows of one column fall in different banks.  After the atomics
+// the box is drained into one of two dense staging boxes (the TMA source,
+// pitch BW) and cleared in the same pass; a staging box is rewritten only
+// after the reduce that read it.  Reduces never start at a negative
+// coordinate: the box origin is clamped to >= 0, which only drops samples
+// outside the detector (weight 0 anyway).
+template <int TX, int TY, bool PARTIAL>
 __global__ void __launch_bounds__(TX *TY, 2)
     fp_scatter_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P,
                       const float *__restrict__ vin)
 {
     constexpr int NT = TX * TY;
+    constexpr int TZ = 32;  // one slice per lane of a warp at every step
     extern __shared__ __align__(128) unsigned char smem[];
-    float *boxes = reinterpret_cast<float *>(smem);
-    int2 *boxo = reinterpret_cast<int2 *>(boxes + 2 * (size_t)P.stage_elems);
+    const int BW = P.BW, BWp = P.BW + 1, BH = P.BH;
+    float *staging = reinterpret_cast<float *>(smem);           // 2 x [BH][BW]
+    float *acc = staging + 2 * (size_t)P.stage_elems;            // [BH][BW + 1]
+    int2 *boxo = reinterpret_cast<int2 *>(acc + (size_t)((BH * BWp + 31) & ~31));
 
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int tx = tid % TX, ty = tid / TX;
     const int x0 = (blockIdx.x % P.tilesX) * TX, y0 = (blockIdx.x / P.tilesX) * TY;
     const int zc = blockIdx.y * TZ;
@@ -556,30 +566,27 @@ __global__ void __launch_bounds__(TX *TY, 2)
         o.y = max(o.y, 0);
         boxo[b] = o;
     }
-    // this thread's voxel values, scaled; slices owned by another chunk are 0
-    float g[TZ];
+    for (int i = tid; i < BH * BWp; i += NT) acc[i] = 0.f;
+    // This thread's voxel values (scaled) and slice coordinates in its
+    // rotated slice order; slices owned by another chunk, or past the end,
+    // carry 0.  aZ is formed per voxel exactly as bp_tma_kernel forms it, so
+    // the masks v in [0, H-1] agree voxel by voxel and this is the transpose
+    // of that kernel to FP32 rounding of the weights.
+    float g[TZ], aZ[TZ];
 #pragma unroll
-    for (int z = 0; z < TZ; ++z) {
-        g[z] = 0.f;
+    for (int k = 0; k < TZ; ++k) {
+        const int z = (k + lane) & (TZ - 1);
+        g[k] = 0.f;
         if (active && z <= zlast && z0 + z >= zc)
-            g[z] = P.fscale * vin[(size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x];
+            g[k] = P.fscale * vin[(size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x];
+        aZ[k] = flip(P.scale * ((float)min(z0 + z, P.nz - 1) + P.zoff), P.dirz);
     }
-    // v is formed per voxel exactly as bp_tma_kernel forms it, so the masks
-    // v in [0, H-1] agree voxel by voxel and this is the transpose of that
-    // kernel to FP32 rounding of the weights.
-    float aZ[TZ];
-#pragma unroll
-    for (int z = 0; z < TZ; ++z) aZ[z] = flip(P.scale * ((float)min(z0 + z, P.nz - 1) + P.zoff), P.dirz);
+    const float aZf = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
+    const float aZl = flip(P.scale * ((float)(z0 + zlast) + P.zoff), P.dirz);
     const float cZ = P.cZ, Hm1 = P.Hm1;
-    const int BW = P.BW;
     __syncthreads();
 
     for (int b = 0; b < P.N; ++b) {
-        float *box = boxes + (size_t)(b & 1) * P.stage_elems;
-        if (tid == 0 && b >= 2) bulk_wait_group_read<1>();  // the reduce of b-2 has read this box
-        __syncthreads();
-        for (int i = tid; i < P.BW * P.BH; i += NT) box[i] = 0.f;
-        __syncthreads();
         const int bx0 = boxo[b].x, by0 = boxo[b].y;
         if (active) {
             const float2 cs = P.trig[b];
@@ -592,28 +599,26 @@ __global__ void __launch_bounds__(TX *TY, 2)
                 const int col = __float_as_int(fla) - kMagicBits - bx0;
                 const float fu = u - (fla - kMagic);
                 const float U2 = U * U;
-                const float v0 = aZ[0] * U + cZ;
-                const float vL = aZ[TZ - 1] * U + cZ;  // slices past zlast repeat zlast
+                const float v0 = aZf * U + cZ, vL = aZl * U + cZ;
                 const float vlo = fmaxf(fminf(v0, vL), 0.f), vhi = fminf(fmaxf(v0, vL), Hm1);
                 if (vlo <= vhi) {
                     const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) + 1 - by0;
-                    if (col >= 0 && col + 1 < BW && rlo >= 0 && rhi < P.BH) {
-                        float *base = box + col;
+                    if (col >= 0 && col + 1 < BW && rlo >= 0 && rhi < BH) {
+                        float *base = acc + col;
 #pragma unroll
-                        for (int z = 0; z < TZ; ++z) {
-                            if (PARTIAL && z > zlast) break;
-                            const float v = aZ[z] * U + cZ;
-                            if (g[z] != 0.f && v >= 0.f && v <= Hm1) {
+                        for (int k = 0; k < TZ; ++k) {
+                            const float v = aZ[k] * U + cZ;
+                            if (g[k] != 0.f && v >= 0.f && v <= Hm1) {
                                 const float fl = __fadd_rd(v, kMagic);
                                 const float fv = v - (fl - kMagic);
                                 const int row = __float_as_int(fl) - kMagicBits - by0;
-                                const float w = U2 * g[z];
+                                const float w = U2 * g[k];
                                 const float w1 = w * fu, w0 = w - w1;  // columns col, col+1
-                                float *r0 = base + row * BW;
+                                float *r0 = base + row * BWp;
                                 atomicAdd(r0, w0 - w0 * fv);
                                 atomicAdd(r0 + 1, w1 - w1 * fv);
-                                atomicAdd(r0 + BW, w0 * fv);
-                                atomicAdd(r0 + BW + 1, w1 * fv);
+                                atomicAdd(r0 + BWp, w0 * fv);
+                                atomicAdd(r0 + BWp + 1, w1 * fv);
                             }
                         }
                     } else {
@@ -622,10 +627,19 @@ __global__ void __launch_bounds__(TX *TY, 2)
                 }
             }
         }
+        float *st = staging + (size_t)(b & 1) * P.stage_elems;
+        if (tid == 0 && b >= 2) bulk_wait_group_read<1>();  // the reduce of b-2 has read this staging box
+        __syncthreads();
+        for (int i = tid; i < BH * BW; i += NT) {
+            const int r = i / BW, c = i - r * BW;
+            float *a = acc + r * BWp + c;
+            st[i] = *a;
+            *a = 0.f;
+        }
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
-            if (bx0 < (int)P.Wm1 + 1 && by0 < (int)P.Hm1 + 1) tma_reduce_add_3d(&tmap, bx0, by0, b, box);
+            if (bx0 < (int)P.Wm1 + 1 && by0 < (int)P.Hm1 + 1) tma_reduce_add_3d(&tmap, bx0, by0, b, st);
             bulk_commit_group();  // one group per projection, empty when the box misses the detector
         }
     }
@@ -842,8 +856,8 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     TK_CHECK((long long)tilesX * tilesY < (1ll << 31) && zchunks < 65536, TK_ERR_UNSUPPORTED,
              "volume too large for one launch");
     const bool partial = nz < TZ;
-    const void *fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, TZ, true>)
-                             : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, TZ, false>);
+    const void *fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
+                             : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>);
 
     static thread_local BPParams P;
     std::memset(&P, 0, sizeof(P));
@@ -886,7 +900,8 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
-        const size_t smem = 2 * (size_t)P.stage_elems * sizeof(float) + (size_t)nb * sizeof(int2) + 16;
+        const size_t acc_elems = (size_t)((BH * (BW + 1) + 31) & ~31);  // odd-pitch accumulation box
+        const size_t smem = (2 * (size_t)P.stage_elems + acc_elems) * sizeof(float) + (size_t)nb * sizeof(int2) + 16;
         TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "forward project: %zu B of shared memory needed", smem);
         TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         dim3 grid((unsigned)(tilesX * tilesY), partial ? 1u : (unsigned)zchunks, 1);
