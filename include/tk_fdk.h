@@ -161,6 +161,24 @@ int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_type, int la
                   const tk_flatfield *ff, int window, int precision,
                   void *d_workspace, size_t workspace_bytes, float *d_vol, void *stream);
 
+/* ---------------------------------------------------------- out-of-core
+ * Whole FDK with the projections left in host memory (projection-major
+ * [N][H][W], TK_INPUT_F32 or TK_INPUT_U16), streamed to the GPU in chunks of
+ * `chunk` projections: the host-to-device copy of chunk k+1 (and k+2) runs on
+ * a library-owned copy stream while chunk k is filtered and backprojected on
+ * `stream`, and the volume d_vol[Z][Y][X] accumulates the chunks.  Page-locked
+ * host memory (cudaHostAlloc / cudaHostRegister) lets the copies overlap;
+ * pageable memory works but serialises them.  The reference splits the angles
+ * into sub-allocations and sums partial volumes ("collecting",
+ * kernel.cu:342-371, 849-876); here the volume stays whole in HBM and the
+ * projections stream instead.  Returns once the work is enqueued: h_in must
+ * stay valid and unchanged until `stream` has passed it.  Allocates nothing
+ * on the device (the workspace holds two raw chunks and one filtered chunk). */
+size_t tk_fdk_stream_workspace_bytes(const tk_geometry *g, int input_type, int precision, int chunk);
+int tk_fdk_stream(const tk_geometry *g, const void *h_in, int input_type, const tk_flatfield *ff, int window,
+                  int precision, int chunk, void *d_workspace, size_t workspace_bytes, float *d_vol,
+                  void *stream);
+
 /* ------------------------------------------------ adjoint (differentiation)
  * The FDK A = B F W is linear in the line integrals: W the cosine weight
  * (diagonal), F the ramp filter (symmetric Toeplitz: its spectrum is real and

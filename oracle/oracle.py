@@ -93,6 +93,8 @@ def _declare(L):
     d = ctypes.c_double
     L.orc_fdk_u16_f32_sampled.argtypes = [P(ctypes.c_uint16), d, d, d, d, ctypes.c_int, d, gp, ctypes.c_int,
                                           i32p, ctypes.c_int, f32p, ctypes.c_int]
+    L.orc_fdk_u16_f64_sampled.argtypes = [P(ctypes.c_uint16), d, d, d, d, ctypes.c_int, d, gp, ctypes.c_int,
+                                          i32p, ctypes.c_int, f64p, ctypes.c_int]
     L.orc_log_u16_f64.argtypes = [P(ctypes.c_uint16), f32p, f32p, ctypes.c_int, ctypes.c_int,
                                   ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_double, f32p, ctypes.c_int]
@@ -183,6 +185,23 @@ def fdk_u16_f32_sampled(raw: np.ndarray, g: Geom, flat: float, dark: float = 0.0
                                        _ptr(vol, ctypes.c_float), _threads(nthreads))
     if rc:
         raise MemoryError("oracle fdk_u16_f32_sampled failed")
+    return vol
+
+
+def fdk_u16_f64_sampled(raw: np.ndarray, g: Geom, flat: float, dark: float = 0.0, A=1.0, B=0.0, invert=True,
+                        floor_counts=0.5, window="ramlak", zlist=None, nthreads=0) -> np.ndarray:
+    """FP64 oracle from raw uint16 [N][H][W] on sampled slices, streaming the
+    projections in small blocks (memory independent of N)."""
+    r = np.ascontiguousarray(raw).view(np.uint16)
+    assert r.shape == (g.N, g.H, g.W), r.shape
+    z = _zlist(g, zlist)
+    vol = np.zeros((len(z), g.Y, g.X), dtype=np.float64)
+    win = WINDOWS[window] if isinstance(window, str) else int(window)
+    rc = lib().orc_fdk_u16_f64_sampled(_ptr(r, ctypes.c_uint16), dark, flat, A, B, int(bool(invert)), floor_counts,
+                                       ctypes.byref(g), win, _ptr(z, ctypes.c_int), len(z),
+                                       _ptr(vol, ctypes.c_double), _threads(nthreads))
+    if rc:
+        raise MemoryError("oracle fdk_u16_f64_sampled failed")
     return vol
 
 

@@ -630,6 +630,142 @@ int orc_fdk_f64(const float *sino, const orc_geom *g, int window,
     return 0;
 }
 
+/* FP64 FDK of raw uint16 counts on listed slices, with the projections taken
+ * in blocks of ORC_U16_BLOCK so that memory stays O(rows x block x W) however
+ * many projections there are: log as orc_log_u16_f64 with scalar dark/flat
+ * (rsq_load.cpp:299-325) kept in double, cosine weight (kernel.cu:179-201),
+ * ramp filter (kernel.cu:557-802) and bilinear backprojection
+ * (kernel.cu:68-177), all in double. */
+#define ORC_U16_BLOCK 16
+
+typedef struct {
+    const uint16_t *raw;
+    const orc_geom *g;
+    double *q; /* [nr][nb][W] */
+    const double *Hf, *tw;
+    int p, row_lo, b0, nb;
+    double dark, flat, A, B, fl;
+    int invert;
+} orc_u16f64_filt_ctx;
+
+static void orc_u16f64_filt_row(void *vctx, long i)
+{
+    orc_u16f64_filt_ctx *c = (orc_u16f64_filt_ctx *)vctx;
+    const orc_geom *g = c->g;
+    int p = c->p, W = g->W;
+    int rr = (int)(i / c->nb), bb = (int)(i % c->nb), r = c->row_lo + rr, b = c->b0 + bb;
+    double *re = (double *)malloc(sizeof(double) * 2 * (size_t)p);
+    double *im = re + p;
+    const uint16_t *src = c->raw + ((size_t)b * g->H + r) * W;
+    double D = g->D, cs = (double)r - g->cZ;
+    double den = c->flat - c->dark;
+    if (den < c->fl) den = c->fl;
+    for (int x = 0; x < p; ++x) {
+        im[x] = 0;
+        re[x] = 0;
+        if (x < W) {
+            double num = (double)src[x] - c->dark;
+            if (num < c->fl) num = c->fl;
+            double v = c->A * log(num / den) + c->B;
+            if (c->invert) v = -v;
+            double ce = (double)x - g->cX;
+            re[x] = v * D / sqrt(ce * ce + D * D + cs * cs);
+        }
+    }
+    orc_fft_f64(re, im, p, c->tw, -1);
+    for (int k = 0; k < p; ++k) {
+        double h = c->Hf[k <= p / 2 ? k : p - k];
+        re[k] *= h;
+        im[k] *= h;
+    }
+    orc_fft_f64(re, im, p, c->tw, +1);
+    double *dst = c->q + ((size_t)rr * c->nb + bb) * W;
+    for (int x = 0; x < W; ++x) dst[x] = re[x] / (double)p;
+    free(re);
+}
+
+typedef struct {
+    const double *q;
+    const orc_geom *g;
+    const int *zlist;
+    double *vol;
+    const double *sn, *cs;
+    int row_lo, nrows, b0, nb;
+} orc_u16f64_bp_ctx;
+
+static void orc_u16f64_bp_row(void *vctx, long idx)
+{
+    orc_u16f64_bp_ctx *c = (orc_u16f64_bp_ctx *)vctx;
+    const orc_geom *g = c->g;
+    int zi = (int)(idx / g->Y), y = (int)(idx % g->Y);
+    double *out = c->vol + ((size_t)zi * g->Y + y) * g->X;
+    double s = g->scale, D = g->D;
+    double aY = s * ((double)y - g->cy);
+    double aZ = s * ((double)c->zlist[zi] - (g->Z - 1) / 2.0 - g->cz);
+    if (g->diry) aY = -aY;
+    if (g->dirz) aZ = -aZ;
+    for (int x = 0; x < g->X; ++x) {
+        double aX = s * ((double)x - g->cx);
+        if (g->dirx) aX = -aX;
+        if (!(sqrt(aX * aX + aY * aY) < g->W / 2.0)) continue;
+        double acc = 0;
+        for (int bb = 0; bb < c->nb; ++bb) {
+            int b = c->b0 + bb;
+            double S = aX * c->cs[b] + aY * c->sn[b];
+            double T = aY * c->cs[b] - aX * c->sn[b];
+            double U = D / (D - S);
+            double u = T * U + g->cX, v = aZ * U + g->cZ;
+            if (u < 0 || u > g->W - 1 || v < 0 || v > g->H - 1) continue;
+            int a = (int)floor(u), r = (int)floor(v);
+            double fu = u - a, fv = v - r;
+            int a1 = a + 1 < g->W ? a + 1 : a, r1 = r + 1 < g->H ? r + 1 : r;
+            int rb = r - c->row_lo, rb1 = r1 - c->row_lo;
+            if (rb < 0 || rb1 >= c->nrows) { acc = NAN; break; } /* band too small: make it loud */
+            const double *q0 = c->q + ((size_t)rb * c->nb + bb) * g->W;
+            const double *q1 = c->q + ((size_t)rb1 * c->nb + bb) * g->W;
+            double top = q0[a] + (q0[a1] - q0[a]) * fu;
+            double bot = q1[a] + (q1[a1] - q1[a]) * fu;
+            acc += U * U * (top + (bot - top) * fv);
+        }
+        out[x] += acc;
+    }
+}
+
+int orc_fdk_u16_f64_sampled(const uint16_t *raw, double dark, double flat, double A, double B, int invert,
+                            double floor_counts, const orc_geom *g, int window,
+                            const int *zlist, int nz, double *vol, int nthreads)
+{
+    int lo, hi;
+    orc_rows_needed(g, zlist, nz, &lo, &hi);
+    int nr = hi - lo + 1, nb = g->N < ORC_U16_BLOCK ? g->N : ORC_U16_BLOCK;
+    int p = orc_pad_length(g->W);
+    double *q = (double *)malloc(sizeof(double) * (size_t)nr * nb * g->W);
+    double *Hf = (double *)malloc(sizeof(double) * (size_t)(p / 2 + 1));
+    double *tw = (double *)malloc(sizeof(double) * (size_t)p);
+    double *sn = (double *)malloc(sizeof(double) * 2 * (size_t)g->N);
+    if (!q || !Hf || !tw || !sn) { free(q); free(Hf); free(tw); free(sn); return -1; }
+    double *cs = sn + g->N;
+    orc_spectrum_f64(g->W, g->tau, window, p, Hf);
+    orc_twiddles_f64(tw, p);
+    for (int b = 0; b < g->N; ++b) {
+        double a = orc_angle(g, b);
+        sn[b] = sin(a);
+        cs[b] = cos(a);
+    }
+    size_t nvox = (size_t)nz * g->Y * g->X;
+    memset(vol, 0, sizeof(double) * nvox);
+    for (int b0 = 0; b0 < g->N; b0 += nb) {
+        int nbb = g->N - b0 < nb ? g->N - b0 : nb;
+        orc_u16f64_filt_ctx fc = {raw, g, q, Hf, tw, p, lo, b0, nbb, dark, flat, A, B, floor_counts, invert};
+        orc_parallel_for((long)nr * nbb, nthreads, orc_u16f64_filt_row, &fc);
+        orc_u16f64_bp_ctx bc = {q, g, zlist, vol, sn, cs, lo, nr, b0, nbb};
+        orc_parallel_for((long)nz * g->Y, nthreads, orc_u16f64_bp_row, &bc);
+    }
+    for (size_t i = 0; i < nvox; ++i) vol[i] *= (double)g->dfi;
+    free(q); free(Hf); free(tw); free(sn);
+    return 0;
+}
+
 /* adjoint: scatter every voxel into the filtered-sample gradient, one
  * projection per task (no races), then filter and weight each row */
 typedef struct {

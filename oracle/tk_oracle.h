@@ -94,6 +94,14 @@ void orc_bp_f64(const double *q64, const orc_geom *g, const int *zlist, int nz, 
                 int row_lo, int nthreads);
 int orc_fdk_f64(const float *sino, const orc_geom *g, int window,
                 const int *zlist, int nz, double *vol, int nthreads);
+/* FP64 FDK of raw uint16 counts [N][H][W] on listed slices (log, weight,
+ * filter and backprojection in double, scalar dark/flat as
+ * orc_fdk_u16_f32_sampled), streaming the projections in small blocks so
+ * that memory stays O(rows x block x W): the oracle of the out-of-core path.
+ * vol [nz][Y][X] double. */
+int orc_fdk_u16_f64_sampled(const uint16_t *raw, double dark, double flat, double A, double B, int invert,
+                            double floor_counts, const orc_geom *g, int window,
+                            const int *zlist, int nz, double *vol, int nthreads);
 /* FP64 adjoint of the FDK A = B F W (line integrals -> volume, exact slice
  * centring): out = W F B^T vol, with B^T the transpose of the bilinear
  * backprojection (same masks and weights) and F the symmetric ramp filter.

@@ -102,6 +102,25 @@ def test_workspace_bytes(tklib):
     assert tklib.tk_filtered_bytes(ctypes.byref(g2), 1) == 3 * 5 * 62 * 8
 
 
+def test_stream_workspace_and_argument_checks(tklib):
+    g = small_geometry(W=60, N=10, H=7)
+    gc = g.to_c()
+    a = lambda x: (x + 255) // 256 * 256
+    # header + two raw chunks + one filtered chunk, each 256-byte aligned
+    assert tklib.tk_fdk_stream_workspace_bytes(ctypes.byref(gc), 1, 1, 4) == 256 + 2 * a(4 * 7 * 60 * 2) + a(
+        4 * 7 * 60 * 8)
+    assert tklib.tk_fdk_stream_workspace_bytes(ctypes.byref(gc), 0, 0, 64) == 256 + 2 * a(10 * 7 * 60 * 4) + a(
+        10 * 7 * 64 * 4)
+    assert tklib.tk_fdk_stream_workspace_bytes(ctypes.byref(gc), 0, 0, 0) == 0
+    assert tklib.tk_fdk_stream_workspace_bytes(ctypes.byref(gc), 5, 0, 4) == 0
+    p = ctypes.c_void_p(256)
+    # chunk 0, null host input, workspace too small: rejected before any device work
+    assert tklib.tk_fdk_stream(ctypes.byref(gc), p, 0, None, 0, 0, 0, p, 1 << 20, p, None) == _lib.TK_ERR_INVALID
+    assert tklib.tk_fdk_stream(ctypes.byref(gc), None, 0, None, 0, 0, 4, p, 1 << 20, p, None) == _lib.TK_ERR_INVALID
+    assert tklib.tk_fdk_stream(ctypes.byref(gc), p, 0, None, 0, 0, 4, p, 16, p, None) == _lib.TK_ERR_INVALID
+    assert b"workspace" in tklib.tk_last_error()
+
+
 def test_handle_setters_and_state_errors(tklib):
     from tomokvas_gb300 import FilteredBackProjection
 

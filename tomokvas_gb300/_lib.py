@@ -26,6 +26,7 @@ EXPORTS = [
     "tk_version", "tk_last_error", "tk_get_free_mem_info", "tk_pad_length", "tk_default_zoff",
     "tk_zblock_offsets", "tk_device_error_flags", "tk_filter_projections", "tk_backproject",
     "tk_filtered_bytes", "tk_fdk_workspace_bytes", "tk_fdk_device", "tk_fdk_device_noalloc",
+    "tk_fdk_stream_workspace_bytes", "tk_fdk_stream",
     "tk_forward_project", "tk_filter_transpose", "tk_fdk_forward", "tk_fdk_backward", "tk_phantom_project", "tk_bp_variant_count",
     "tk_bp_variant_name", "tk_bp_variant_precision", "tk_bp_select_variant", "tk_fdk_create", "tk_fdk_destroy",
     "tk_fdk_set_gpu_id", "tk_fdk_set_block_size", "tk_fdk_set_allocation_limit", "tk_fdk_set_collecting",
@@ -109,6 +110,9 @@ def _declare(L):
     L.tk_filter_transpose.argtypes = [G, vp, ip, vp, ip, vp]
     L.tk_fdk_forward.argtypes = [G, vp, ip, ip, vp, ctypes.c_size_t, vp, vp]
     L.tk_fdk_backward.argtypes = [G, vp, ip, ip, vp, ctypes.c_size_t, vp, vp]
+    L.tk_fdk_stream_workspace_bytes.argtypes = [G, ip, ip, ip]
+    L.tk_fdk_stream_workspace_bytes.restype = ctypes.c_size_t
+    L.tk_fdk_stream.argtypes = [G, vp, ip, ctypes.POINTER(FlatField), ip, ip, ip, vp, ctypes.c_size_t, vp, vp]
     L.tk_fdk_device_noalloc.argtypes = [G, vp, ip, ip, ctypes.POINTER(FlatField), ip, ip, vp, vp]
     L.tk_phantom_project.argtypes = [G, ctypes.POINTER(ctypes.c_double), ip, ip, vp, vp]
     L.tk_bp_variant_count.restype = ip

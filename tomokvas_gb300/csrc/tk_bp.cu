@@ -24,6 +24,7 @@
 //    coefficient pairs {(Q, dV), (dU, dUV)} so that one LDS.64 + one packed
 //    HFMA2 give the two row interpolants, halving shared-memory traffic;
 //  * accumulation is FP32 in registers; each voxel is written once.
+#include "tk_bp_core.cuh"
 #include "tk_common.cuh"
 #include "tk_internal.h"
 
@@ -55,11 +56,6 @@ struct BPParams {
     const float *q_scale;       // device storage scale of the filtered projections, or null (= 1)
     float2 trig[kMaxParamProj]; // (cos, sin) per projection (kernel.cu:430-441)
 };
-
-__device__ __forceinline__ float flip(float v, unsigned mask)
-{
-    return __uint_as_float(__float_as_uint(v) ^ mask);
-}
 
 // Storage traits -------------------------------------------------------------
 struct StoreF32 {
@@ -98,8 +94,6 @@ __device__ __forceinline__ int2 footprint_origin(const BPParams &P, int b, int x
     const int by = (int)floorf(vmin) - 1;
     return make_int2(bx, by);
 }
-
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: a TMA stage never takes this long
 
 // ---------------------------------------------------------------------------
 // Direct FP32 backprojector: bilinear gathers straight from the staged
@@ -279,55 +273,6 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // for a 64-voxel z column.  Loads use 32-bit shared addresses (inline PTX)
 // so the address of an update is one IMAD.
 
-template <int PREC> struct Cimg;
-template <> struct Cimg<TK_F32_COEF> {
-    static constexpr int kBytes = 16, kAlign = 1;
-    static __device__ __forceinline__ float2 eval(uint32_t addr, float fu, float2)
-    {
-        float q, du, dv, duv;
-        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(q), "=f"(du), "=f"(dv), "=f"(duv) : "r"(addr));
-        return make_float2(fmaf(fu, du, q), fmaf(fu, duv, dv));
-    }
-};
-template <> struct Cimg<TK_F16> {
-    static constexpr int kBytes = 8, kAlign = 2;
-    static __device__ __forceinline__ float2 eval(uint32_t addr, float, float2 fu2raw)
-    {
-        uint32_t lo, hi;
-        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(lo), "=r"(hi) : "r"(addr));
-        const __half2 h = __hfma2(*reinterpret_cast<const __half2 *>(&hi),
-                                  *reinterpret_cast<const __half2 *>(&fu2raw.x),
-                                  *reinterpret_cast<const __half2 *>(&lo));
-        return __half22float2(h);
-    }
-};
-template <> struct Cimg<TK_BF16> {
-    static constexpr int kBytes = 8, kAlign = 2;
-    static __device__ __forceinline__ float2 eval(uint32_t addr, float, float2 fu2raw)
-    {
-        uint32_t lo, hi;
-        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(lo), "=r"(hi) : "r"(addr));
-        const __nv_bfloat162 h = __hfma2(*reinterpret_cast<const __nv_bfloat162 *>(&hi),
-                                         *reinterpret_cast<const __nv_bfloat162 *>(&fu2raw.x),
-                                         *reinterpret_cast<const __nv_bfloat162 *>(&lo));
-        return __bfloat1622float2(h);
-    }
-};
-
-// fu packed for the 16-bit HFMA2 (carried in the bits of a float2.x).
-template <int PREC> __device__ __forceinline__ float2 pack_fu(float fu)
-{
-    float2 r = make_float2(0.f, 0.f);
-    if constexpr (PREC == TK_F16) {
-        const __half2 h = __float2half2_rn(fu);
-        r.x = *reinterpret_cast<const float *>(&h);
-    } else if constexpr (PREC == TK_BF16) {
-        const __nv_bfloat162 h = __float2bfloat162_rn(fu);
-        r.x = *reinterpret_cast<const float *>(&h);
-    }
-    return r;
-}
-
 // Bounding-box origin (entries) of a tile's footprint; the z range is
 // [z0, z1] in slab slices.
 template <int TX, int TY, int ALIGN>
@@ -355,29 +300,6 @@ __device__ __forceinline__ int2 footprint_origin_z(const BPParams &P, int b, int
     int bx = (int)floorf(umin) - 1;
     bx &= ~(ALIGN - 1);
     return make_int2(bx, (int)floorf(vmin) - 1);
-}
-
-template <int PREC, int TZ, bool ALL_IN, bool PARTIAL>
-__device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu,
-                                            float U2, float Hm1, int zlast, float (&acc)[TZ])
-{
-    const float2 fu2 = pack_fu<PREC>(fu);
-#pragma unroll
-    for (int z = 0; z < TZ; ++z) {
-        if (PARTIAL && z > zlast) break;
-        const float v = fmaf((float)z, dv, v0);
-        const float fl = __fadd_rd(v, kMagic);
-        const float fv = v - (fl - kMagic);
-        const uint32_t addr = (uint32_t)__float_as_int(fl) * row_bytes + sbase;
-        const float2 ab = Cimg<PREC>::eval(addr, fu, fu2);
-        const float val = fmaf(fv, ab.y, ab.x);
-        if constexpr (ALL_IN) {
-            acc[z] = fmaf(U2, val, acc[z]);
-        } else {
-            const float w = (v >= 0.f && v <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
-            acc[z] = fmaf(w, val, acc[z]);
-        }
-    }
 }
 
 template <int PREC, int TX, int TY, int TZ, int STAGES, bool PARTIAL, int MINB>
@@ -735,7 +657,7 @@ static int box_dims(const tk_geometry &g, int nz, float zoff, const BPVariant &v
 }
 
 int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale, int nz,
-                       float zoff, float *d_vol, int accumulate, cudaStream_t stream)
+                       float zoff, float *d_vol, int accumulate, cudaStream_t stream, int angle0)
 {
     if (int rc = validate_geometry(&g)) return rc;
     TK_CHECK(d_q && d_vol, TK_ERR_INVALID, "backproject: null device pointer");
@@ -756,8 +678,9 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     if (int rc = box_dims(g, nz, zoff, *v, align, &BW, &BH)) return rc;
     TK_CHECK(!v->coef || BW * ES / 4 <= 256, TK_ERR_UNSUPPORTED, "tile footprint of %d entries too wide", BW);
 
+    TK_CHECK(angle0 >= 0, TK_ERR_INVALID, "backproject: negative first angle index");
     std::vector<float> cs(g.N), sn(g.N);
-    build_trig(g, cs.data(), sn.data());
+    build_trig(g, cs.data(), sn.data(), angle0);
     const int p = reference_pad_length(g.W);
 
     const int tilesX = (g.X + v->TX - 1) / v->TX, tilesY = (g.Y + v->TY - 1) / v->TY;

@@ -1,0 +1,99 @@
+// tk_bp_core.cuh -- device pieces shared by the backprojection kernels
+// (per-volume kernels in tk_bp.cu, the batched persistent kernel in
+// tk_batch.cu): axis sign flips, the coefficient-image storage traits and
+// the z-column update.
+#pragma once
+
+#include "tk_common.cuh"
+
+namespace tk {
+
+__device__ __forceinline__ float flip(float v, unsigned mask)
+{
+    return __uint_as_float(__float_as_uint(v) ^ mask);
+}
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: a TMA stage never takes this long
+
+// Coefficient-image storage (see tk_precision): entry (r, c) covers the
+// detector cell [r, r+1] x [c, c+1], so an update is one shared load of one
+// entry and
+//   A = Q + fu dU,  B = dV + fu dUV,  acc += U^2 (A + fv B)
+// (FP16/BF16: A and B come from one packed HFMA2).  Loads use 32-bit shared
+// addresses (inline PTX) so the address of an update is one IMAD.
+template <int PREC> struct Cimg;
+template <> struct Cimg<TK_F32_COEF> {
+    static constexpr int kBytes = 16, kAlign = 1;
+    static __device__ __forceinline__ float2 eval(uint32_t addr, float fu, float2)
+    {
+        float q, du, dv, duv;
+        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(q), "=f"(du), "=f"(dv), "=f"(duv) : "r"(addr));
+        return make_float2(fmaf(fu, du, q), fmaf(fu, duv, dv));
+    }
+};
+template <> struct Cimg<TK_F16> {
+    static constexpr int kBytes = 8, kAlign = 2;
+    static __device__ __forceinline__ float2 eval(uint32_t addr, float, float2 fu2raw)
+    {
+        uint32_t lo, hi;
+        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(lo), "=r"(hi) : "r"(addr));
+        const __half2 h = __hfma2(*reinterpret_cast<const __half2 *>(&hi),
+                                  *reinterpret_cast<const __half2 *>(&fu2raw.x),
+                                  *reinterpret_cast<const __half2 *>(&lo));
+        return __half22float2(h);
+    }
+};
+template <> struct Cimg<TK_BF16> {
+    static constexpr int kBytes = 8, kAlign = 2;
+    static __device__ __forceinline__ float2 eval(uint32_t addr, float, float2 fu2raw)
+    {
+        uint32_t lo, hi;
+        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(lo), "=r"(hi) : "r"(addr));
+        const __nv_bfloat162 h = __hfma2(*reinterpret_cast<const __nv_bfloat162 *>(&hi),
+                                         *reinterpret_cast<const __nv_bfloat162 *>(&fu2raw.x),
+                                         *reinterpret_cast<const __nv_bfloat162 *>(&lo));
+        return __bfloat1622float2(h);
+    }
+};
+
+// fu packed for the 16-bit HFMA2 (carried in the bits of a float2.x).
+template <int PREC> __device__ __forceinline__ float2 pack_fu(float fu)
+{
+    float2 r = make_float2(0.f, 0.f);
+    if constexpr (PREC == TK_F16) {
+        const __half2 h = __float2half2_rn(fu);
+        r.x = *reinterpret_cast<const float *>(&h);
+    } else if constexpr (PREC == TK_BF16) {
+        const __nv_bfloat162 h = __float2bfloat162_rn(fu);
+        r.x = *reinterpret_cast<const float *>(&h);
+    }
+    return r;
+}
+
+// One column's update over a TZ-voxel z walk, v_z = v0 + z dv, reading the
+// entries of the staged box at sbase (shared address, already offset by the
+// column and by -(kMagicBits + box row origin) rows).
+template <int PREC, int TZ, bool ALL_IN, bool PARTIAL>
+__device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu,
+                                            float U2, float Hm1, int zlast, float (&acc)[TZ])
+{
+    const float2 fu2 = pack_fu<PREC>(fu);
+#pragma unroll
+    for (int z = 0; z < TZ; ++z) {
+        if (PARTIAL && z > zlast) break;
+        const float v = fmaf((float)z, dv, v0);
+        const float fl = __fadd_rd(v, kMagic);
+        const float fv = v - (fl - kMagic);
+        const uint32_t addr = (uint32_t)__float_as_int(fl) * row_bytes + sbase;
+        const float2 ab = Cimg<PREC>::eval(addr, fu, fu2);
+        const float val = fmaf(fv, ab.y, ab.x);
+        if constexpr (ALL_IN) {
+            acc[z] = fmaf(U2, val, acc[z]);
+        } else {
+            const float w = (v >= 0.f && v <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
+            acc[z] = fmaf(w, val, acc[z]);
+        }
+    }
+}
+
+}  // namespace tk

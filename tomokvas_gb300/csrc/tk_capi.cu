@@ -6,6 +6,7 @@
 #include "tk_common.cuh"
 #include "tk_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -60,10 +61,10 @@ int validate_geometry(const tk_geometry *g)
 
 // CalcSinCos (kernel.cu:430-441): beta_rad = beta * delta_f + rot is formed
 // in float, sin/cos are taken in double and stored as float.
-void build_trig(const tk_geometry &g, float *cos_out, float *sin_out)
+void build_trig(const tk_geometry &g, float *cos_out, float *sin_out, int angle0)
 {
     for (int b = 0; b < g.N; ++b) {
-        const float bf = (float)b * g.dfi;
+        const float bf = (float)(angle0 + b) * g.dfi;
         const double beta_rad = (double)(float)(bf + g.rot);
         cos_out[b] = (float)std::cos(beta_rad);
         sin_out[b] = (float)std::sin(beta_rad);
@@ -190,6 +191,100 @@ extern "C" int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_t
     void *d_q = static_cast<char *>(d_workspace) + kWsHeader;
     if (int rc = launch_filter(*g, d_in, input_type, layout, ff, window, d_q, precision, d_scale, st)) return rc;
     return launch_backproject(*g, d_q, precision, d_scale, g->Z, tk_default_zoff(g), d_vol, 0, st);
+}
+
+// ---------------------------------------------------------------- out-of-core
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static size_t input_elem_bytes(int input_type) { return input_type == TK_INPUT_U16 ? 2 : 4; }
+
+extern "C" size_t tk_fdk_stream_workspace_bytes(const tk_geometry *g, int input_type, int precision, int chunk)
+{
+    if (!g || !valid_precision(precision) || chunk <= 0 || g->N <= 0 || g->H <= 0 || g->W <= 0) return 0;
+    if (input_type != TK_INPUT_F32 && input_type != TK_INPUT_U16) return 0;
+    tk_geometry gc = *g;
+    gc.N = std::min(chunk, g->N);
+    const size_t raw = (size_t)gc.N * g->H * g->W * input_elem_bytes(input_type);
+    return kWsHeader + 2 * align256(raw) + align256(filtered_bytes(gc, precision));
+}
+
+namespace {
+// Streams and events of one tk_fdk_stream call, released on every return
+// path (release is deferred by the runtime until their work has finished).
+struct StreamSet {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t start = nullptr, copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+    ~StreamSet()
+    {
+        for (cudaEvent_t e : {start, copied[0], copied[1], consumed[0], consumed[1]})
+            if (e) cudaEventDestroy(e);
+        if (copy) cudaStreamDestroy(copy);
+    }
+};
+}  // namespace
+
+extern "C" int tk_fdk_stream(const tk_geometry *g, const void *h_in, int input_type, const tk_flatfield *ff,
+                             int window, int precision, int chunk, void *d_workspace, size_t workspace_bytes,
+                             float *d_vol, void *stream)
+{
+    if (int rc = validate_geometry(g)) return rc;
+    TK_CHECK(valid_precision(precision), TK_ERR_INVALID, "bad precision %d", precision);
+    TK_CHECK(input_type == TK_INPUT_F32 || input_type == TK_INPUT_U16, TK_ERR_INVALID, "bad input type %d",
+             input_type);
+    TK_CHECK(h_in && d_vol, TK_ERR_INVALID, "stream: null pointer");
+    TK_CHECK(chunk > 0, TK_ERR_INVALID, "stream: chunk must be > 0");
+    const size_t need = tk_fdk_stream_workspace_bytes(g, input_type, precision, chunk);
+    TK_CHECK(d_workspace && workspace_bytes >= need, TK_ERR_INVALID, "workspace of %zu B needed, %zu given", need,
+             workspace_bytes);
+    TK_CHECK((reinterpret_cast<uintptr_t>(d_workspace) & 255) == 0, TK_ERR_INVALID,
+             "workspace must be 256-byte aligned");
+    const int C = std::min(chunk, g->N);
+    const int nchunks = (g->N + C - 1) / C;
+    const size_t frame = (size_t)g->H * g->W * input_elem_bytes(input_type);
+    char *ws = static_cast<char *>(d_workspace);
+    float *d_scale = reinterpret_cast<float *>(ws);
+    char *raw[2] = {ws + kWsHeader, ws + kWsHeader + align256(frame * C)};
+    void *d_q = ws + kWsHeader + 2 * align256(frame * C);
+    const char *host = static_cast<const char *>(h_in);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    StreamSet ss;
+    TK_CUDA(cudaStreamCreateWithFlags(&ss.copy, cudaStreamNonBlocking));
+    TK_CUDA(cudaEventCreateWithFlags(&ss.start, cudaEventDisableTiming));
+    for (int i = 0; i < 2; ++i) {
+        TK_CUDA(cudaEventCreateWithFlags(&ss.copied[i], cudaEventDisableTiming));
+        TK_CUDA(cudaEventCreateWithFlags(&ss.consumed[i], cudaEventDisableTiming));
+    }
+    // copies start only after the caller's earlier work on `stream` (which may use the workspace)
+    TK_CUDA(cudaEventRecord(ss.start, st));
+    TK_CUDA(cudaStreamWaitEvent(ss.copy, ss.start, 0));
+    auto copy_chunk = [&](int k) -> int {
+        const int b0 = k * C, nb = std::min(C, g->N - b0);
+        TK_CUDA(cudaMemcpyAsync(raw[k & 1], host + (size_t)b0 * frame, (size_t)nb * frame, cudaMemcpyHostToDevice,
+                                ss.copy));
+        TK_CUDA(cudaEventRecord(ss.copied[k & 1], ss.copy));
+        return TK_OK;
+    };
+    if (int rc = copy_chunk(0)) return rc;
+    if (nchunks > 1)
+        if (int rc = copy_chunk(1)) return rc;
+    const float zoff = tk_default_zoff(g);
+    for (int k = 0; k < nchunks; ++k) {
+        const int slot = k & 1, b0 = k * C;
+        tk_geometry gc = *g;
+        gc.N = std::min(C, g->N - b0);
+        TK_CUDA(cudaStreamWaitEvent(st, ss.copied[slot], 0));
+        if (int rc = launch_filter(gc, raw[slot], input_type, TK_LAYOUT_PROJECTION, ff, window, d_q, precision,
+                                   d_scale, st))
+            return rc;
+        TK_CUDA(cudaEventRecord(ss.consumed[slot], st));
+        if (int rc = launch_backproject(gc, d_q, precision, d_scale, g->Z, zoff, d_vol, k > 0, st, b0)) return rc;
+        if (k + 2 < nchunks) {
+            TK_CUDA(cudaStreamWaitEvent(ss.copy, ss.consumed[slot], 0));  // raw[slot] is free again
+            if (int rc = copy_chunk(k + 2)) return rc;
+        }
+    }
+    return TK_OK;
 }
 
 // ------------------------------------------------------------- adjoint pair

@@ -35,15 +35,18 @@ inline bool valid_precision(int p) { return p >= TK_F32 && p <= TK_F32_COEF; }
 int validate_geometry(const tk_geometry *g);
 int reference_pad_length(int W);
 
-// Angle tables exactly as CalcSinCos builds them (FBPG/kernel.cu:430-441).
-void build_trig(const tk_geometry &g, float *cos_out, float *sin_out);
+// Angle tables exactly as CalcSinCos builds them (FBPG/kernel.cu:430-441),
+// for projections angle0 .. angle0 + g.N - 1.
+void build_trig(const tk_geometry &g, float *cos_out, float *sin_out, int angle0 = 0);
 
 // Launchers (asynchronous on `stream`).
 int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int layout,
                   const tk_flatfield *ff, int window, void *d_q, int precision, float *d_q_scale,
                   cudaStream_t stream);
+// d_q holds g.N projections whose angle indices start at angle0 (a chunk of
+// a longer scan when angle0 > 0).
 int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale,
-                       int nz, float zoff, float *d_vol, int accumulate, cudaStream_t stream);
+                       int nz, float zoff, float *d_vol, int accumulate, cudaStream_t stream, int angle0 = 0);
 int launch_filter_transpose(const tk_geometry &g, const float *d_qbar, int window, float *d_pbar, int layout,
                             cudaStream_t stream);
 int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, float zoff, float *d_qbar,

@@ -109,6 +109,31 @@ def fdk_device(g, d_in, input_type=_lib.TK_INPUT_F32, layout=_lib.TK_LAYOUT_SINO
     return vol
 
 
+def stream_workspace_bytes(g, input_type=_lib.TK_INPUT_U16, precision=_lib.TK_F16, chunk=64) -> int:
+    gc = _geom(g)
+    return int(load().tk_fdk_stream_workspace_bytes(ctypes.byref(gc), input_type, precision, int(chunk)))
+
+
+def fdk_stream(g, h_in, input_type=_lib.TK_INPUT_U16, ff=None, window=_lib.TK_WINDOW_RAMLAK,
+               precision=_lib.TK_F16, chunk=64, workspace=None, vol=None, stream=None, device=None):
+    """Out-of-core FDK: h_in is a host (preferably pinned) tensor or array of
+    projection-major [N][H][W] data, streamed to the GPU in chunks."""
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else device
+    if workspace is None:
+        workspace = torch.empty(stream_workspace_bytes(g, input_type, precision, chunk), dtype=torch.uint8,
+                                device=dev)
+    if vol is None:
+        vol = torch.empty((g.Z, g.Y, g.X), dtype=torch.float32, device=dev)
+    ptr = h_in.data_ptr() if hasattr(h_in, "data_ptr") else h_in.ctypes.data
+    check(L.tk_fdk_stream(ctypes.byref(gc), ptr, input_type, None if ff is None else ctypes.byref(ff), window,
+                          precision, int(chunk), workspace.data_ptr(), workspace.numel(), vol.data_ptr(),
+                          _stream_ptr(stream)))
+    return vol
+
+
 def forward_project(g, vol, nz=None, zoff=None, out=None, accumulate=False, stream=None):
     """B^T: transpose of the backprojection; returns [N][H][Wp] FP32."""
     torch = _torch()
