@@ -54,7 +54,14 @@ def parse():
     ap.add_argument("--outofcore", action="store_true",
                     help="out-of-core workload: 2048^3 from 1440 x 2048^2 uint16 streamed from pinned host "
                          "memory in chunks (FP16 filtered chunks), RMSE vs FP64 on 32 sampled slices")
+    ap.add_argument("--batch", action="store_true",
+                    help="batched workload: 64 seeded phantoms of uneven sizes (W in {128..512}, 90-360 "
+                         "projections, SOD/SDD 0.3-0.6, 96^3-384^3), one persistent launch / CUDA graph vs one "
+                         "launch per volume")
     ap.add_argument("--chunk", type=int, default=64, help="projections per streamed chunk (--outofcore)")
+    ap.add_argument("--profile-filter", choices=["f32", "f16", "bf16", "f32c"], default=None,
+                    help="small case for ncu: the u16 log + Hann filter of 90 x 1024^2 projections into one "
+                         "storage format; one untimed and two timed launches")
     ap.add_argument("--sweep", action="store_true", help="with --profile-bp: time every variant of that precision")
     ap.add_argument("--profile-bp", choices=["f32", "f16", "bf16", "f32c"], default=None,
                     help="small case for ncu: 180 x 1024^2 projections, a 64-slice slab of the 1024^2 volume; "
@@ -452,6 +459,46 @@ def run_profile_bp(args):
     return 0
 
 
+def run_profile_filter(args):
+    """Filter-only case small enough for an ncu capture: 90 x 1024^2 uint16 projections (189 MB in,
+    0.38-1.5 GB out, above L2)."""
+    import torch
+
+    from tomokvas_gb300 import _build, _lib, device
+
+    _build.build()
+    torch.cuda.set_device(0)
+    g = workload().replace(N=90, dfi=float(np.float32(2.0 * np.pi / 90)))
+    prec = _lib.PRECISIONS[args.profile_filter]
+    line = device.phantom_project(g, phantom(g), _lib.TK_LAYOUT_PROJECTION)
+    gen = torch.Generator(device="cuda").manual_seed(PHANTOM_SEED)
+    raw = torch.poisson(I0 * torch.exp(-line), generator=gen).clamp_(0, 65535).to(torch.int32).to(torch.int16)
+    del line
+    ff = device.flatfield(flat_value=I0, A=1.0, B=0.0, invert=True, floor_counts=0.5)
+    q, scale = device.alloc_filtered(g, prec)
+
+    def one():
+        device.filter_projections(g, raw, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff, _lib.TK_WINDOW_HANN,
+                                  prec, out=(q, scale))
+
+    one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(2):
+        one()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 2
+    samples = g.N * g.H * g.W
+    out_bytes = device.filtered_bytes(g, prec)
+    emit({"profile_filter": args.profile_filter, "ms_per_call": ms, "samples": samples,
+          "gsamples_per_s": samples / (ms * 1e-3) / 1e9,
+          "hbm_algorithmic_gbs": (samples * 2 + out_bytes) / (ms * 1e-3) / 1e9,
+          "flags": device.device_error_flags()})
+    return 0
+
+
 def run_adjoint(args):
     """A and A^T on the 512^3 / 360 x 768^2 differentiation workload."""
     import torch
@@ -570,10 +617,97 @@ def run_outofcore(args):
     return 0
 
 
+def batch_geometries(n=64, seed=3):
+    """The uneven batch: square detectors W in {128,192,256,384,512} at 0.2 mm, 90-360 projections,
+    SOD 300 mm with SOD/SDD in [0.3, 0.6], cubic volumes of 96-384 voxels covering the field of view
+    where the tile footprint allows (scale <= 1.5)."""
+    from tomokvas_gb300.geometry import FDKGeometry
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        W = int(rng.choice([128, 192, 256, 384, 512]))
+        N = int(rng.integers(90, 361))
+        ratio = float(rng.uniform(0.3, 0.6))
+        nv = int(rng.integers(96, 385))
+        sod, pitch = 300.0, 0.2
+        sdd = sod / ratio
+        s = min(0.9 * W / nv, 1.5)
+        out.append(FDKGeometry.circular(N, W, W, pitch, sod, sdd, (nv, nv, nv), s * pitch * sod / sdd))
+    return out
+
+
+def run_batch(args):
+    """64 uneven reconstructions: one launch per volume vs the batched persistent launch (eager and as a
+    CUDA graph), after the autotuner picked the batch's tile shape."""
+    import torch
+
+    from tomokvas_gb300 import _build, _lib, device
+    from tomokvas_gb300.batch import Batch
+    from tomokvas_gb300.phantom import random_ellipsoids
+
+    _build.build()
+    torch.cuda.set_device(0)
+    geos = batch_geometries()
+    prec = _lib.TK_F16
+    ins, vols, wss = [], [], []
+    for k, g in enumerate(geos):
+        ell = random_ellipsoids(20, g.fov_radius_cm, g.Z * g.voxel_cm / 2, seed=100 + k)
+        ins.append(device.phantom_project(g, ell, _lib.TK_LAYOUT_SINOGRAM))
+        vols.append(torch.empty((g.Z, g.Y, g.X), device="cuda"))
+        wss.append(torch.empty(device.workspace_bytes(g, prec), dtype=torch.uint8, device="cuda"))
+    updates = sum(g.updates for g in geos)
+    stream = torch.cuda.current_stream()
+
+    def timeit(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    def per_volume():
+        for g, x, v, w in zip(geos, ins, vols, wss):
+            device.fdk_device(g, x, precision=prec, workspace=w, vol=v)
+
+    ms_single = timeit(per_volume)
+    ref = [v[v.shape[0] // 2].cpu().numpy() for v in vols]
+    b = Batch(prec)
+    for g, x, v in zip(geos, ins, vols):
+        b.submit(g, x, v)
+    b.plan()
+    tuned, tune_ms = b.autotune()
+    ms_eager = timeit(lambda: b.run(graph=False))
+    ms_graph = timeit(lambda: b.run(graph=True))
+    diff = max(float(np.abs(v[v.shape[0] // 2].cpu().numpy() - r).max() / max(np.abs(r).max(), 1e-30))
+               for v, r in zip(vols, ref))
+    flags = device.device_error_flags()
+    emit({"workload": "batch_64_uneven_fdk", "metric": "GUPS", "unit": "GUPS", "items": len(geos),
+          "updates": updates, "storage": "f16 coefficients", "steps": args.steps, "warmup": args.warmup,
+          "per_volume": {"ms": ms_single, "gups": updates / (ms_single * 1e-3) / 1e9},
+          "batch_eager": {"ms": ms_eager, "gups": updates / (ms_eager * 1e-3) / 1e9},
+          "batch_graph": {"ms": ms_graph, "gups": updates / (ms_graph * 1e-3) / 1e9},
+          "speedup_graph_vs_per_volume": ms_single / ms_graph, "autotuned_variant": tuned,
+          "autotune_ms": tune_ms, "max_rel_diff_vs_per_volume_mid_slices": diff, "flags": flags,
+          "detector_widths": sorted({g.W for g in geos}),
+          "data": "synthetic: 64 seeded 20-ellipsoid phantoms, analytic FP32 line integrals (no dataset)"})
+    b.close()
+    return 0
+
+
 def main():
     args = parse()
+    if args.batch:
+        return run_batch(args)
     if args.adjoint:
         return run_adjoint(args)
+    if args.profile_filter:
+        return run_profile_filter(args)
     if args.outofcore:
         return run_outofcore(args)
     if args.profile_bp:

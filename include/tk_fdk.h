@@ -237,6 +237,43 @@ int tk_bp_select_variant(int i);
 int tk_phantom_project(const tk_geometry *g, const double *ell, int nell, int layout,
                        float *d_out, void *stream);
 
+/* ---------------------------------------------------------------- batches
+ * Many independent reconstructions of uneven detector, angle and volume sizes
+ * in one persistent backprojection launch.  Submit items (device input,
+ * output volume, geometry, filter), plan them onto one device workspace, then
+ * run: each item is filtered (one launch per item), then ONE persistent
+ * kernel backprojects the voxel tiles of all items, taken from a shared work
+ * counter, larger items first.  tk_batch_run(use_graph = 1) captures the run
+ * into a CUDA graph on first use and replays it afterwards (inputs are read
+ * from the submitted pointers at every run).  tk_batch_autotune times every
+ * compiled tile shape of the batch's storage format on the planned batch and
+ * keeps the fastest.  Storage is a coefficient image (TK_F16 by default, or
+ * TK_BF16 / TK_F32_COEF); W <= 2048.  Results equal tk_fdk_device's for the
+ * same tile shape.  No counterpart in the reference (one volume per process).
+ * A batch is not thread-safe; submitted buffers must outlive its runs. */
+typedef struct tk_batch tk_batch;
+int tk_batch_create(tk_batch **out);
+void tk_batch_destroy(tk_batch *b);
+int tk_batch_set_precision(tk_batch *b, int precision);
+/* Adds one item (index = tk_batch_size(b) - 1 after success). */
+int tk_batch_submit(tk_batch *b, const tk_geometry *g, const void *d_in, int input_type, int layout,
+                    const tk_flatfield *ff, int window, float *d_vol);
+int tk_batch_size(const tk_batch *b);
+size_t tk_batch_workspace_bytes(tk_batch *b);
+/* Lays out the workspace (256-byte aligned) and uploads the item tables;
+ * synchronises `stream`. */
+int tk_batch_plan(tk_batch *b, void *d_workspace, size_t workspace_bytes, void *stream);
+int tk_batch_run(tk_batch *b, int use_graph, void *stream);
+/* Times each tile shape of the storage format (3 runs each) and keeps the
+ * fastest; writes its index and time per run (ms).  Synchronous. */
+int tk_batch_autotune(tk_batch *b, void *stream, int *variant_out, float *ms_out);
+int tk_batch_variant_count(void);
+const char *tk_batch_variant_name(int i);
+/* The tile shape the planned batch uses (-1 before planning). */
+int tk_batch_variant(const tk_batch *b);
+/* Forces a tile shape (-1: default); takes effect at the next plan. */
+int tk_batch_select_variant(tk_batch *b, int i);
+
 /* ------------------------------ FilteredBackProjection mirror (handle) */
 /* One handle = one FilteredBackProjection object (kernel.cuh:82-151).
  * Call order as in FBPG/para_TC.cpp:130-153: setters -> initialize ->

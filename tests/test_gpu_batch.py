@@ -1,0 +1,138 @@
+"""Batches of uneven reconstructions (tk_batch_*): one persistent
+backprojection launch over every item's voxel tiles, eager or as a replayed
+CUDA graph.
+
+Checks:
+  * every item equals tk_fdk_device on the same input bit for bit, for each
+    storage format's default tile shape (the arithmetic and its order are the
+    per-volume kernel's); items cover sinogram and projection layouts, FP32
+    line integrals and raw uint16 counts, Ram-Lak and Hann, axis flips and a
+    rotation offset, scale != 1, a volume thinner than one z chunk and one
+    whose depth is not a multiple of it;
+  * a graph replay equals the eager run, and replays read the inputs anew;
+  * after the autotuner picks a tile shape, every item stays within the FP16
+    bound (5e-4 relative RMSE) of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from _util import rel_rmse, small_geometry
+from tomokvas_gb300 import _lib, device
+from tomokvas_gb300.batch import Batch, variants
+from tomokvas_gb300.phantom import counts_u16, head_phantom
+
+pytestmark = pytest.mark.gpu
+
+ITEMS = [
+    dict(geo=dict(W=64, N=72, H=56, vol=(48, 48, 40)), layout="sinogram", window="ramlak", raw=False),
+    dict(geo=dict(W=48, N=50, H=48, vol=(32, 36, 30), dirx=1, rot=0.3), layout="sinogram", window="ramlak",
+         raw=False),
+    dict(geo=dict(W=64, N=90, H=64, vol=(40, 40, 100)), layout="projection", window="hann", raw=False),
+    dict(geo=dict(W=32, N=40, H=32, vol=(24, 24, 24)), layout="projection", window="hann", raw=True),
+    dict(geo=dict(W=96, N=60, H=80, vol=(64, 64, 70), voxel_mm=1.0, diry=1, dirz=1), layout="sinogram",
+         window="shepp_logan", raw=False),
+]
+I0 = 60000.0
+
+
+@pytest.fixture(scope="module")
+def items(orc, cuda):
+    import torch
+
+    out = []
+    for k, it in enumerate(ITEMS):
+        g = small_geometry(**it["geo"])
+        G = orc.geom_from(g)
+        ell = head_phantom(g.fov_radius_cm * 0.85, seed=20 + k)
+        lay = "sino" if it["layout"] == "sinogram" else "proj"
+        p = orc.project_ellipsoids(ell, G, lay)
+        if it["raw"]:
+            host = counts_u16(p, I0, seed=30 + k)
+            d_in = torch.from_numpy(host.view(np.int16)).cuda()
+            ff = device.flatfield(flat_value=I0)
+            itype = _lib.TK_INPUT_U16
+        else:
+            host, d_in, ff, itype = p, torch.from_numpy(p).cuda(), None, _lib.TK_INPUT_F32
+        out.append(dict(g=g, G=G, host=host, d_in=d_in, ff=ff, itype=itype, layout=_lib.LAYOUTS[it["layout"]],
+                        window=_lib.WINDOWS[it["window"]]))
+    return out
+
+
+def single(it, precision):
+    return device.fdk_device(it["g"], it["d_in"], it["itype"], it["layout"], ff=it["ff"], window=it["window"],
+                             precision=precision)
+
+
+def make_batch(items, precision):
+    import torch
+
+    b = Batch(precision)
+    vols = []
+    for it in items:
+        v = torch.full((it["g"].Z, it["g"].Y, it["g"].X), float("nan"), device="cuda")
+        b.submit(it["g"], it["d_in"], v, it["itype"], it["layout"], it["ff"], it["window"])
+        vols.append(v)
+    b.plan()
+    return b, vols
+
+
+@pytest.mark.parametrize("precision", [_lib.TK_F16, _lib.TK_BF16, _lib.TK_F32_COEF])
+def test_batch_equals_per_volume(items, precision):
+    import torch
+
+    b, vols = make_batch(items, precision)
+    b.run(graph=False)
+    torch.cuda.synchronize()
+    for it, v in zip(items, vols):
+        np.testing.assert_array_equal(v.cpu().numpy(), single(it, precision).cpu().numpy())
+    assert device.device_error_flags() == 0
+    b.close()
+
+
+def test_graph_replay_equals_eager_and_rereads_inputs(items):
+    import torch
+
+    b, vols = make_batch(items, _lib.TK_F16)
+    b.run(graph=False)
+    torch.cuda.synchronize()
+    eager = [v.cpu().numpy() for v in vols]
+    for v in vols:
+        v.fill_(float("nan"))
+    b.run(graph=True)
+    b.run(graph=True)
+    torch.cuda.synchronize()
+    for e, v in zip(eager, vols):
+        np.testing.assert_array_equal(v.cpu().numpy(), e)
+    # replays read the submitted inputs anew: doubling an FP32 input doubles its volume
+    items[0]["d_in"].mul_(2.0)
+    try:
+        b.run(graph=True)
+        torch.cuda.synchronize()
+        np.testing.assert_allclose(vols[0].cpu().numpy(), 2.0 * eager[0], rtol=1e-6, atol=1e-6 * np.abs(eager[0]).max())
+        np.testing.assert_array_equal(vols[1].cpu().numpy(), eager[1])
+    finally:
+        items[0]["d_in"].mul_(0.5)
+    b.close()
+
+
+def test_autotuned_batch_vs_fp64(orc, items):
+    import torch
+
+    b, vols = make_batch(items, _lib.TK_F16)
+    name, ms = b.autotune()
+    assert name in [n for _, n in variants(_lib.TK_F16)] and ms > 0
+    assert b.variant == name
+    for v in vols:
+        v.fill_(float("nan"))
+    b.run(graph=True)
+    torch.cuda.synchronize()
+    for it, v in zip(items, vols):
+        if it["itype"] == _lib.TK_INPUT_U16:
+            ref = orc.fdk_u16_f64_sampled(it["host"], it["G"], I0, window=it["window"],
+                                          zlist=np.arange(it["g"].Z, dtype=np.int32))
+        else:
+            sino = it["host"] if it["layout"] == _lib.TK_LAYOUT_SINOGRAM else np.transpose(it["host"], (1, 0, 2))
+            ref = orc.fdk_f64(np.ascontiguousarray(sino), it["G"], it["window"])
+        assert rel_rmse(v.cpu().numpy(), ref) < 5e-4
+    assert device.device_error_flags() == 0
+    b.close()

@@ -17,9 +17,11 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "libtk_fdk.so")
-SOURCES = ["tk_capi.cu", "tk_filter.cu", "tk_bp.cu", "tk_phantom.cu", "tk_noalloc.cu"]
-HEADERS = ["tk_common.cuh", "tk_internal.h"]
+SOURCES = ["tk_capi.cu", "tk_filter.cu", "tk_bp.cu", "tk_batch.cu", "tk_phantom.cu", "tk_noalloc.cu"]
+HEADERS = ["tk_common.cuh", "tk_internal.h", "tk_bp_core.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CLI_SRC = os.path.join(PKG, "cli", "tk_para_tc.cpp")
+CLI = os.path.join(LIB_DIR, "tk_para_tc")
 
 
 def nvcc() -> str:
@@ -71,7 +73,26 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
             print(r.stdout + r.stderr)
             raise RuntimeError("linking libtk_fdk.so failed")
         os.replace(tmp, LIB)
+    build_cli(force)
     return LIB
+
+
+def build_cli(force: bool = False) -> str:
+    """The para_TC-equivalent driver (host C++ over libtk_fdk.so): lib/tk_para_tc."""
+    deps = [CLI_SRC, LIB] + [os.path.join(ROOT, "include", h) for h in ("tk_fdk.h", "tk_fdk.hpp", "tk_io.hpp")]
+    if not (force or _stale(CLI, deps)):
+        return CLI
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "include")
+    tmp = CLI + f".tmp{os.getpid()}"
+    cmd = ["g++", "-std=c++17", "-O2", "-pthread", "-I", os.path.join(ROOT, "include"), "-I", cuda_inc, CLI_SRC,
+           "-o", tmp, "-L", LIB_DIR, "-ltk_fdk", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        print(" ".join(cmd))
+        print(r.stdout + r.stderr)
+        raise RuntimeError("building tk_para_tc failed")
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":

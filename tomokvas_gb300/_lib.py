@@ -34,6 +34,9 @@ EXPORTS = [
     "tk_fdk_set_reconstruction_properties", "tk_fdk_set_scale_xyz", "tk_fdk_set_projections_u16",
     "tk_fdk_set_input_layout", "tk_fdk_set_filter", "tk_fdk_set_precision", "tk_fdk_set_stream",
     "tk_fdk_initialize", "tk_fdk_calculate_reconstruction", "tk_fdk_reconstruct_device", "tk_fdk_get_timings",
+    "tk_batch_create", "tk_batch_destroy", "tk_batch_set_precision", "tk_batch_submit", "tk_batch_size",
+    "tk_batch_workspace_bytes", "tk_batch_plan", "tk_batch_run", "tk_batch_autotune", "tk_batch_variant_count",
+    "tk_batch_variant_name", "tk_batch_variant", "tk_batch_select_variant",
 ]
 
 
@@ -120,6 +123,21 @@ def _declare(L):
     L.tk_bp_variant_name.restype = ctypes.c_char_p
     L.tk_bp_variant_precision.argtypes = [ip]
     L.tk_bp_select_variant.argtypes = [ip]
+    L.tk_batch_create.argtypes = [ctypes.POINTER(vp)]
+    L.tk_batch_destroy.argtypes = [vp]
+    L.tk_batch_destroy.restype = None
+    L.tk_batch_set_precision.argtypes = [vp, ip]
+    L.tk_batch_submit.argtypes = [vp, G, vp, ip, ip, ctypes.POINTER(FlatField), ip, vp]
+    L.tk_batch_size.argtypes = [vp]
+    L.tk_batch_workspace_bytes.argtypes = [vp]
+    L.tk_batch_workspace_bytes.restype = ctypes.c_size_t
+    L.tk_batch_plan.argtypes = [vp, vp, ctypes.c_size_t, vp]
+    L.tk_batch_run.argtypes = [vp, ip, vp]
+    L.tk_batch_autotune.argtypes = [vp, vp, ctypes.POINTER(ip), ctypes.POINTER(fp)]
+    L.tk_batch_variant_name.argtypes = [ip]
+    L.tk_batch_variant_name.restype = ctypes.c_char_p
+    L.tk_batch_variant.argtypes = [vp]
+    L.tk_batch_select_variant.argtypes = [vp, ip]
     H = vp
     L.tk_fdk_create.argtypes = [ctypes.POINTER(vp)]
     L.tk_fdk_destroy.argtypes = [H]

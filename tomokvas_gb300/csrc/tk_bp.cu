@@ -172,19 +172,15 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         }
         const int bx0 = boxo[b].x, by0 = boxo[b].y;
         if (active && got) {
-            const float2 cs = P.trig[b];
-            const float dcos = cs.x, dsin = cs.y;
-            const float Sd = aX * dcos + aY * dsin;
-            const float Td = aY * dcos - aX * dsin;
-            const float U = P.D / (P.D - Sd);
-            const float u = Td * U + P.cX;
+            float U, u;
+            column_geometry(aX, aY, P.trig[b], P.D, P.cX, U, u);
             if (u >= 0.f && u <= P.Wm1) {  // column inside the detector (kernel.cu:127-128)
-                const float U2 = U * U;
+                const float U2 = __fmul_rn(U, U);
                 const float fla = __fadd_rd(u, kMagic);
                 const int a = __float_as_int(fla) - kMagicBits;
                 const float fu = u - (fla - kMagic);
                 const int col = a - bx0;
-                const float vA = aZ[0] * U + cZ, vB = aZ[TZ - 1] * U + cZ;
+                const float vA = slice_v(aZ[0], U, cZ), vB = slice_v(aZ[TZ - 1], U, cZ);
                 const float vlo = fminf(vA, vB), vhi = fmaxf(vA, vB);
                 const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) + 1 - by0;
                 if (col >= 0 && col + 1 < P.BW && rlo >= 0 && rhi < P.BH) {
@@ -195,7 +191,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                         if (all_in) {
 #pragma unroll
                             for (int z = 0; z < TZ; ++z) {
-                                const float v = aZ[z] * U + cZ;
+                                const float v = slice_v(aZ[z], U, cZ);
                                 const float fl = __fadd_rd(v, kMagic);
                                 const float fv = v - (fl - kMagic);
                                 const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
@@ -208,7 +204,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                         } else {
 #pragma unroll
                             for (int z = 0; z < TZ; ++z) {
-                                const float v = aZ[z] * U + cZ;
+                                const float v = slice_v(aZ[z], U, cZ);
                                 const float fl = __fadd_rd(v, kMagic);
                                 const float fv = v - (fl - kMagic);
                                 const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
@@ -373,25 +369,22 @@ __global__ void __launch_bounds__(TX *TY, MINB)
             s_abort = 1;
         }
         if (active && got) {
-            const float2 cs = P.trig[b];
-            const float Sd = aX * cs.x + aY * cs.y;
-            const float Td = aY * cs.x - aX * cs.y;
-            const float U = P.D / (P.D - Sd);
-            const float u = Td * U + P.cX;
+            float U, u;
+            column_geometry(aX, aY, P.trig[b], P.D, P.cX, U, u);
             if (u >= 0.f && u <= P.Wm1) {  // column inside the detector (kernel.cu:127-128)
                 const int bx0 = boxo[b].x, by0 = boxo[b].y;
                 const float fla = __fadd_rd(u, kMagic);
                 const int col = __float_as_int(fla) - kMagicBits - bx0;
                 const float fu = u - (fla - kMagic);
-                const float v0 = aZ0 * U + cZ;
-                const float dv = daZ * U;
+                const float v0 = slice_v(aZ0, U, cZ);
+                const float dv = __fmul_rn(daZ, U);
                 const float vL = fmaf((float)zlast, dv, v0);
                 const float vlo = fminf(v0, vL), vhi = fmaxf(v0, vL);
                 const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) - by0;
                 if (col >= 0 && col < P.BW && rlo >= 0 && rhi < P.BH) {
                     const uint32_t sbase = smem0 + (uint32_t)s * P.stage_elems * ES + (uint32_t)col * ES -
                                            (uint32_t)(kMagicBits + by0) * row_bytes;
-                    const float U2 = U * U;
+                    const float U2 = __fmul_rn(U, U);
                     if (vlo >= 0.f && vhi <= Hm1)
                         update_cimg<PREC, TZ, true, PARTIAL>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                     else
@@ -511,17 +504,14 @@ __global__ void __launch_bounds__(TX *TY, 2)
     for (int b = 0; b < P.N; ++b) {
         const int bx0 = boxo[b].x, by0 = boxo[b].y;
         if (active) {
-            const float2 cs = P.trig[b];
-            const float Sd = aX * cs.x + aY * cs.y;
-            const float Td = aY * cs.x - aX * cs.y;
-            const float U = P.D / (P.D - Sd);
-            const float u = Td * U + P.cX;
+            float U, u;
+            column_geometry(aX, aY, P.trig[b], P.D, P.cX, U, u);
             if (u >= 0.f && u <= P.Wm1) {
                 const float fla = __fadd_rd(u, kMagic);
                 const int col = __float_as_int(fla) - kMagicBits - bx0;
                 const float fu = u - (fla - kMagic);
-                const float U2 = U * U;
-                const float v0 = aZf * U + cZ, vL = aZl * U + cZ;
+                const float U2 = __fmul_rn(U, U);
+                const float v0 = slice_v(aZf, U, cZ), vL = slice_v(aZl, U, cZ);
                 const float vlo = fmaxf(fminf(v0, vL), 0.f), vhi = fminf(fmaxf(v0, vL), Hm1);
                 if (vlo <= vhi) {
                     const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) + 1 - by0;
@@ -529,7 +519,7 @@ __global__ void __launch_bounds__(TX *TY, 2)
                         float *base = acc + col;
 #pragma unroll
                         for (int k = 0; k < TZ; ++k) {
-                            const float v = aZ[k] * U + cZ;
+                            const float v = slice_v(aZ[k], U, cZ);
                             if (g[k] != 0.f && v >= 0.f && v <= Hm1) {
                                 const float fl = __fadd_rd(v, kMagic);
                                 const float fv = v - (fl - kMagic);
@@ -629,7 +619,8 @@ static const BPVariant *pick_variant(int precision)
 // design notes): for two voxels of one tile,
 //   |du| <= s*dxy*Umax + Rmax*D/(D-Rmax)^2*s*dxy,
 //   |dv| <= s*(TZ-1)*Umax + |aZ|max*D/(D-Rmax)^2*s*dxy.
-static int box_dims(const tk_geometry &g, int nz, float zoff, const BPVariant &v, int align, int *BW, int *BH)
+int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ, bool coef, int align, int *BW,
+                int *BH)
 {
     const double s = std::fabs((double)g.scale), D = g.D;
     const double ex = s * std::fmax(std::fabs(0.0 - g.cx), std::fabs((double)(g.X - 1) - g.cx)) + 1.0;
@@ -638,17 +629,17 @@ static int box_dims(const tk_geometry &g, int nz, float zoff, const BPVariant &v
     TK_CHECK(D - R > 1e-3 * D, TK_ERR_UNSUPPORTED,
              "volume corners (radius %.1f px) reach the source (D = %.1f px)", R, D);
     const double Umax = D / (D - R), dU = D / ((D - R) * (D - R));
-    const double dxy = s * std::sqrt((double)(v.TX - 1) * (v.TX - 1) + (double)(v.TY - 1) * (v.TY - 1));
+    const double dxy = s * std::sqrt((double)(TX - 1) * (TX - 1) + (double)(TY - 1) * (TY - 1));
     const double azmax = s * std::fmax(std::fabs((double)zoff), std::fabs((double)(nz - 1) + zoff)) + 1.0;
     const double du = dxy * Umax + R * dU * dxy;
-    const double dv = s * (v.TZ - 1) * Umax + azmax * dU * dxy;
+    const double dv = s * (TZ - 1) * Umax + azmax * dU * dxy;
     // Sample boxes need columns floor(umin)-1 .. floor(umax)+1 plus the rounding
     // of the origin to the TMA granularity; coefficient entries cover a cell,
     // so their box is one column and one row smaller.  One extra of each
     // absorbs FP32-vs-FP64 differences of the device's corner evaluation.
-    int bw = (int)std::floor(du) + (v.coef ? 4 : 5) + align;
+    int bw = (int)std::floor(du) + (coef ? 4 : 5) + align;
     bw = (bw + align - 1) / align * align;
-    int bh = (int)std::floor(dv) + (v.coef ? 5 : 7);
+    int bh = (int)std::floor(dv) + (coef ? 5 : 7);
     TK_CHECK(bw <= 256 && bh <= 256, TK_ERR_UNSUPPORTED,
              "tile footprint %dx%d exceeds the 256x256 TMA box", bw, bh);
     *BW = bw;
@@ -675,7 +666,7 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     const int ES = (int)entry_size(precision);
     const int align = v->coef ? (ES >= 16 ? 1 : 16 / ES) : 4;
     int BW, BH;
-    if (int rc = box_dims(g, nz, zoff, *v, align, &BW, &BH)) return rc;
+    if (int rc = bp_box_dims(g, nz, zoff, v->TX, v->TY, v->TZ, v->coef, align, &BW, &BH)) return rc;
     TK_CHECK(!v->coef || BW * ES / 4 <= 256, TK_ERR_UNSUPPORTED, "tile footprint of %d entries too wide", BW);
 
     TK_CHECK(angle0 >= 0, TK_ERR_INVALID, "backproject: negative first angle index");
@@ -770,7 +761,7 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
 
     const BPVariant shape = {nullptr, nullptr, TK_F32, TX, TY, TZ, 2, false, "fp"};
     int BW, BH;
-    if (int rc = box_dims(g, nz, zoff, shape, 4, &BW, &BH)) return rc;
+    if (int rc = bp_box_dims(g, nz, zoff, shape.TX, shape.TY, shape.TZ, shape.coef, 4, &BW, &BH)) return rc;
     std::vector<float> cs(g.N), sn(g.N);
     build_trig(g, cs.data(), sn.data());
     const int p = reference_pad_length(g.W);

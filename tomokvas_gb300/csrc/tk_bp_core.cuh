@@ -15,6 +15,22 @@ __device__ __forceinline__ float flip(float v, unsigned mask)
 
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: a TMA stage never takes this long
 
+// Per column-angle geometry with every rounding spelled out:
+//   S = aX cos + aY sin,  T = aY cos - aX sin,  U = D / (D - S),  u = T U + cX
+// (kernel.cu:102-109).  Every kernel evaluates it through this function --
+// the per-volume backprojectors, the batched kernel and the forward
+// projector that must be their exact transpose -- so they get the same bits
+// whatever FMA contraction the compiler would otherwise pick per kernel.
+__device__ __forceinline__ void column_geometry(float aX, float aY, float2 cs, float D, float cX, float &U, float &u)
+{
+    const float S = fmaf(aX, cs.x, __fmul_rn(aY, cs.y));
+    const float T = fmaf(aY, cs.x, -__fmul_rn(aX, cs.y));
+    U = __fdiv_rn(D, __fsub_rn(D, S));
+    u = fmaf(T, U, cX);
+}
+// Detector row of slice coordinate aZ: aZ U + cZ with one rounding.
+__device__ __forceinline__ float slice_v(float aZ, float U, float cZ) { return fmaf(aZ, U, cZ); }
+
 // Coefficient-image storage (see tk_precision): entry (r, c) covers the
 // detector cell [r, r+1] x [c, c+1], so an update is one shared load of one
 // entry and

@@ -54,6 +54,12 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
 int launch_phantom(const tk_geometry &g, const double *ell, int nell, int layout, float *d_out,
                    cudaStream_t stream);
 
+// Analytic bound (entries) of the footprint box of a TX x TY x TZ voxel tile
+// in any projection, for sample (coef = false) or coefficient storage, with
+// the box width rounded to the TMA granularity `align`.
+int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ, bool coef, int align, int *BW,
+                int *BH);
+
 // Device error word of the current device (allocated on first use).
 unsigned *device_error_word();
 
