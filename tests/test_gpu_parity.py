@@ -79,6 +79,21 @@ def test_filter_stage_matches_oracle(orc, cuda, case, window, layout):
     assert rel_rmse(qd, np.transpose(q_ref, (1, 0, 2))) < 2e-6
 
 
+@pytest.mark.parametrize("W", [24, 33, 130, 300, 768, 1500, 2048, 4096])
+def test_filter_every_pad_length(orc, cuda, W):
+    """Every FFT pass schedule of the filter: p = 64 (16,4) ... 8192 (16,16,16,2)."""
+    import torch
+
+    g = small_geometry(W=W, N=3, H=5, vol=(16, 16, 8))
+    G = orc.geom_from(g)
+    rng = np.random.default_rng(W)
+    sino = rng.normal(size=(g.H, g.N, g.W)).astype(np.float32)
+    q_ref = orc.filter_f32(orc.weight_f32(sino, G), G, "hann")
+    q, _ = device.filter_projections(g, to_dev(sino, torch), window=_lib.TK_WINDOW_HANN)
+    torch.cuda.synchronize()
+    assert rel_rmse(q.cpu().numpy()[:, :, :g.W], np.transpose(q_ref, (1, 0, 2))) < 2e-6
+
+
 def coefficients_from_samples(q):
     """(Q, dU, dV, dUV) of every cell of q[N][H][W], samples outside are 0."""
     qp = np.zeros((q.shape[0], q.shape[1] + 1, q.shape[2] + 1), dtype=np.float64)
@@ -164,6 +179,33 @@ def test_every_bp_variant_matches_oracle(orc, cuda, case):
             assert device.device_error_flags() == 0, name
     finally:
         check(L.tk_bp_select_variant(-1))
+
+
+def test_packed_variants_equal_scalar(orc, cuda, case):
+    """The *_x2 variants walk two slices per step with packed FP32 but do the
+    same IEEE operations per voxel as the scalar walk: identical bits."""
+    import torch
+
+    g, G, ell, sino = case
+    g = g.replace(Z=100)  # full chunks and a moved-down last chunk
+    L = _lib.load()
+    names = {i: L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())}
+    pairs = [(i, j) for i, n in names.items() if "_x2<" in n
+             for j, m in names.items() if m == n.replace("_x2<", "<")]
+    assert pairs
+    try:
+        for i, j in pairs:
+            prec = L.tk_bp_variant_precision(i)
+            q, sc = device.filter_projections(g, to_dev(sino, torch), precision=prec)
+            sc = sc if prec in (_lib.TK_F16, _lib.TK_BF16) else None
+            out = []
+            for vi in (i, j):
+                _lib.check(L.tk_bp_select_variant(vi))
+                out.append(device.backproject(g, q, sc, prec).cpu().numpy())
+            np.testing.assert_array_equal(out[0], out[1])
+    finally:
+        _lib.check(L.tk_bp_select_variant(-1))
+    assert device.device_error_flags() == 0
 
 
 def test_fdk_f32_matches_restatement_and_fp64(orc, cuda, case):

@@ -239,11 +239,13 @@ struct BatchVariant {
     {reinterpret_cast<const void *>(&bp_batch_kernel<P, TX, TY, TZ, ST, MB>), P, TX, TY, TZ, ST, \
      "batch<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
-// The first entry of each storage format is its default.
+// The first entry of each storage format is its default, with the tile
+// shape of the per-volume default (tk_bp.cu) so that both give the same bits:
+// the z walk starts at each chunk's first slice, so results depend on TZ.
 static const BatchVariant kBatchVariants[] = {
     TK_BATCH(TK_F16, "f16", 16, 16, 64, 3, 2),
     TK_BATCH(TK_BF16, "bf16", 16, 16, 64, 3, 2),
-    TK_BATCH(TK_F32_COEF, "f32c", 16, 16, 32, 2, 2),
+    TK_BATCH(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
     TK_BATCH(TK_F16, "f16", 16, 16, 32, 3, 3),
     TK_BATCH(TK_F16, "f16", 16, 16, 48, 3, 2),
     TK_BATCH(TK_F16, "f16", 16, 16, 64, 2, 2),

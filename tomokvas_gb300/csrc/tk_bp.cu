@@ -95,10 +95,78 @@ __device__ __forceinline__ int2 footprint_origin(const BPParams &P, int b, int x
     return make_int2(bx, by);
 }
 
+// Bilinear interpolation and weighted accumulation of two voxels with packed
+// FP32: per lane exactly top = fma(fu, q01-q00, q00), bot = fma(fu, q11-q10,
+// q10), acc = fma(w, fma(fv, bot-top, top), acc).
+__device__ __forceinline__ void bilinear_acc_x2(float q00a, float q00b, float q01a, float q01b, float q10a,
+                                                float q10b, float q11a, float q11b, float fu, float fva, float fvb,
+                                                float wa, float wb, float &acc0, float &acc1)
+{
+    asm("{\n\t.reg .b64 Q00, Q01, Q10, Q11, FU, FV, W, C, D0, D1;\n\t"
+        "mov.b64 Q00, {%2, %3};\n\t"
+        "mov.b64 Q01, {%4, %5};\n\t"
+        "mov.b64 Q10, {%6, %7};\n\t"
+        "mov.b64 Q11, {%8, %9};\n\t"
+        "mov.b64 FU, {%10, %10};\n\t"
+        "mov.b64 FV, {%11, %12};\n\t"
+        "mov.b64 W, {%13, %14};\n\t"
+        "mov.b64 C, {%0, %1};\n\t"
+        "sub.rn.f32x2 D0, Q01, Q00;\n\t"
+        "sub.rn.f32x2 D1, Q11, Q10;\n\t"
+        "fma.rn.f32x2 Q00, FU, D0, Q00;\n\t"
+        "fma.rn.f32x2 Q10, FU, D1, Q10;\n\t"
+        "sub.rn.f32x2 D0, Q10, Q00;\n\t"
+        "fma.rn.f32x2 Q00, FV, D0, Q00;\n\t"
+        "fma.rn.f32x2 C, W, Q00, C;\n\t"
+        "mov.b64 {%0, %1}, C;\n\t}"
+        : "+f"(acc0), "+f"(acc1)
+        : "f"(q00a), "f"(q00b), "f"(q01a), "f"(q01b), "f"(q10a), "f"(q10b), "f"(q11a), "f"(q11b), "f"(fu),
+          "f"(fva), "f"(fvb), "f"(wa), "f"(wb));
+}
+
+// One column's update of the direct kernel over its TZ slices; PACKED walks
+// two slices per step with packed FP32 and gives the same bits.
+template <int TZ, bool ALL_IN, bool PACKED>
+__device__ __forceinline__ void direct_update(const float *st, uint32_t BW, uint32_t cbase, float fu, float U,
+                                              float U2, float cZ, float Hm1, const float (&aZ)[TZ], float (&acc)[TZ])
+{
+    if constexpr (PACKED && (TZ % 2 == 0)) {
+#pragma unroll
+        for (int z = 0; z < TZ; z += 2) {
+            const float va = slice_v(aZ[z], U, cZ), vb = slice_v(aZ[z + 1], U, cZ);
+            float fla, flb, fva, fvb;
+            floor_frac_x2(va, vb, fla, flb, fva, fvb);
+            const uint32_t oa = (uint32_t)__float_as_int(fla) * BW + cbase;
+            const uint32_t ob = (uint32_t)__float_as_int(flb) * BW + cbase;
+            float wa = U2, wb = U2;
+            if constexpr (!ALL_IN) {
+                wa = (va >= 0.f && va <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
+                wb = (vb >= 0.f && vb <= Hm1) ? U2 : 0.f;
+            }
+            bilinear_acc_x2(st[oa], st[ob], st[oa + 1], st[ob + 1], st[oa + BW], st[ob + BW], st[oa + BW + 1],
+                            st[ob + BW + 1], fu, fva, fvb, wa, wb, acc[z], acc[z + 1]);
+        }
+    } else {
+#pragma unroll
+        for (int z = 0; z < TZ; ++z) {
+            const float v = slice_v(aZ[z], U, cZ);
+            const float fl = __fadd_rd(v, kMagic);
+            const float fv = v - (fl - kMagic);
+            const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
+            const float q00 = st[o], q01 = st[o + 1];
+            const float q10 = st[o + BW], q11 = st[o + BW + 1];
+            const float top = fmaf(fu, q01 - q00, q00);
+            const float bot = fmaf(fu, q11 - q10, q10);
+            const float w = ALL_IN ? U2 : ((v >= 0.f && v <= Hm1) ? U2 : 0.f);  // kernel.cu:130-131
+            acc[z] = fmaf(w, fmaf(fv, bot - top, top), acc[z]);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Direct FP32 backprojector: bilinear gathers straight from the staged
 // sample tile (four LDS.32 per update).
-template <typename S, int TX, int TY, int TZ, int STAGES, int MINB>
+template <typename S, int TX, int TY, int TZ, int STAGES, int MINB, bool PACKED = false>
 __global__ void __launch_bounds__(TX *TY, MINB)
     bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
@@ -186,37 +254,11 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                 if (col >= 0 && col + 1 < P.BW && rlo >= 0 && rhi < P.BH) {
                     const uint32_t cbase = (uint32_t)col - (uint32_t)(kMagicBits + by0) * BW;
                     const bool all_in = (vlo >= 0.f) && (vhi <= Hm1);
-                    {
-                        const float *st = reinterpret_cast<const float *>(stages) + (size_t)s * P.stage_elems;
-                        if (all_in) {
-#pragma unroll
-                            for (int z = 0; z < TZ; ++z) {
-                                const float v = slice_v(aZ[z], U, cZ);
-                                const float fl = __fadd_rd(v, kMagic);
-                                const float fv = v - (fl - kMagic);
-                                const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
-                                const float q00 = st[o], q01 = st[o + 1];
-                                const float q10 = st[o + BW], q11 = st[o + BW + 1];
-                                const float top = fmaf(fu, q01 - q00, q00);
-                                const float bot = fmaf(fu, q11 - q10, q10);
-                                acc[z] = fmaf(U2, fmaf(fv, bot - top, top), acc[z]);
-                            }
-                        } else {
-#pragma unroll
-                            for (int z = 0; z < TZ; ++z) {
-                                const float v = slice_v(aZ[z], U, cZ);
-                                const float fl = __fadd_rd(v, kMagic);
-                                const float fv = v - (fl - kMagic);
-                                const uint32_t o = (uint32_t)__float_as_int(fl) * BW + cbase;
-                                const float q00 = st[o], q01 = st[o + 1];
-                                const float q10 = st[o + BW], q11 = st[o + BW + 1];
-                                const float top = fmaf(fu, q01 - q00, q00);
-                                const float bot = fmaf(fu, q11 - q10, q10);
-                                const float w = (v >= 0.f && v <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
-                                acc[z] = fmaf(w, fmaf(fv, bot - top, top), acc[z]);
-                            }
-                        }
-                    }
+                    const float *st = reinterpret_cast<const float *>(stages) + (size_t)s * P.stage_elems;
+                    if (all_in)
+                        direct_update<TZ, true, PACKED>(st, BW, cbase, fu, U, U2, cZ, Hm1, aZ, acc);
+                    else
+                        direct_update<TZ, false, PACKED>(st, BW, cbase, fu, U, U2, cZ, Hm1, aZ, acc);
                 } else {
                     atomicOr(P.err, ERR_BOX_OVERFLOW);
                 }
@@ -298,7 +340,7 @@ __device__ __forceinline__ int2 footprint_origin_z(const BPParams &P, int b, int
     return make_int2(bx, (int)floorf(vmin) - 1);
 }
 
-template <int PREC, int TX, int TY, int TZ, int STAGES, bool PARTIAL, int MINB>
+template <int PREC, int TX, int TY, int TZ, int STAGES, bool PARTIAL, int MINB, bool PACKED = false>
 __global__ void __launch_bounds__(TX *TY, MINB)
     bp_cimg_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
@@ -386,9 +428,9 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                                            (uint32_t)(kMagicBits + by0) * row_bytes;
                     const float U2 = __fmul_rn(U, U);
                     if (vlo >= 0.f && vhi <= Hm1)
-                        update_cimg<PREC, TZ, true, PARTIAL>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                        update_cimg<PREC, TZ, true, PARTIAL, PACKED>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                     else
-                        update_cimg<PREC, TZ, false, PARTIAL>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                        update_cimg<PREC, TZ, false, PARTIAL, PACKED>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                 } else {
                     atomicOr(P.err, ERR_BOX_OVERFLOW);
                 }
@@ -586,10 +628,18 @@ struct BPVariant {
 #define TK_BP_DIRECT(TX, TY, TZ, ST) \
     {reinterpret_cast<const void *>(&bp_tma_kernel<StoreF32, TX, TY, TZ, ST, 2>), nullptr, TK_F32, TX, TY, TZ, ST, \
      false, "direct<f32," #TX "," #TY "," #TZ "," #ST ">"}
+#define TK_BP_DIRECT_PK(TX, TY, TZ, ST) \
+    {reinterpret_cast<const void *>(&bp_tma_kernel<StoreF32, TX, TY, TZ, ST, 2, true>), nullptr, TK_F32, TX, TY, TZ, \
+     ST, false, "direct_x2<f32," #TX "," #TY "," #TZ "," #ST ">"}
 #define TK_BP_CIMG(P, PN, TX, TY, TZ, ST, MB) \
     {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB>), \
      reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB>), P, TX, TY, TZ, ST, true, \
      "cimg<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
+
+#define TK_BP_CIMG_PK(P, PN, TX, TY, TZ, ST, MB) \
+    {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB, true>), \
+     reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, true>), P, TX, TY, TZ, ST, true, \
+     "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
 // The first entry of each storage format is its default.
 static const BPVariant kVariants[] = {
@@ -602,6 +652,11 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG(TK_F16, "f16", 16, 16, 48, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
+    TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
+    TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
+    TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
+    TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 48, 3, 2),
+    TK_BP_DIRECT_PK(16, 16, 32, 4),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant

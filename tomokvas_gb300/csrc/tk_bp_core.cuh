@@ -89,25 +89,78 @@ template <int PREC> __device__ __forceinline__ float2 pack_fu(float fu)
 // One column's update over a TZ-voxel z walk, v_z = v0 + z dv, reading the
 // entries of the staged box at sbase (shared address, already offset by the
 // column and by -(kMagicBits + box row origin) rows).
-template <int PREC, int TZ, bool ALL_IN, bool PARTIAL>
+// Floor and fraction of two row coordinates with packed FP32 (one
+// add.rm.f32x2 and two sub.f32x2 for both lanes); per lane the same IEEE
+// operations as the scalar walk: fl = RD(v + M), fv = v - (fl - M).
+__device__ __forceinline__ void floor_frac_x2(float va, float vb, float &fla, float &flb, float &fva, float &fvb)
+{
+    asm("{\n\t.reg .b64 V, M, F, T;\n\t"
+        "mov.b64 V, {%4, %5};\n\t"
+        "mov.b64 M, {%6, %6};\n\t"
+        "add.rm.f32x2 F, V, M;\n\t"
+        "sub.rn.f32x2 T, F, M;\n\t"
+        "sub.rn.f32x2 T, V, T;\n\t"
+        "mov.b64 {%0, %1}, F;\n\t"
+        "mov.b64 {%2, %3}, T;\n\t}"
+        : "=f"(fla), "=f"(flb), "=f"(fva), "=f"(fvb)
+        : "f"(va), "f"(vb), "f"(kMagic));
+}
+// acc_i = fma(w_i, fma(fv_i, b_i, a_i), acc_i) for i = 0, 1 as two fma.rn.f32x2.
+__device__ __forceinline__ void interp_acc_x2(float aa, float ab, float ba, float bb, float fva, float fvb, float wa,
+                                              float wb, float &acc0, float &acc1)
+{
+    asm("{\n\t.reg .b64 A, B, FV, W, C;\n\t"
+        "mov.b64 A, {%2, %3};\n\t"
+        "mov.b64 B, {%4, %5};\n\t"
+        "mov.b64 FV, {%6, %7};\n\t"
+        "mov.b64 W, {%8, %9};\n\t"
+        "mov.b64 C, {%0, %1};\n\t"
+        "fma.rn.f32x2 A, FV, B, A;\n\t"
+        "fma.rn.f32x2 C, W, A, C;\n\t"
+        "mov.b64 {%0, %1}, C;\n\t}"
+        : "+f"(acc0), "+f"(acc1)
+        : "f"(aa), "f"(ab), "f"(ba), "f"(bb), "f"(fva), "f"(fvb), "f"(wa), "f"(wb));
+}
+
+// PACKED walks two slices per step with packed FP32 (floor/frac, the row
+// interpolation and the accumulation); per voxel it performs exactly the
+// operations of the scalar walk, so both give the same bits.
+template <int PREC, int TZ, bool ALL_IN, bool PARTIAL, bool PACKED = false>
 __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu,
                                             float U2, float Hm1, int zlast, float (&acc)[TZ])
 {
     const float2 fu2 = pack_fu<PREC>(fu);
+    if constexpr (PACKED && !PARTIAL && (TZ % 2 == 0)) {
 #pragma unroll
-    for (int z = 0; z < TZ; ++z) {
-        if (PARTIAL && z > zlast) break;
-        const float v = fmaf((float)z, dv, v0);
-        const float fl = __fadd_rd(v, kMagic);
-        const float fv = v - (fl - kMagic);
-        const uint32_t addr = (uint32_t)__float_as_int(fl) * row_bytes + sbase;
-        const float2 ab = Cimg<PREC>::eval(addr, fu, fu2);
-        const float val = fmaf(fv, ab.y, ab.x);
-        if constexpr (ALL_IN) {
-            acc[z] = fmaf(U2, val, acc[z]);
-        } else {
-            const float w = (v >= 0.f && v <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
-            acc[z] = fmaf(w, val, acc[z]);
+        for (int z = 0; z < TZ; z += 2) {
+            const float va = fmaf((float)z, dv, v0), vb = fmaf((float)(z + 1), dv, v0);
+            float fla, flb, fva, fvb;
+            floor_frac_x2(va, vb, fla, flb, fva, fvb);
+            const float2 x = Cimg<PREC>::eval((uint32_t)__float_as_int(fla) * row_bytes + sbase, fu, fu2);
+            const float2 y = Cimg<PREC>::eval((uint32_t)__float_as_int(flb) * row_bytes + sbase, fu, fu2);
+            float wa = U2, wb = U2;
+            if constexpr (!ALL_IN) {
+                wa = (va >= 0.f && va <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
+                wb = (vb >= 0.f && vb <= Hm1) ? U2 : 0.f;
+            }
+            interp_acc_x2(x.x, y.x, x.y, y.y, fva, fvb, wa, wb, acc[z], acc[z + 1]);
+        }
+    } else {
+#pragma unroll
+        for (int z = 0; z < TZ; ++z) {
+            if (PARTIAL && z > zlast) break;
+            const float v = fmaf((float)z, dv, v0);
+            const float fl = __fadd_rd(v, kMagic);
+            const float fv = v - (fl - kMagic);
+            const uint32_t addr = (uint32_t)__float_as_int(fl) * row_bytes + sbase;
+            const float2 ab = Cimg<PREC>::eval(addr, fu, fu2);
+            const float val = fmaf(fv, ab.y, ab.x);
+            if constexpr (ALL_IN) {
+                acc[z] = fmaf(U2, val, acc[z]);
+            } else {
+                const float w = (v >= 0.f && v <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
+                acc[z] = fmaf(w, val, acc[z]);
+            }
         }
     }
 }

@@ -31,6 +31,42 @@ constexpr int kMaxHf = 4097;  // p/2 + 1 for p <= 8192
 constexpr int kFiltThreads = 256;
 constexpr float kScaleTarget = 16384.f;  // bound of |stored value| for 16-bit storage
 
+// ---------------------------------------------------------------------------
+// Mixed-radix Stockham FFT in shared memory.
+//
+// A length p = 2^lg transform runs as radix-16 passes and one final radix
+// 8/4/2 pass (p = 2048: 16, 16, 8).  Pass m with span Ns and radix R maps
+// butterfly j (k = j mod Ns) as
+//   v[r] = x[j + r p/R] * w^(r k p/(R Ns)),  y[(j-k) R + k + s Ns] = DFT_R(v)[s],
+// one butterfly per thread, the R points in registers.  Buffers are padded by
+// one element per 16 (pidx), which makes every pass's loads and stores
+// conflict-free; twiddles come from per-pass tables laid out [k][r] (one
+// thread reads R-1 consecutive entries).
+struct FFTPlan {
+    int npass;
+    int R[5], Ns[5], off[5];  // radix, span and twiddle-table offset of each pass
+    int tw_total;             // twiddle entries of all passes
+};
+
+__host__ __device__ inline FFTPlan fft_plan(int lg)
+{
+    FFTPlan pl{};
+    int Ns = 1, rem = lg, off = 0;
+    while (rem > 0) {
+        const int b = rem >= 4 ? 4 : rem;
+        const int R = 1 << b;
+        pl.R[pl.npass] = R;
+        pl.Ns[pl.npass] = Ns;
+        pl.off[pl.npass] = off;
+        if (Ns > 1) off += Ns * (R - 1);
+        Ns *= R;
+        rem -= b;
+        ++pl.npass;
+    }
+    pl.tw_total = off;
+    return pl;
+}
+
 struct LoadParams {
     const void *in;
     const float *dark, *flat;
@@ -52,6 +88,7 @@ struct FiltParams {
     long long nunits;
     int out_layout;         // raw output: TK_LAYOUT_PROJECTION [N][H][Wp] or TK_LAYOUT_SINOGRAM [H][N][Wp]
     int weight_out;         // multiply the output by the cosine weight (the filter's transpose)
+    FFTPlan plan;           // passes of the length-p transform (fft_plan(lg))
     float Hf[kMaxHf];  // tau * |R2C_p(h)| * window, k = 0..p/2
 };
 
@@ -95,73 +132,174 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 
-// One radix-4 Stockham pass (decimation in time, twiddle before butterfly):
-//   v[r] = x[j + r p/4] * w^(k r p/(4 Ns)),  k = j mod Ns,
-//   y[(j-k)*4 + k + s Ns] = DFT4(v)[s].
-__device__ __forceinline__ void radix4_pass(const float2 *__restrict__ x, float2 *__restrict__ y,
-                                            const float2 *__restrict__ tw, int p, int Ns, int t, int TPF)
+// Padded index of element i of a transform buffer.
+__host__ __device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ int padded_len(int p) { return p + (p >> 4); }
+
+// Twiddle tables of every pass: entry (k, r) of pass m is w^(r k p/(R Ns)) =
+// exp(-2 pi i r k / (R Ns)), r = 1..R-1, k < Ns.  All threads of the CTA.
+__device__ __forceinline__ void fill_twiddles(float2 *twp, const FFTPlan &pl)
 {
-    const int q = p >> 2;
-    const int tstep = p / (Ns << 2);
-    for (int j = t; j < q; j += TPF) {
-        const int k = j & (Ns - 1);
-        float2 v0 = x[j], v1 = x[j + q], v2 = x[j + 2 * q], v3 = x[j + 3 * q];
-        if (Ns > 1) {
-            const int e = k * tstep;
-            v1 = cmul(v1, tw[e]);
-            v2 = cmul(v2, tw[2 * e]);
-            v3 = cmul(v3, tw[3 * e]);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        if (m >= pl.npass) break;
+        const int R = pl.R[m], Ns = pl.Ns[m];
+        if (Ns == 1) continue;
+        for (int i = threadIdx.x; i < Ns * (R - 1); i += blockDim.x) {
+            const int k = i / (R - 1), r = i - k * (R - 1) + 1;
+            float sn, cs;
+            sincospif(-2.0f * (float)(r * k) / (float)(R * Ns), &sn, &cs);  // exact argument: R Ns is 2^n
+            twp[pl.off[m] + i] = make_float2(cs, sn);
         }
-        const float2 a = make_float2(v0.x + v2.x, v0.y + v2.y);
-        const float2 b = make_float2(v0.x - v2.x, v0.y - v2.y);
-        const float2 c = make_float2(v1.x + v3.x, v1.y + v3.y);
-        const float2 d = make_float2(v1.x - v3.x, v1.y - v3.y);
-        const int o = ((j - k) << 2) + k;
-        y[o] = make_float2(a.x + c.x, a.y + c.y);
-        y[o + Ns] = make_float2(b.x + d.y, b.y - d.x);
-        y[o + 2 * Ns] = make_float2(a.x - c.x, a.y - c.y);
-        y[o + 3 * Ns] = make_float2(b.x - d.y, b.y + d.x);
     }
 }
 
-__device__ __forceinline__ void radix2_pass(const float2 *__restrict__ x, float2 *__restrict__ y,
-                                            const float2 *__restrict__ tw, int p, int Ns, int t, int TPF)
+// Forward DFTs of 2, 4, 8 and 16 points in registers (natural order).
+__device__ __forceinline__ void dft2(float2 &a, float2 &b)
 {
-    const int q = p >> 1;
-    const int tstep = p / (Ns << 1);
+    const float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+__device__ __forceinline__ void dft4(float2 &x0, float2 &x1, float2 &x2, float2 &x3)
+{
+    const float2 a = cadd(x0, x2), b = csub(x0, x2), c = cadd(x1, x3), d = csub(x1, x3);
+    x0 = cadd(a, c);
+    x2 = csub(a, c);
+    x1 = make_float2(b.x + d.y, b.y - d.x);  // b - i d
+    x3 = make_float2(b.x - d.y, b.y + d.x);  // b + i d
+}
+constexpr float kR2 = 0.70710678118654752440f;  // cos(pi/4)
+constexpr float kC8 = 0.92387953251128675613f;  // cos(pi/8)
+constexpr float kS8 = 0.38268343236508977173f;  // sin(pi/8)
+
+template <int R> __device__ __forceinline__ void dft(float2 (&v)[R]);
+template <> __device__ __forceinline__ void dft<2>(float2 (&v)[2]) { dft2(v[0], v[1]); }
+template <> __device__ __forceinline__ void dft<4>(float2 (&v)[4]) { dft4(v[0], v[1], v[2], v[3]); }
+// 8 = 2 x 4: X[k + 4h] = E0[k] + (-1)^h W8^k E1[k], E_e = DFT4(x[e], x[e+2], x[e+4], x[e+6]).
+template <> __device__ __forceinline__ void dft<8>(float2 (&v)[8])
+{
+    dft4(v[0], v[2], v[4], v[6]);
+    dft4(v[1], v[3], v[5], v[7]);
+    const float2 t1 = make_float2(kR2 * (v[3].x + v[3].y), kR2 * (v[3].y - v[3].x));   // W8^1 = (r, -r)
+    const float2 t2 = make_float2(v[5].y, -v[5].x);                                     // W8^2 = -i
+    const float2 t3 = make_float2(kR2 * (v[7].y - v[7].x), -kR2 * (v[7].x + v[7].y));  // W8^3 = (-r, -r)
+    const float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    v[0] = cadd(e0, v[1]);
+    v[4] = csub(e0, v[1]);
+    v[1] = cadd(e1, t1);
+    v[5] = csub(e1, t1);
+    v[2] = cadd(e2, t2);
+    v[6] = csub(e2, t2);
+    v[3] = cadd(e3, t3);
+    v[7] = csub(e3, t3);
+}
+// 16 = 4 x 4: E_e = DFT4(x[e], x[e+4], x[e+8], x[e+12]); T_e[k] = W16^(e k) E_e[k];
+// X[k + 4h] = DFT4_h(T_0[k], T_1[k], T_2[k], T_3[k]).
+template <> __device__ __forceinline__ void dft<16>(float2 (&v)[16])
+{
+#pragma unroll
+    for (int e = 0; e < 4; ++e) dft4(v[e], v[e + 4], v[e + 8], v[e + 12]);
+    // E_e[k] sits in v[e + 4k]; apply W16^(e k)
+    const float2 w1 = make_float2(kC8, -kS8), w2 = make_float2(kR2, -kR2), w3 = make_float2(kS8, -kC8);
+    const float2 w6 = make_float2(-kR2, -kR2), w9 = make_float2(-kC8, kS8);
+    v[5] = cmul(v[5], w1);                          // e=1,k=1
+    v[9] = cmul(v[9], w2);                          // e=1,k=2
+    v[13] = cmul(v[13], w3);                        // e=1,k=3
+    v[6] = cmul(v[6], w2);                          // e=2,k=1
+    v[10] = make_float2(v[10].y, -v[10].x);         // e=2,k=2: W16^4 = -i
+    v[14] = cmul(v[14], w6);                        // e=2,k=3
+    v[7] = cmul(v[7], w3);                          // e=3,k=1
+    v[11] = cmul(v[11], w6);                        // e=3,k=2
+    v[15] = cmul(v[15], w9);                        // e=3,k=3
+    float2 o[16];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float2 a = v[4 * k], b = v[4 * k + 1], c = v[4 * k + 2], d = v[4 * k + 3];
+        dft4(a, b, c, d);
+        o[k] = a;
+        o[k + 4] = b;
+        o[k + 8] = c;
+        o[k + 12] = d;
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = o[i];
+}
+
+template <int R>
+__device__ __forceinline__ void fft_pass(const float2 *__restrict__ x, float2 *__restrict__ y,
+                                         const float2 *__restrict__ tw, int p, int Ns, int t, int TPF)
+{
+    const int q = p / R;
     for (int j = t; j < q; j += TPF) {
         const int k = j & (Ns - 1);
-        const float2 v0 = x[j];
-        float2 v1 = x[j + q];
-        if (Ns > 1) v1 = cmul(v1, tw[k * tstep]);
-        const int o = ((j - k) << 1) + k;
-        y[o] = make_float2(v0.x + v1.x, v0.y + v1.y);
-        y[o + Ns] = make_float2(v0.x - v1.x, v0.y - v1.y);
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = x[pidx(j + r * q)];
+        if (Ns > 1) {
+            const float2 *w = tw + k * (R - 1) - 1;
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[r] = cmul(v[r], w[r]);
+        }
+        dft<R>(v);
+        const int o = (j - k) * R + k;
+#pragma unroll
+        for (int s2 = 0; s2 < R; ++s2) y[pidx(o + s2 * Ns)] = v[s2];
     }
 }
 
-// Forward FFT of length 2^lg; ping-pongs between a and b, returns the buffer
-// holding the result.  Every thread of the CTA calls it (barriers inside).
-__device__ __forceinline__ float2 *fft_forward(float2 *a, float2 *b, const float2 *tw, int p, int lg, int t, int TPF)
+// Forward FFT of length p (padded buffers); ping-pongs between a and b and
+// returns the buffer holding the result.  Every thread of the CTA calls it
+// (barriers inside).
+__device__ __forceinline__ float2 *fft_forward(float2 *a, float2 *b, const float2 *twp, const FFTPlan &pl, int p,
+                                               int t, int TPF)
 {
-    int Ns = 1, l = 0;
-    for (; l + 2 <= lg; l += 2) {
-        radix4_pass(a, b, tw, p, Ns, t, TPF);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {  // p <= 8192: at most four passes
+        if (m >= pl.npass) break;
+        const float2 *tw = twp + pl.off[m];
+        switch (pl.R[m]) {
+        case 16: fft_pass<16>(a, b, tw, p, pl.Ns[m], t, TPF); break;
+        case 8: fft_pass<8>(a, b, tw, p, pl.Ns[m], t, TPF); break;
+        case 4: fft_pass<4>(a, b, tw, p, pl.Ns[m], t, TPF); break;
+        default: fft_pass<2>(a, b, tw, p, pl.Ns[m], t, TPF); break;
+        }
         __syncthreads();
-        float2 *s = a;
+        float2 *s2 = a;
         a = b;
-        b = s;
-        Ns <<= 2;
-    }
-    if (l < lg) {
-        radix2_pass(a, b, tw, p, Ns, t, TPF);
-        __syncthreads();
-        float2 *s = a;
-        a = b;
-        b = s;
+        b = s2;
     }
     return a;
+}
+
+// Threads per transform (one radix-16 butterfly each) and groups per CTA.
+__host__ __device__ __forceinline__ int fft_threads(int p)
+{
+    const int t = (p >> 4) > 32 ? (p >> 4) : 32;
+    return t < kFiltThreads ? t : kFiltThreads;
+}
+
+// Shared-memory layout of the filter kernels: twiddle tables, the spectrum
+// Hf (p/2+1 floats), then per group two padded transform buffers and (for
+// coefficient output) the previous filtered row.
+struct FiltSmem {
+    int tw_total, hf_floats, group_bytes, groups;
+    __host__ __device__ size_t bytes() const
+    {
+        return (size_t)tw_total * 8 + (size_t)hf_floats * 4 + (size_t)groups * group_bytes;
+    }
+};
+__host__ __device__ inline FiltSmem filt_smem(int p, int tw_total, int W, bool coef)
+{
+    FiltSmem f;
+    f.tw_total = tw_total;
+    f.hf_floats = ((p / 2 + 1) + 3) & ~3;  // 16-byte multiple
+    f.group_bytes = 2 * padded_len(p) * 8 + (coef ? ((W + 3) & ~3) * 4 : 0);
+    f.groups = kFiltThreads / fft_threads(p);
+    return f;
 }
 
 template <typename T> __device__ __forceinline__ T store_cvt(float v);
@@ -185,17 +323,17 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
 {
     extern __shared__ __align__(16) float2 fsm[];
     const int p = P.p;
-    const int TPF = min(kFiltThreads, p >> 2);
+    const FFTPlan &pl = P.plan;
+    const FiltSmem lay = filt_smem(p, pl.tw_total, P.L.W, false);
+    const int TPF = fft_threads(p);
     const int G = kFiltThreads / TPF;
     const int grp = threadIdx.x / TPF, t = threadIdx.x - grp * TPF;
-    float2 *tw = fsm;  // exp(-2 pi i k / p), k < 3p/4 are used
-    float2 *bufA = fsm + p + (size_t)grp * 2 * p;
-    float2 *bufB = bufA + p;
-    for (int k = threadIdx.x; k < p; k += kFiltThreads) {
-        float s, c;
-        sincospif(-2.0f * (float)k / (float)p, &s, &c);
-        tw[k] = make_float2(c, s);
-    }
+    float2 *twp = fsm;
+    float *hf = reinterpret_cast<float *>(fsm + lay.tw_total);
+    float2 *bufA = reinterpret_cast<float2 *>(reinterpret_cast<char *>(hf + lay.hf_floats) + (size_t)grp * lay.group_bytes);
+    float2 *bufB = bufA + padded_len(p);
+    fill_twiddles(twp, pl);
+    for (int k = threadIdx.x; k <= p / 2; k += kFiltThreads) hf[k] = P.Hf[k];
     const float sigma = P.q_scale ? *P.q_scale : 1.f;
     const int W = P.L.W;
     T *out = static_cast<T *>(P.out);
@@ -216,32 +354,32 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
                     a = load_pre(P.L, oa, r_a, x);
                     if (hasb) b = load_pre(P.L, ob, r_b, x);
                 }
-                bufA[x] = make_float2(a, b);
+                bufA[pidx(x)] = make_float2(a, b);
             }
         }
         __syncthreads();
-        float2 *R = fft_forward(bufA, bufB, tw, p, P.lg, t, TPF);
+        float2 *R = fft_forward(bufA, bufB, twp, pl, p, t, TPF);
         float2 *Sb = (R == bufA) ? bufB : bufA;
         // conj(Z) * Hf (Hf real and even)
         for (int k = t; k < p; k += TPF) {
-            const float h = P.Hf[k <= (p >> 1) ? k : p - k];
-            const float2 z = R[k];
-            R[k] = make_float2(z.x * h, -z.y * h);
+            const float h = hf[k <= (p >> 1) ? k : p - k];
+            const float2 z = R[pidx(k)];
+            R[pidx(k)] = make_float2(z.x * h, -z.y * h);
         }
         __syncthreads();
-        float2 *Q = fft_forward(R, Sb, tw, p, P.lg, t, TPF);
+        float2 *Q = fft_forward(R, Sb, twp, pl, p, t, TPF);
         if (valid) {
             int r_a, r_b;
             T *qa = out + out_row_offset(P, ra, r_a);
             for (int i = t; i < W; i += TPF) {
                 const float w = P.weight_out ? cosine_weight(P.L, r_a, i) : 1.f;
-                qa[i] = store_cvt<T>(Q[i].x * sigma * w);
+                qa[i] = store_cvt<T>(Q[pidx(i)].x * sigma * w);
             }
             if (hasb) {
                 T *qb = out + out_row_offset(P, rb, r_b);
                 for (int i = t; i < W; i += TPF) {
                     const float w = P.weight_out ? cosine_weight(P.L, r_b, i) : 1.f;
-                    qb[i] = store_cvt<T>(-Q[i].y * sigma * w);
+                    qb[i] = store_cvt<T>(-Q[pidx(i)].y * sigma * w);
                 }
             }
         }
@@ -290,11 +428,11 @@ template <> struct CoefStore<TK_BF16> {
 // the kept previous row; index W reads as 0.
 struct RowRe {
     const float2 *q; float s; int W;
-    __device__ __forceinline__ float operator()(int c) const { return c < W ? q[c].x * s : 0.f; }
+    __device__ __forceinline__ float operator()(int c) const { return c < W ? q[pidx(c)].x * s : 0.f; }
 };
 struct RowNegIm {
     const float2 *q; float s; int W;
-    __device__ __forceinline__ float operator()(int c) const { return c < W ? -q[c].y * s : 0.f; }
+    __device__ __forceinline__ float operator()(int c) const { return c < W ? -q[pidx(c)].y * s : 0.f; }
 };
 struct RowBuf {
     const float *q; int W;
@@ -319,18 +457,18 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
 {
     extern __shared__ __align__(16) float2 fsm[];
     const int p = P.p;
-    const int TPF = min(kFiltThreads, p >> 2);
+    const FFTPlan &pl = P.plan;
+    const FiltSmem lay = filt_smem(p, pl.tw_total, P.L.W, true);
+    const int TPF = fft_threads(p);
     const int G = kFiltThreads / TPF;
     const int grp = threadIdx.x / TPF, t = threadIdx.x - grp * TPF;
-    float2 *tw = fsm;
-    float2 *bufA = fsm + p + (size_t)grp * 3 * p;
-    float2 *bufB = bufA + p;
-    float *prev = reinterpret_cast<float *>(bufB + p);  // W floats
-    for (int k = threadIdx.x; k < p; k += kFiltThreads) {
-        float sn, cs;
-        sincospif(-2.0f * (float)k / (float)p, &sn, &cs);
-        tw[k] = make_float2(cs, sn);
-    }
+    float2 *twp = fsm;
+    float *hf = reinterpret_cast<float *>(fsm + lay.tw_total);
+    float2 *bufA = reinterpret_cast<float2 *>(reinterpret_cast<char *>(hf + lay.hf_floats) + (size_t)grp * lay.group_bytes);
+    float2 *bufB = bufA + padded_len(p);
+    float *prev = reinterpret_cast<float *>(bufB + padded_len(p));  // W floats
+    fill_twiddles(twp, pl);
+    for (int k = threadIdx.x; k <= p / 2; k += kFiltThreads) hf[k] = P.Hf[k];
     const float sigma = P.q_scale ? *P.q_scale : 1.f;
     const int W = P.L.W, H = P.L.H, RC = P.rc;
     const int Wc = MODE == TK_F32_COEF ? W : ((W + 1) & ~1);
@@ -360,19 +498,19 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
                         va = load_pre(P.L, oa, ra, x);
                         if (hasb) vb = load_pre(P.L, ob, rb, x);
                     }
-                    bufA[x] = make_float2(va, vb);
+                    bufA[pidx(x)] = make_float2(va, vb);
                 }
             }
             __syncthreads();
-            float2 *R = fft_forward(bufA, bufB, tw, p, P.lg, t, TPF);
+            float2 *R = fft_forward(bufA, bufB, twp, pl, p, t, TPF);
             float2 *Sb = (R == bufA) ? bufB : bufA;
             for (int kk = t; kk < p; kk += TPF) {
-                const float h = P.Hf[kk <= (p >> 1) ? kk : p - kk];
-                const float2 z = R[kk];
-                R[kk] = make_float2(z.x * h, -z.y * h);
+                const float h = hf[kk <= (p >> 1) ? kk : p - kk];
+                const float2 z = R[pidx(kk)];
+                R[pidx(kk)] = make_float2(z.x * h, -z.y * h);
             }
             __syncthreads();
-            const float2 *Q = fft_forward(R, Sb, tw, p, P.lg, t, TPF);
+            const float2 *Q = fft_forward(R, Sb, twp, pl, p, t, TPF);
             if (live) {
                 const size_t base = (size_t)b * H;
                 const RowRe rowa{Q, sigma, W};
@@ -390,7 +528,7 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
             }
             __syncthreads();
             if (live && hasb)
-                for (int c = t; c < W; c += TPF) prev[c] = -Q[c].y * sigma;
+                for (int c = t; c < W; c += TPF) prev[c] = -Q[pidx(c)].y * sigma;
             __syncthreads();
         }
     }
@@ -508,16 +646,14 @@ static const Spectrum &spectrum(int W, float tau, int window, int p)
 static int launch_filter_typed(const FiltParams &P, int p, cudaStream_t stream, int precision)
 {
     const void *fn = nullptr;
-    size_t per_group = 2;  // complex buffers of p per FFT group
     switch (precision) {
     case TK_F32: fn = reinterpret_cast<const void *>(&filter_fft_kernel<float>); break;
-    case TK_F16: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_F16>); per_group = 3; break;
-    case TK_BF16: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_BF16>); per_group = 3; break;
-    default: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_F32_COEF>); per_group = 3; break;
+    case TK_F16: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_F16>); break;
+    case TK_BF16: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_BF16>); break;
+    default: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_F32_COEF>); break;
     }
-    const int TPF = std::min(kFiltThreads, p >> 2);
-    const int G = kFiltThreads / TPF;
-    const size_t smem = (size_t)p * sizeof(float2) * (1 + per_group * (size_t)G);
+    const int G = kFiltThreads / fft_threads(p);
+    const size_t smem = filt_smem(p, P.plan.tw_total, P.L.W, is_coef(precision)).bytes();
     TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "filter: pad length %d needs too much shared memory", p);
     TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, sms = 0, per_sm = 0;
@@ -589,6 +725,7 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     int lg = 0;
     while ((1 << lg) < p) ++lg;
     P.lg = lg;
+    P.plan = fft_plan(lg);
     P.precision = precision;
     P.rc = 64;
     P.nchunks = (g.H + P.rc - 1) / P.rc;
@@ -662,6 +799,7 @@ int launch_filter_transpose(const tk_geometry &g, const float *d_qbar, int windo
     int lg = 0;
     while ((1 << lg) < p) ++lg;
     P.lg = lg;
+    P.plan = fft_plan(lg);
     P.precision = TK_F32;
     std::memcpy(P.Hf, sp.Hf.data(), sizeof(float) * sp.Hf.size());
     return launch_filter_typed(P, p, stream, TK_F32);
