@@ -58,6 +58,10 @@ def parse():
                     help="batched workload: 64 seeded phantoms of uneven sizes (W in {128..512}, 90-360 "
                          "projections, SOD/SDD 0.3-0.6, 96^3-384^3), one persistent launch / CUDA graph vs one "
                          "launch per volume")
+    ap.add_argument("--reference-gpu", action="store_true",
+                    help="time the reference's own kernels (FBPG/kernel.cu built for sm_103a, cuFFT) on this GPU "
+                         "at the 256^3 and 1024^3 workloads beside ours on the same log sinograms (Ram-Lak), "
+                         "with the relative RMSE between the two")
     ap.add_argument("--chunk", type=int, default=64, help="projections per streamed chunk (--outofcore)")
     ap.add_argument("--profile-filter", choices=["f32", "f16", "bf16", "f32c"], default=None,
                     help="small case for ncu: the u16 log + Hann filter of 90 x 1024^2 projections into one "
@@ -172,6 +176,26 @@ def emit(obj):
     print(json.dumps(obj), flush=True)
 
 
+# ------------------------------------------------- replicas (N > 1 ranks)
+# One process per GPU, each reconstructing its own volume: no collective on
+# the data path.  The only cross-rank steps are the barriers around the timed
+# region and the maximum of the per-rank times.
+def ranks_max(x: float, dist=None, device="cuda") -> float:
+    """Maximum of x over all ranks (x itself without a process group)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_gups(updates_per_rank: int, world: int, seconds: float) -> float:
+    """Whole-job throughput: every rank did updates_per_rank in at most `seconds`."""
+    return world * updates_per_rank / seconds / 1e9
+
+
 # --------------------------------------------------------- reference arm
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
@@ -227,11 +251,7 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return ranks_max(x, dist)
 
     g = workload()
     ell = phantom(g)
@@ -297,8 +317,8 @@ def run_ours(args):
     plain_name = min(plain_runs, key=lambda k: plain_runs[k][0][0])
     (ms32, f32_filter, f32_bp, _), vol32 = plain_runs[plain_name]
     plain_alt = {k: {"ms_per_step": v[0][0], "bp_ms": v[0][2], "filter_ms": v[0][1]} for k, v in plain_runs.items()}
-    value = world * upd / (ms16 * 1e-3) / 1e9
-    plain = world * upd / (ms32 * 1e-3) / 1e9
+    value = replica_gups(upd, world, ms16 * 1e-3)
+    plain = replica_gups(upd, world, ms32 * 1e-3)
     flags = device.device_error_flags()
 
     # end to end through the reference-facing handle: pinned host raw in, pinned host volume out
@@ -337,7 +357,7 @@ def run_ours(args):
         barrier()
         e2e_s = max_over_ranks((time.perf_counter() - t0) / K)
         fbp.close()
-        e2e = {"value": world * upd / e2e_s / 1e9, "unit": "GUPS", "s_per_volume": e2e_s,
+        e2e = {"value": replica_gups(upd, world, e2e_s), "unit": "GUPS", "s_per_volume": e2e_s,
                "h2d_bytes_per_step": int(raw.numel() * 2), "d2h_bytes_per_step": int(g.X * g.Y * g.Z * 4),
                "api": "C ABI tk_fdk_* (FilteredBackProjection mirror): u16 projections from pinned host, "
                       "volume to pinned host via the bin_siz-style block sink, 128-slice blocks"}
@@ -700,8 +720,81 @@ def run_batch(args):
     return 0
 
 
+def run_reference_gpu(args):
+    """The reference's FDK kernels vs ours on the same GPU and inputs.  The
+    reference reads FP32 log sinograms [H][N][W] and has only the Ram-Lak
+    filter, so both sides get that; its Z blocks are 30 slices (setting.xml)."""
+    import torch
+
+    from oracle import ref_build, refrun
+    from tomokvas_gb300 import _build, _lib, device
+    from tomokvas_gb300.geometry import config
+
+    _build.build()
+    torch.cuda.set_device(0)
+    if ref_build.build_fatbin() is None:
+        emit({"reference_gpu": "unavailable: oracle/_ref/tk_ref_kernels.fatbin missing"})
+        return 0
+    out = {}
+    for name, seed in (("c1", 1), ("c2", 2)):
+        g = config(name).replace(zb=30)
+        from tomokvas_gb300.phantom import random_ellipsoids
+
+        ell = random_ellipsoids(40, g.fov_radius_cm, g.Z * g.voxel_cm / 2, seed=seed)
+        line = device.phantom_project(g, ell, _lib.TK_LAYOUT_SINOGRAM)
+        gen = torch.Generator(device="cuda").manual_seed(seed)
+        counts = torch.poisson(I0 * torch.exp(-line), generator=gen).clamp_(min=0.5)
+        sino = -torch.log(counts / I0)  # FP32 log sinogram [H][N][W], the reference's input
+        del line, counts
+        host = sino.cpu().numpy()
+        # ours, same input, Ram-Lak: FP32 samples (the reference's arithmetic) and the chosen FP16 form
+        res = {}
+        vols = {}
+        for pname, prec in (("f32", _lib.TK_F32), ("f16", _lib.TK_F16)):
+            ws = torch.empty(device.workspace_bytes(g, prec), dtype=torch.uint8, device="cuda")
+            vol = torch.empty((g.Z, g.Y, g.X), device="cuda")
+            for _ in range(2):
+                device.fdk_device(g, sino, precision=prec, workspace=ws, vol=vol)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(3):
+                device.fdk_device(g, sino, precision=prec, workspace=ws, vol=vol)
+            e1.record()
+            torch.cuda.synchronize()
+            res[pname] = e0.elapsed_time(e1) / 3
+            vols[pname] = vol.cpu().numpy()
+            del ws, vol
+        del sino
+        torch.cuda.empty_cache()
+        times = {}
+        refrun.fdk(host, g, times) if name == "c1" else None  # warm-up (module load, cuFFT plans) on the small case
+        t0 = time.perf_counter()
+        ref = refrun.fdk(host, g, times)
+        wall = time.perf_counter() - t0
+        computed = slice(0, g.Z - 1) if (g.Z - 1) % g.zb == 0 else slice(0, g.Z)  # the reference's last-slice quirk
+        den = float(np.sqrt(np.mean(ref[computed].astype(np.float64) ** 2)))
+        rm = {k: float(np.sqrt(np.mean((v[computed].astype(np.float64) - ref[computed]) ** 2)) / den)
+              for k, v in vols.items()}
+        out[name] = {"volume": [g.X, g.Y, g.Z], "projections": [g.N, g.H, g.W], "updates": g.updates,
+                     "reference": {**times, "wall_s": wall, "gups_bp_kernels": g.updates / (times["bp_kernels_ms"] * 1e-3) / 1e9,
+                                   "gups_total": g.updates / (times["total_ms"] * 1e-3) / 1e9},
+                     "ours_ms": {"f32_samples": res["f32"], "f16_coefficients": res["f16"]},
+                     "ours_gups": {k: g.updates / (v * 1e-3) / 1e9 for k, v in res.items()},
+                     "speedup_total_f32": times["total_ms"] / res["f32"],
+                     "speedup_total_f16": times["total_ms"] / res["f16"],
+                     "rel_rmse_vs_reference": rm}
+        del host, ref, vols
+    emit({"reference_gpu": out, "note": "reference = FBPG/kernel.cu compiled for sm_103a and driven in its own "
+          "stage order with cuFFT (oracle/tk_refrun.cpp); times are its wall clock with its own device "
+          "synchronisations; ours = tk_fdk_device, inputs resident in HBM, CUDA events"})
+    return 0
+
+
 def main():
     args = parse()
+    if args.reference_gpu:
+        return run_reference_gpu(args)
     if args.batch:
         return run_batch(args)
     if args.adjoint:

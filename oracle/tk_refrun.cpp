@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -127,16 +128,34 @@ unsigned blocks(size_t n, unsigned b) { return (unsigned)std::ceil((float)n / b)
 
 extern "C" const char *tkref_last_error(void) { return g_msg.c_str(); }
 
+using Clock = std::chrono::steady_clock;
+static double ms_since(Clock::time_point t0)
+{
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
 // sino: host [H][N][W]; vol_out: host [Z][Y][X] (slices the reference never
-// computes stay 0).  Returns 0 on success.
+// computes stay 0).  times_ms (optional, 6 entries, wall clock with the
+// reference's own device synchronisations): [0] upload (Initialize),
+// [1] cosine weight (fRBcomma), [2] filter (fConvolution), [3] backprojection
+// kernels (sum of FBPConeKernel CUDA-event times), [4] reconstruction loop
+// with its per-block D2H (CalculateReconstruction), [5] total.  Returns 0 on
+// success.
 extern "C" int tkref_fdk(const char *fatbin, const float *sino, int W, float cX, int N, int H, float cZ, float dfi,
                          float D, float tau, int X, float cx, int Y, float cy, int Z, float cz, float rot, float scale,
-                         int dirx, int diry, int dirz, int zb, float *vol_out)
+                         int dirx, int diry, int dirz, int zb, float *vol_out, float *times_ms)
 {
     RT(cudaSetDevice(0));
     RT(cudaFree(nullptr));  // primary context for the driver API calls
     Kernels k;
     if (find_kernels(fatbin, k)) return -1;
+    double t_upload = 0, t_weight = 0, t_filter = 0, t_recon = 0;
+    float t_bp = 0;
+    cudaEvent_t e0, e1;
+    RT(cudaEventCreate(&e0));
+    RT(cudaEventCreate(&e1));
+    const auto t_start = Clock::now();
+    auto t0 = Clock::now();
 
     sin_par_t sing;
     std::memset(&sing, 0, sizeof(sing));
@@ -163,6 +182,9 @@ extern "C" int tkref_fdk(const char *fatbin, const float *sino, int W, float cX,
     float dcorZ = (nblk - nr_Z) * zb / 2;
     RT(cudaMallocPitch((void **)&recn.dev_reconstruction, &recn.rec_p, X * sizeof(float), (size_t)Y * zb));
 
+    RT(cudaDeviceSynchronize());
+    t_upload = ms_since(t0);
+
     // CalcSinCos
     std::vector<float> ds(N), dc(N);
     for (int beta = 0; beta < N; beta++) {
@@ -176,13 +198,16 @@ extern "C" int tkref_fdk(const char *fatbin, const float *sino, int W, float cX,
     RT(cudaMemcpy(sing.dev_dcos, dc.data(), N * sizeof(float), cudaMemcpyHostToDevice));
 
     // fRBcomma
+    t0 = Clock::now();
     {
         void *args[] = {&sing};
         DRV(cuLaunchKernel(k.rb, blocks(N, 16), blocks(H, 16), 1, 16, 16, 1, 0, nullptr, args, nullptr));
         RT(cudaDeviceSynchronize());
     }
+    t_weight = ms_since(t0);
 
     // fConvolution
+    t0 = Clock::now();
     int p = 2;
     while (p < W) p *= 2;
     p *= 2;
@@ -228,20 +253,39 @@ extern "C" int tkref_fdk(const char *fatbin, const float *sino, int W, float cX,
     cudaFree(dev_data);
     cudaFree(dev_abs);
     cudaFree(dev_filter);
+    RT(cudaDeviceSynchronize());
+    t_filter = ms_since(t0);
 
     // CalculateReconstruction
     std::memset(vol_out, 0, sizeof(float) * (size_t)X * Y * Z);
+    t0 = Clock::now();
     recn.ZBlockSize = zb;
     for (int n = 0; n < nblk; n++) {
         recn.dZ = dZ + (n - (float)nblk / 2.) * zb + dcorZ;
         void *args[] = {&recn, &sing};
+        RT(cudaEventRecord(e0));
         DRV(cuLaunchKernel(k.fbp, blocks(X, 8), blocks(Y, 8), blocks(zb, 8), 8, 8, 8, 0, nullptr, args, nullptr));
+        RT(cudaEventRecord(e1));
         RT(cudaDeviceSynchronize());
+        float ms = 0.f;
+        RT(cudaEventElapsedTime(&ms, e0, e1));
+        t_bp += ms;
         int slices = zb;
         if ((n + 1) * zb > Z) slices = Z - n * zb;
         RT(cudaMemcpy2D(vol_out + (size_t)n * zb * X * Y, X * sizeof(float), recn.dev_reconstruction, recn.rec_p,
                         X * sizeof(float), (size_t)Y * slices, cudaMemcpyDeviceToHost));
     }
+    t_recon = ms_since(t0);
+    if (times_ms) {
+        times_ms[0] = (float)t_upload;
+        times_ms[1] = (float)t_weight;
+        times_ms[2] = (float)t_filter;
+        times_ms[3] = t_bp;
+        times_ms[4] = (float)t_recon;
+        times_ms[5] = (float)ms_since(t_start);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     cudaFree(recn.dev_reconstruction);
     cudaFree(sing.dev_sinogram[0]);
     cudaFree(sing.dev_dsin);
