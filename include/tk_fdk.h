@@ -237,6 +237,20 @@ int tk_bp_select_variant(int i);
 int tk_phantom_project(const tk_geometry *g, const double *ell, int nell, int layout,
                        float *d_out, void *stream);
 
+/* ------------------------------------------------ fan-beam rsq helpers
+ * Offset-detector (half-fan) sinogram completion and fan->parallel
+ * rebinning of `rows` independent fan-beam sinograms d_in [rows][N][W]
+ * (FP32) with the rotation axis at column axis_move, source distance D
+ * (pixels, D > W) and angle step dfi (a full 360-degree scan):
+ * rsq::Half2FullFan (FBPG/rsq_load.cpp:327-380) writes d_out
+ * [rows][N][2W-1-2 axis_move] (flip: angles in reverse order);
+ * rsq::Half2Para / Fan2Para (FBPG/rsq_load.cpp:382-470) writes d_out
+ * [rows][N/2][2W-1-2 axis_move].  Asynchronous on `stream`. */
+int tk_half_to_full_fan(const float *d_in, int W, int N, int rows, int axis_move, double D, double dfi, int flip,
+                        float *d_out, void *stream);
+int tk_half_to_parallel(const float *d_in, int W, int N, int rows, int axis_move, double D, double dfi,
+                        float *d_out, void *stream);
+
 /* ---------------------------------------------------------------- batches
  * Many independent reconstructions of uneven detector, angle and volume sizes
  * in one persistent backprojection launch.  Submit items (device input,

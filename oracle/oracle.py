@@ -95,6 +95,9 @@ def _declare(L):
                                           i32p, ctypes.c_int, f32p, ctypes.c_int]
     L.orc_fdk_u16_f64_sampled.argtypes = [P(ctypes.c_uint16), d, d, d, d, ctypes.c_int, d, gp, ctypes.c_int,
                                           i32p, ctypes.c_int, f64p, ctypes.c_int]
+    L.orc_half2fullfan_f64.argtypes = [f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d,
+                                       ctypes.c_int, f64p]
+    L.orc_half2para_f64.argtypes = [f64p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, d, d, f64p]
     L.orc_log_u16_f64.argtypes = [P(ctypes.c_uint16), f32p, f32p, ctypes.c_int, ctypes.c_int,
                                   ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_double, f32p, ctypes.c_int]
@@ -203,6 +206,25 @@ def fdk_u16_f64_sampled(raw: np.ndarray, g: Geom, flat: float, dark: float = 0.0
     if rc:
         raise MemoryError("oracle fdk_u16_f64_sampled failed")
     return vol
+
+
+def half2fullfan(sino: np.ndarray, axis_move: int, D: float, dfi: float, flip=False) -> np.ndarray:
+    """Half-fan completion of sinograms [rows][N][W] (double)."""
+    x = np.ascontiguousarray(sino, dtype=np.float64)
+    rows, N, W = x.shape
+    out = np.empty((rows, N, 2 * W - 1 - 2 * axis_move), dtype=np.float64)
+    lib().orc_half2fullfan_f64(_ptr(x, ctypes.c_double), W, N, rows, axis_move, D, dfi, int(bool(flip)),
+                               _ptr(out, ctypes.c_double))
+    return out
+
+
+def half2para(sino: np.ndarray, axis_move: int, D: float, dfi: float) -> np.ndarray:
+    """Fan->parallel rebinning of half-fan sinograms [rows][N][W] (double)."""
+    x = np.ascontiguousarray(sino, dtype=np.float64)
+    rows, N, W = x.shape
+    out = np.empty((rows, N // 2, 2 * W - 1 - 2 * axis_move), dtype=np.float64)
+    lib().orc_half2para_f64(_ptr(x, ctypes.c_double), W, N, rows, axis_move, D, dfi, _ptr(out, ctypes.c_double))
+    return out
 
 
 def fdk_adjoint_f64(vol: np.ndarray, g: Geom, window="ramlak", nthreads=0) -> np.ndarray:

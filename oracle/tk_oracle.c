@@ -766,6 +766,69 @@ int orc_fdk_u16_f64_sampled(const uint16_t *raw, double dark, double flat, doubl
     return 0;
 }
 
+/* Half-fan completion and fan->parallel rebinning in double, restating
+ * rsq::Half2FullFan (rsq_load.cpp:327-380) and rsq::Half2Para/Fan2Para
+ * (rsq_load.cpp:382-470) for `rows` independent [N][W] sinograms.  Angle
+ * indices past the last angle wrap to the first as in the reference. */
+static int orc_wrap(int a, int N)
+{
+    if (a > N - 1) a -= N;
+    if (a < 0) a += N;
+    return a;
+}
+
+void orc_half2fullfan_f64(const double *in, int W, int N, int rows, int am, double D, double dfi, int flip,
+                          double *out)
+{
+    int Wc = 2 * W - 1 - 2 * am, c0 = W - 1 - am;
+    for (int r = 0; r < rows; ++r) {
+        const double *img = in + (size_t)r * N * W;
+        for (int f = 0; f < N; ++f) {
+            double *row = out + ((size_t)r * N + (flip ? N - 1 - f : f)) * Wc;
+            for (int c = c0; c < Wc; ++c) row[c] = img[(size_t)f * W + (c - c0) + am];
+            double fi = f * dfi;
+            for (int t = -c0; t < 0; ++t) {
+                double at = atan(t / D);
+                double nf = (fi - 2 * at - ORC_PI) / dfi;
+                if (nf > (N - 1) || nf < 0) nf = (fi - 2 * at + ORC_PI) / dfi;
+                int a = (int)ceil(nf), b = (int)floor(nf);
+                double A = img[(size_t)orc_wrap(a, N) * W + (-t) + am];
+                double B = img[(size_t)orc_wrap(b, N) * W + (-t) + am];
+                row[t + c0] = (a != b) ? A + (B - A) * (-nf + a) : A;
+            }
+        }
+    }
+}
+
+void orc_half2para_f64(const double *in, int W, int N, int rows, int am, double D, double dfi, double *out)
+{
+    int Wc = 2 * W - 1 - 2 * am, Np = N / 2, center = W - 1 - am;
+    for (int r = 0; r < rows; ++r) {
+        const double *img = in + (size_t)r * N * W;
+        for (int f = 0; f < Np; ++f)
+            for (int u = 0; u < Wc; ++u) {
+                double ui = (double)u - (double)center, beta, s = ui;
+                if (ui >= 0.) beta = f + asin(ui / D) / dfi;
+                else beta = f - (asin(ui / D) - ORC_PI) / dfi;
+                if (beta < 0.) beta += N;
+                if (beta > N - 1) beta -= N;
+                if (ui < 0.) s *= -1;
+                int ba = (int)ceil(beta), bb = (int)floor(beta);
+                int sa = (int)ceil(s);
+                int col = sa + am; /* both taps use the ceiling (rsq_load.cpp:436-437) */
+                double v;
+                if (ba != bb) {
+                    double va = img[(size_t)orc_wrap(ba, N) * W + col];
+                    double vb = img[(size_t)orc_wrap(bb, N) * W + col];
+                    v = va + (vb - va) * (-beta + ba);
+                } else {
+                    v = img[(size_t)orc_wrap(ba, N) * W + col];
+                }
+                out[((size_t)r * Np + f) * Wc + u] = v;
+            }
+    }
+}
+
 /* adjoint: scatter every voxel into the filtered-sample gradient, one
  * projection per task (no races), then filter and weight each row */
 typedef struct {

@@ -102,6 +102,12 @@ int orc_fdk_f64(const float *sino, const orc_geom *g, int window,
 int orc_fdk_u16_f64_sampled(const uint16_t *raw, double dark, double flat, double A, double B, int invert,
                             double floor_counts, const orc_geom *g, int window,
                             const int *zlist, int nz, double *vol, int nthreads);
+/* Half-fan sinogram completion (out [rows][N][2W-1-2am]) and fan->parallel
+ * rebinning (out [rows][N/2][2W-1-2am]) in double, for rows independent
+ * [N][W] sinograms (rsq_load.cpp:327-470). */
+void orc_half2fullfan_f64(const double *in, int W, int N, int rows, int am, double D, double dfi, int flip,
+                          double *out);
+void orc_half2para_f64(const double *in, int W, int N, int rows, int am, double D, double dfi, double *out);
 /* FP64 adjoint of the FDK A = B F W (line integrals -> volume, exact slice
  * centring): out = W F B^T vol, with B^T the transpose of the bilinear
  * backprojection (same masks and weights) and F the symmetric ramp filter.

@@ -121,6 +121,17 @@ def test_stream_workspace_and_argument_checks(tklib):
     assert b"workspace" in tklib.tk_last_error()
 
 
+def test_rebin_argument_checks(tklib):
+    import math
+
+    p = ctypes.c_void_p(256)
+    # rotation axis beyond the detector; not a full 360-degree scan; odd angle count for parallel rebinning
+    assert tklib.tk_half_to_full_fan(p, 8, 10, 1, 7, 100.0, 2 * math.pi / 10, 0, p, None) == _lib.TK_ERR_INVALID
+    assert tklib.tk_half_to_parallel(p, 8, 10, 1, 2, 100.0, 0.1, p, None) == _lib.TK_ERR_UNSUPPORTED
+    assert tklib.tk_half_to_parallel(p, 8, 9, 1, 2, 100.0, 2 * math.pi / 9, p, None) == _lib.TK_ERR_INVALID
+    assert tklib.tk_half_to_full_fan(p, 8, 10, 1, 2, 5.0, 2 * math.pi / 10, 0, p, None) == _lib.TK_ERR_INVALID
+
+
 def test_handle_setters_and_state_errors(tklib):
     from tomokvas_gb300 import FilteredBackProjection
 

@@ -72,7 +72,7 @@ __device__ __forceinline__ int2 batch_footprint(const BatchItem &I, float2 cs, i
     return make_int2(bx, (int)floorf(vmin) - 1);
 }
 
-template <int PREC, int TX, int TY, int TZ, int STAGES, int MINB>
+template <int PREC, int TX, int TY, int TZ, int STAGES, int MINB, bool PACKED = true>
 __global__ void __launch_bounds__(TX *TY, MINB)
     bp_batch_kernel(const BatchItem *__restrict__ items, int nitems, int nunits, int *counter, unsigned *err,
                     int maxN, int slot_elems)
@@ -189,10 +189,11 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                                 update_cimg<PREC, TZ, false, true>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                         } else {
                             if (all_in)
-                                update_cimg<PREC, TZ, true, false>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                                update_cimg<PREC, TZ, true, false, PACKED>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
+                                                                           acc);
                             else
-                                update_cimg<PREC, TZ, false, false>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
-                                                                    acc);
+                                update_cimg<PREC, TZ, false, false, PACKED>(sbase, row_bytes, v0, dv, fu, U2, Hm1,
+                                                                            zlast, acc);
                         }
                     } else {
                         atomicOr(err, ERR_BOX_OVERFLOW);

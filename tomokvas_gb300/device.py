@@ -134,6 +134,28 @@ def fdk_stream(g, h_in, input_type=_lib.TK_INPUT_U16, ff=None, window=_lib.TK_WI
     return vol
 
 
+def half_to_full_fan(sino, axis_move: int, D: float, dfi: float, flip=False, out=None, stream=None):
+    """Half-fan completion of fan-beam sinograms sino [rows][N][W] (device FP32)."""
+    torch = _torch()
+    rows, N, W = sino.shape
+    if out is None:
+        out = torch.empty((rows, N, 2 * W - 1 - 2 * axis_move), dtype=torch.float32, device=sino.device)
+    check(load().tk_half_to_full_fan(sino.data_ptr(), W, N, rows, int(axis_move), float(D), float(dfi),
+                                     int(bool(flip)), out.data_ptr(), _stream_ptr(stream)))
+    return out
+
+
+def half_to_parallel(sino, axis_move: int, D: float, dfi: float, out=None, stream=None):
+    """Fan->parallel rebinning of half-fan sinograms sino [rows][N][W] (device FP32)."""
+    torch = _torch()
+    rows, N, W = sino.shape
+    if out is None:
+        out = torch.empty((rows, N // 2, 2 * W - 1 - 2 * axis_move), dtype=torch.float32, device=sino.device)
+    check(load().tk_half_to_parallel(sino.data_ptr(), W, N, rows, int(axis_move), float(D), float(dfi),
+                                     out.data_ptr(), _stream_ptr(stream)))
+    return out
+
+
 def forward_project(g, vol, nz=None, zoff=None, out=None, accumulate=False, stream=None):
     """B^T: transpose of the backprojection; returns [N][H][Wp] FP32."""
     torch = _torch()
