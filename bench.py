@@ -389,13 +389,14 @@ def run_ours(args):
     cpu_gups, cpu_s, sample = cpu_sample(g, cores)
 
     bp_tflops = upd * FLOPS_PER_UPDATE / (f16_bp * 1e-3) / 1e12
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "bp_traffic.json")
-    if os.path.exists(tf):
-        try:
-            traffic = json.load(open(tf)).get("f16_bytes_per_launch")
-        except (OSError, ValueError):
-            traffic = None
+    traffic = None  # DRAM bytes per backprojection launch, from the committed ncu summary
+    tf = os.path.join(ROOT, "profiles", "bp_cimg_x2_f16_1024cube_dram.md")
+    try:
+        for line in open(tf):
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = int(line.split(":", 1)[1])
+    except (OSError, ValueError):
+        traffic = None
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -418,7 +419,7 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": 4 * K,
         "device_error_flags": flags,
-        "roofline": {"bound": "fp32", "kernel": "bp_cimg_kernel<f16,16,16,64,3>",
+        "roofline": {"bound": "fp32", "kernel": "bp_cimg_kernel<f16,16,16,64,3,packed>",
                      "achieved": bp_tflops, "peak": PEAK_FP32_NOMINAL, "unit": "TFLOP/s",
                      "frac": bp_tflops / PEAK_FP32_NOMINAL, "traffic": traffic,
                      "flops_per_update": FLOPS_PER_UPDATE,

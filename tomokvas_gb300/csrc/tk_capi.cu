@@ -359,7 +359,7 @@ struct tk_fdk {
     float *d_block[2] = {nullptr, nullptr};
     size_t block_cap = 0;
     bool initialized = false, filtered = false;
-    cudaEvent_t ev[8] = {};
+    cudaEvent_t ev[10] = {};
     float t_filter = 0, t_bp = 0, t_h2d = 0, t_d2h = 0;
 };
 
@@ -586,7 +586,16 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
     if (int rc = ensure(&h->d_ws, &h->d_ws_cap, tk_fdk_workspace_bytes(&g, h->precision))) return rc;
     h->t_h2d = h->t_filter = h->t_bp = h->t_d2h = 0;
     TK_CUDA(cudaEventRecord(h->ev[0], h->stream));
-    TK_CUDA(cudaMemcpyAsync(h->d_in, h->host_in, in_bytes, cudaMemcpyHostToDevice, h->stream));
+    // Projection-major input whose storage scale is known before the data is
+    // seen (FP32 storage, or uint16 with scalar flat/dark) is copied in chunks
+    // and each chunk is filtered as soon as it has landed, so the upload
+    // overlaps the filter; otherwise one copy, and the filter runs later.
+    const bool scale_free = !(h->precision == TK_F16 || h->precision == TK_BF16) ||
+                            (h->input_type == TK_INPUT_U16 && !h->host_dark && !h->host_flat);
+    const int chunk = 64;
+    const bool overlap = h->layout == TK_LAYOUT_PROJECTION && scale_free && g.N >= 2 * chunk;
+    if (!overlap)
+        TK_CUDA(cudaMemcpyAsync(h->d_in, h->host_in, in_bytes, cudaMemcpyHostToDevice, h->stream));
     if (h->input_type == TK_INPUT_U16) {
         const size_t fb = (size_t)g.W * g.H * sizeof(float);
         if (h->host_dark || h->host_flat) {
@@ -615,11 +624,39 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
             h->ff.flat = h->d_flat;
         }
     }
-    TK_CUDA(cudaEventRecord(h->ev[1], h->stream));
-    TK_CUDA(cudaStreamSynchronize(h->stream));  // the host buffer is only borrowed until we return
+    h->filtered = false;
+    if (overlap) {
+        // copies on the copy stream (after the flat/dark uploads above), filters on the stream
+        TK_CUDA(cudaEventRecord(h->ev[8], h->stream));
+        TK_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev[8], 0));
+        const size_t frame = in_bytes / (size_t)g.N;
+        float *d_scale = static_cast<float *>(h->d_ws);
+        char *d_q = static_cast<char *>(h->d_ws) + kWsHeader;
+        const size_t qframe = filtered_bytes(g, h->precision) / (size_t)g.N;
+        TK_CUDA(cudaEventRecord(h->ev[2], h->stream));
+        for (int b0 = 0; b0 < g.N; b0 += chunk) {
+            const int nb = std::min(chunk, g.N - b0);
+            const size_t off = (size_t)b0 * frame;
+            TK_CUDA(cudaMemcpyAsync(static_cast<char *>(h->d_in) + off, static_cast<const char *>(h->host_in) + off,
+                                    (size_t)nb * frame, cudaMemcpyHostToDevice, h->copy_stream));
+            TK_CUDA(cudaEventRecord(h->ev[9], h->copy_stream));
+            TK_CUDA(cudaStreamWaitEvent(h->stream, h->ev[9], 0));
+            tk_geometry gc = g;
+            gc.N = nb;
+            if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + off, h->input_type, h->layout, &h->ff,
+                                       h->window, d_q + (size_t)b0 * qframe, h->precision, d_scale, h->stream))
+                return rc;
+        }
+        TK_CUDA(cudaEventRecord(h->ev[3], h->stream));
+        TK_CUDA(cudaEventRecord(h->ev[1], h->copy_stream));
+        TK_CUDA(cudaStreamSynchronize(h->copy_stream));  // the host buffer is only borrowed until we return
+        h->filtered = true;
+    } else {
+        TK_CUDA(cudaEventRecord(h->ev[1], h->stream));
+        TK_CUDA(cudaStreamSynchronize(h->stream));  // the host buffer is only borrowed until we return
+    }
     if (int rc = elapsed(h->ev[0], h->ev[1], &h->t_h2d)) return rc;
     h->initialized = true;
-    h->filtered = false;
     if (h->show) fprintf(stdout, "tk_fdk: %zu MiB of projections on GPU %d\n", in_bytes >> 20, h->dev);
     return TK_OK;
 }

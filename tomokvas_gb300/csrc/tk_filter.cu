@@ -229,49 +229,84 @@ template <> __device__ __forceinline__ void dft<16>(float2 (&v)[16])
     for (int i = 0; i < 16; ++i) v[i] = o[i];
 }
 
-template <int R>
-__device__ __forceinline__ void fft_pass(const float2 *__restrict__ x, float2 *__restrict__ y,
-                                         const float2 *__restrict__ tw, int p, int Ns, int t, int TPF)
+// Threads per transform (one radix-16 butterfly each); compile-time form.
+__host__ __device__ constexpr int fft_threads_c(int p)
 {
-    const int q = p / R;
-    for (int j = t; j < q; j += TPF) {
-        const int k = j & (Ns - 1);
-        float2 v[R];
+    return ((p >> 4) > 32 ? (p >> 4) : 32) < kFiltThreads ? ((p >> 4) > 32 ? (p >> 4) : 32) : kFiltThreads;
+}
+
+// Compile-time length: pass m of a length-2^LG transform has radix 16 except
+// possibly the last (fft_plan), span Ns = 16^m and its twiddle table at
+// offset 16^m - 16 (m >= 1).  With every size a constant, the padded
+// addresses of the loads and stores fold into immediates and the butterfly
+// loops unroll.
+template <int R, int P, int NS>
+__device__ __forceinline__ void fft_pass_c(const float2 *__restrict__ x, float2 *__restrict__ y,
+                                           const float2 *__restrict__ tw, int t)
+{
+    constexpr int Q = P / R;
+    constexpr int TPF = fft_threads_c(P);
+    constexpr int ITER = (Q + TPF - 1) / TPF;
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = x[pidx(j + r * q)];
-        if (Ns > 1) {
+    for (int i = 0; i < ITER; ++i) {
+        const int j = t + i * TPF;
+        if ((Q % TPF) != 0 && j >= Q) break;
+        const int k = j & (NS - 1);
+        float2 v[R];
+        if constexpr (Q % 16 == 0) {  // pidx(j + r Q) = pidx(j) + r (Q + Q/16)
+            const float2 *xs = x + pidx(j);
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = xs[r * (Q + Q / 16)];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = x[pidx(j + r * Q)];
+        }
+        if constexpr (NS > 1) {
             const float2 *w = tw + k * (R - 1) - 1;
 #pragma unroll
             for (int r = 1; r < R; ++r) v[r] = cmul(v[r], w[r]);
         }
         dft<R>(v);
         const int o = (j - k) * R + k;
+        if constexpr (NS % 16 == 0) {
+            float2 *ys = y + pidx(o);
 #pragma unroll
-        for (int s2 = 0; s2 < R; ++s2) y[pidx(o + s2 * Ns)] = v[s2];
+            for (int s2 = 0; s2 < R; ++s2) ys[s2 * (NS + NS / 16)] = v[s2];
+        } else if constexpr (NS == 1 && R == 16) {  // o is a multiple of 16: o + s stays in one padding group
+            float2 *ys = y + pidx(o);
+#pragma unroll
+            for (int s2 = 0; s2 < R; ++s2) ys[s2] = v[s2];
+        } else {
+#pragma unroll
+            for (int s2 = 0; s2 < R; ++s2) y[pidx(o + s2 * NS)] = v[s2];
+        }
     }
 }
 
-// Forward FFT of length p (padded buffers); ping-pongs between a and b and
-// returns the buffer holding the result.  Every thread of the CTA calls it
-// (barriers inside).
-__device__ __forceinline__ float2 *fft_forward(float2 *a, float2 *b, const float2 *twp, const FFTPlan &pl, int p,
-                                               int t, int TPF)
+template <int LG, int M>
+__device__ __forceinline__ void fft_passes_c(float2 *&a, float2 *&b, const float2 *twp, int t)
 {
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {  // p <= 8192: at most four passes
-        if (m >= pl.npass) break;
-        const float2 *tw = twp + pl.off[m];
-        switch (pl.R[m]) {
-        case 16: fft_pass<16>(a, b, tw, p, pl.Ns[m], t, TPF); break;
-        case 8: fft_pass<8>(a, b, tw, p, pl.Ns[m], t, TPF); break;
-        case 4: fft_pass<4>(a, b, tw, p, pl.Ns[m], t, TPF); break;
-        default: fft_pass<2>(a, b, tw, p, pl.Ns[m], t, TPF); break;
-        }
+    if constexpr (LG - 4 * M > 0) {
+        constexpr int rem = LG - 4 * M;
+        constexpr int R = rem >= 4 ? 16 : (1 << rem);
+        constexpr int NS = 1 << (4 * M);
+        constexpr int OFF = M >= 1 ? (1 << (4 * M)) - 16 : 0;
+        fft_pass_c<R, (1 << LG), NS>(a, b, twp + OFF, t);
         __syncthreads();
         float2 *s2 = a;
         a = b;
         b = s2;
+        fft_passes_c<LG, M + 1>(a, b, twp, t);
     }
+}
+
+// Forward FFT of length 2^LG (padded buffers); ping-pongs between a and b and
+// returns the buffer holding the result.  Every thread of the CTA calls it
+// (barriers inside).
+template <int LG>
+__device__ __forceinline__ float2 *fft_forward_c(float2 *a, float2 *b, const float2 *twp, int t)
+{
+    fft_passes_c<LG, 0>(a, b, twp, t);
     return a;
 }
 
@@ -318,15 +353,15 @@ __device__ __forceinline__ long long out_row_offset(const FiltParams &P, long lo
     return P.out_layout == TK_LAYOUT_SINOGRAM ? ((long long)r * P.L.N + b) * P.Wp : row * (long long)P.Wp;
 }
 
-template <typename T>
+template <typename T, int LG>
 __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_constant__ FiltParams P)
 {
     extern __shared__ __align__(16) float2 fsm[];
-    const int p = P.p;
+    constexpr int p = 1 << LG;
     const FFTPlan &pl = P.plan;
     const FiltSmem lay = filt_smem(p, pl.tw_total, P.L.W, false);
-    const int TPF = fft_threads(p);
-    const int G = kFiltThreads / TPF;
+    constexpr int TPF = fft_threads_c(p);
+    constexpr int G = kFiltThreads / TPF;
     const int grp = threadIdx.x / TPF, t = threadIdx.x - grp * TPF;
     float2 *twp = fsm;
     float *hf = reinterpret_cast<float *>(fsm + lay.tw_total);
@@ -358,16 +393,17 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
             }
         }
         __syncthreads();
-        float2 *R = fft_forward(bufA, bufB, twp, pl, p, t, TPF);
+        float2 *R = fft_forward_c<LG>(bufA, bufB, twp, t);
         float2 *Sb = (R == bufA) ? bufB : bufA;
         // conj(Z) * Hf (Hf real and even)
+#pragma unroll 4
         for (int k = t; k < p; k += TPF) {
             const float h = hf[k <= (p >> 1) ? k : p - k];
             const float2 z = R[pidx(k)];
             R[pidx(k)] = make_float2(z.x * h, -z.y * h);
         }
         __syncthreads();
-        float2 *Q = fft_forward(R, Sb, twp, pl, p, t, TPF);
+        float2 *Q = fft_forward_c<LG>(R, Sb, twp, t);
         if (valid) {
             int r_a, r_b;
             T *qa = out + out_row_offset(P, ra, r_a);
@@ -452,15 +488,15 @@ __device__ __forceinline__ void emit_coef_row(void *img, size_t row_base, int W,
     }
 }
 
-template <int MODE>
+template <int MODE, int LG>
 __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_constant__ FiltParams P)
 {
     extern __shared__ __align__(16) float2 fsm[];
-    const int p = P.p;
+    constexpr int p = 1 << LG;
     const FFTPlan &pl = P.plan;
     const FiltSmem lay = filt_smem(p, pl.tw_total, P.L.W, true);
-    const int TPF = fft_threads(p);
-    const int G = kFiltThreads / TPF;
+    constexpr int TPF = fft_threads_c(p);
+    constexpr int G = kFiltThreads / TPF;
     const int grp = threadIdx.x / TPF, t = threadIdx.x - grp * TPF;
     float2 *twp = fsm;
     float *hf = reinterpret_cast<float *>(fsm + lay.tw_total);
@@ -502,15 +538,16 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
                 }
             }
             __syncthreads();
-            float2 *R = fft_forward(bufA, bufB, twp, pl, p, t, TPF);
+            float2 *R = fft_forward_c<LG>(bufA, bufB, twp, t);
             float2 *Sb = (R == bufA) ? bufB : bufA;
+#pragma unroll 4
             for (int kk = t; kk < p; kk += TPF) {
                 const float h = hf[kk <= (p >> 1) ? kk : p - kk];
                 const float2 z = R[pidx(kk)];
                 R[pidx(kk)] = make_float2(z.x * h, -z.y * h);
             }
             __syncthreads();
-            const float2 *Q = fft_forward(R, Sb, twp, pl, p, t, TPF);
+            const float2 *Q = fft_forward_c<LG>(R, Sb, twp, t);
             if (live) {
                 const size_t base = (size_t)b * H;
                 const RowRe rowa{Q, sigma, W};
@@ -643,15 +680,44 @@ static const Spectrum &spectrum(int W, float tau, int window, int p)
     return cache.emplace(key, std::move(sp)).first->second;
 }
 
+// The kernel instantiated for storage `precision` and pad length 2^lg
+// (2 <= lg <= 13; coefficient storage up to lg = 12, i.e. W <= 2048).
+template <int LG> static const void *filter_kernel_lg(int precision)
+{
+    switch (precision) {
+    case TK_F32: return reinterpret_cast<const void *>(&filter_fft_kernel<float, LG>);
+    case TK_F16: if constexpr (LG <= 12) return reinterpret_cast<const void *>(&filter_coef_kernel<TK_F16, LG>); break;
+    case TK_BF16: if constexpr (LG <= 12) return reinterpret_cast<const void *>(&filter_coef_kernel<TK_BF16, LG>); break;
+    case TK_F32_COEF:
+        if constexpr (LG <= 12) return reinterpret_cast<const void *>(&filter_coef_kernel<TK_F32_COEF, LG>);
+        break;
+    }
+    return nullptr;
+}
+
+static const void *filter_kernel_fn(int precision, int lg)
+{
+    switch (lg) {
+    case 2: return filter_kernel_lg<2>(precision);
+    case 3: return filter_kernel_lg<3>(precision);
+    case 4: return filter_kernel_lg<4>(precision);
+    case 5: return filter_kernel_lg<5>(precision);
+    case 6: return filter_kernel_lg<6>(precision);
+    case 7: return filter_kernel_lg<7>(precision);
+    case 8: return filter_kernel_lg<8>(precision);
+    case 9: return filter_kernel_lg<9>(precision);
+    case 10: return filter_kernel_lg<10>(precision);
+    case 11: return filter_kernel_lg<11>(precision);
+    case 12: return filter_kernel_lg<12>(precision);
+    case 13: return filter_kernel_lg<13>(precision);
+    }
+    return nullptr;
+}
+
 static int launch_filter_typed(const FiltParams &P, int p, cudaStream_t stream, int precision)
 {
-    const void *fn = nullptr;
-    switch (precision) {
-    case TK_F32: fn = reinterpret_cast<const void *>(&filter_fft_kernel<float>); break;
-    case TK_F16: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_F16>); break;
-    case TK_BF16: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_BF16>); break;
-    default: fn = reinterpret_cast<const void *>(&filter_coef_kernel<TK_F32_COEF>); break;
-    }
+    const void *fn = filter_kernel_fn(precision, P.lg);
+    TK_CHECK(fn, TK_ERR_UNSUPPORTED, "filter: no kernel for pad length %d with this storage", p);
     const int G = kFiltThreads / fft_threads(p);
     const size_t smem = filt_smem(p, P.plan.tw_total, P.L.W, is_coef(precision)).bytes();
     TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "filter: pad length %d needs too much shared memory", p);
