@@ -108,6 +108,32 @@ __device__ __forceinline__ float cosine_weight(const LoadParams &L, int r, int x
     return L.D / sqrtf(ce * ce + L.D * L.D + cs * cs);
 }
 
+// Raw sample x of the row at element offset off (counts as float for u16).
+__device__ __forceinline__ float load_raw(const LoadParams &L, long long off, int x)
+{
+    return L.input_type == TK_INPUT_U16 ? (float)static_cast<const uint16_t *>(L.in)[off + x]
+                                        : static_cast<const float *>(L.in)[off + x];
+}
+
+// Preprocessing of a raw sample: flat-field + log if raw counts, then the
+// cosine weight (kernel.cu:195-199).
+__device__ __forceinline__ float pre_from_raw(const LoadParams &L, int r, int x, float raw)
+{
+    float val = raw;
+    if (L.input_type == TK_INPUT_U16) {
+        const float I = raw;
+        const size_t px = (size_t)r * L.W + x;
+        const float dk = L.dark ? L.dark[px] : L.dark_v;
+        const float fl = L.flat ? L.flat[px] : L.flat_v;
+        const float num = fmaxf(I - dk, L.floor_counts);
+        const float den = fmaxf(fl - dk, L.floor_counts);
+        val = L.A * logf(num / den) + L.B;
+        if (L.invert) val = -val;
+    }
+    if (!L.weight_in) return val;
+    return val * cosine_weight(L, r, x);
+}
+
 // Preprocessed (log if raw, cosine weighted) sample x of a row.
 __device__ __forceinline__ float load_pre(const LoadParams &L, long long off, int r, int x)
 {
@@ -374,6 +400,25 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
     T *out = static_cast<T *>(P.out);
     __syncthreads();
 
+    // Raw samples of a pair group's two rows, fetched one group ahead so that
+    // their latency overlaps the transforms of the current one.
+    constexpr int NV = (p / 2 + TPF - 1) / TPF;
+    float raw_a[NV], raw_b[NV];
+    auto fetch = [&](long long pgf) {
+        const long long pr = pgf * G + grp;
+        const bool vl = pr < P.npairs;
+        const bool hb = vl && 2 * pr + 1 < P.nrows;
+        int rr;
+        const long long oa = vl ? in_row_offset(P.L, 2 * pr, rr) : 0;
+        const long long ob = hb ? in_row_offset(P.L, 2 * pr + 1, rr) : 0;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const int x = t + i * TPF;
+            raw_a[i] = (vl && x < W) ? load_raw(P.L, oa, x) : 0.f;
+            raw_b[i] = (hb && x < W) ? load_raw(P.L, ob, x) : 0.f;
+        }
+    };
+    if ((long long)blockIdx.x * G < P.npairs) fetch(blockIdx.x);
     for (long long pg = blockIdx.x; pg * G < P.npairs; pg += gridDim.x) {
         const long long pair = pg * G + grp;
         const bool valid = pair < P.npairs;
@@ -381,17 +426,18 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
         const bool hasb = valid && rb < P.nrows;
         if (valid) {
             int r_a = 0, r_b = 0;
-            const long long oa = in_row_offset(P.L, ra, r_a);
-            const long long ob = hasb ? in_row_offset(P.L, rb, r_b) : 0;
-            for (int x = t; x < p; x += TPF) {
-                float a = 0.f, b = 0.f;
-                if (x < W) {
-                    a = load_pre(P.L, oa, r_a, x);
-                    if (hasb) b = load_pre(P.L, ob, r_b, x);
-                }
-                bufA[pidx(x)] = make_float2(a, b);
+            in_row_offset(P.L, ra, r_a);
+            if (hasb) in_row_offset(P.L, rb, r_b);
+#pragma unroll
+            for (int i = 0; i < NV; ++i) {
+                const int x = t + i * TPF;
+                if (x < W)
+                    bufA[pidx(x)] = make_float2(pre_from_raw(P.L, r_a, x, raw_a[i]),
+                                                hasb ? pre_from_raw(P.L, r_b, x, raw_b[i]) : 0.f);
             }
+            for (int x = W + t; x < p; x += TPF) bufA[pidx(x)] = make_float2(0.f, 0.f);  // zero padding
         }
+        if ((pg + gridDim.x) * G < P.npairs) fetch(pg + gridDim.x);
         __syncthreads();
         float2 *R = fft_forward_c<LG>(bufA, bufB, twp, t);
         float2 *Sb = (R == bufA) ? bufB : bufA;
@@ -520,23 +566,40 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
         const int npair = valid ? (rend - r0 + 2) / 2 : 0;
         // every group runs the same number of pair steps (CTA-wide barriers inside)
         const int steps = (min(RC, H - 1) + 2) / 2;
+        // Raw samples x = t + i TPF (< W <= p/2) of the next step's two rows,
+        // fetched one step ahead so that their latency overlaps the transforms.
+        constexpr int NV = (p / 2 + TPF - 1) / TPF;
+        float raw_a[NV], raw_b[NV];
+        auto fetch = [&](int kk) {
+            const bool lv = valid && kk < npair;
+            const int qa = r0 + 2 * kk, qb = qa + 1;
+            const bool hb = lv && qb <= rend;
+            int rr;
+            const long long oa = lv ? in_row_offset(P.L, b * H + qa, rr) : 0;
+            const long long ob = hb ? in_row_offset(P.L, b * H + qb, rr) : 0;
+#pragma unroll
+            for (int i = 0; i < NV; ++i) {
+                const int x = t + i * TPF;
+                raw_a[i] = (lv && x < W) ? load_raw(P.L, oa, x) : 0.f;
+                raw_b[i] = (hb && x < W) ? load_raw(P.L, ob, x) : 0.f;
+            }
+        };
+        fetch(0);
         for (int k = 0; k < steps; ++k) {
             const bool live = valid && k < npair;
             const int ra = r0 + 2 * k, rb = ra + 1;
             const bool hasb = live && rb <= rend;
             if (live) {
-                int rr;
-                const long long oa = in_row_offset(P.L, b * H + ra, rr);
-                const long long ob = hasb ? in_row_offset(P.L, b * H + rb, rr) : 0;
-                for (int x = t; x < p; x += TPF) {
-                    float va = 0.f, vb = 0.f;
-                    if (x < W) {
-                        va = load_pre(P.L, oa, ra, x);
-                        if (hasb) vb = load_pre(P.L, ob, rb, x);
-                    }
-                    bufA[pidx(x)] = make_float2(va, vb);
+#pragma unroll
+                for (int i = 0; i < NV; ++i) {
+                    const int x = t + i * TPF;
+                    if (x < W)
+                        bufA[pidx(x)] = make_float2(pre_from_raw(P.L, ra, x, raw_a[i]),
+                                                    hasb ? pre_from_raw(P.L, rb, x, raw_b[i]) : 0.f);
                 }
+                for (int x = W + t; x < p; x += TPF) bufA[pidx(x)] = make_float2(0.f, 0.f);  // zero padding
             }
+            if (k + 1 < steps) fetch(k + 1);
             __syncthreads();
             float2 *R = fft_forward_c<LG>(bufA, bufB, twp, t);
             float2 *Sb = (R == bufA) ? bufB : bufA;
