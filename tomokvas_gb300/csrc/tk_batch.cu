@@ -110,7 +110,8 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         const BatchItem &I = items[lo];
         const int local = u - I.unit0;
         const int tile = local % I.ntiles, zci = local / I.ntiles;
-        const int x0 = (tile % I.tilesX) * TX, y0 = (tile / I.tilesX) * TY;
+        const int2 tc = tile_of(tile, I.tilesX, I.ntiles / I.tilesX);
+        const int x0 = tc.x * TX, y0 = tc.y * TY;
         const int nz = I.nz;
         const bool partial = nz < TZ;
         const int zc = zci * TZ;

@@ -45,7 +45,7 @@ struct BPParams {
     int X, Y, nz, N;
     int BW, BH;              // staged box (elements)
     int stage_elems;         // elements per raw stage (>= BW*BH, padded)
-    int tilesX;
+    int tilesX, tilesY;
     int accumulate;
     float cX, cZ, D;
     float dX, dY, zoff, scale;
@@ -182,7 +182,8 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX;
-    const int x0 = (blockIdx.x % P.tilesX) * TX, y0 = (blockIdx.x / P.tilesX) * TY;
+    const int2 tile = tile_of(blockIdx.x, P.tilesX, P.tilesY);
+    const int x0 = tile.x * TX, y0 = tile.y * TY;
     const int z0 = blockIdx.y * TZ;
     const int x = x0 + tx, y = y0 + ty;
 
@@ -353,7 +354,8 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX;
-    const int x0 = (blockIdx.x % P.tilesX) * TX, y0 = (blockIdx.x / P.tilesX) * TY;
+    const int2 tile = tile_of(blockIdx.x, P.tilesX, P.tilesY);
+    const int x0 = tile.x * TX, y0 = tile.y * TY;
     // Full chunks: the last one is moved down to end at nz and stores only
     // the slices no earlier chunk owns.  PARTIAL handles nz < TZ.
     const int zc = blockIdx.y * TZ;
@@ -506,7 +508,8 @@ __global__ void __launch_bounds__(TX *TY, 2)
 
     const int tid = threadIdx.x, lane = tid & 31;
     const int tx = tid % TX, ty = tid / TX;
-    const int x0 = (blockIdx.x % P.tilesX) * TX, y0 = (blockIdx.x / P.tilesX) * TY;
+    const int2 tile = tile_of(blockIdx.x, P.tilesX, P.tilesY);
+    const int x0 = tile.x * TX, y0 = tile.y * TY;
     const int zc = blockIdx.y * TZ;
     const int z0 = PARTIAL ? zc : min(zc, P.nz - TZ);
     const int zlast = PARTIAL ? P.nz - 1 - z0 : TZ - 1;
@@ -749,6 +752,7 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     P.stage_elems = v->coef ? (BW * BH + 15) / 16 * 16   // 128-byte aligned stages
                             : (BW * BH + 63) / 64 * 64;
     P.tilesX = tilesX;
+    P.tilesY = tilesY;
     P.accumulate = accumulate ? 1 : 0;
     P.cX = g.cX;
     P.cZ = g.cZ;
@@ -840,6 +844,7 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     P.BH = BH;
     P.stage_elems = (BW * BH + 31) / 32 * 32;  // 128-byte aligned boxes
     P.tilesX = tilesX;
+    P.tilesY = tilesY;
     P.cX = g.cX;
     P.cZ = g.cZ;
     P.D = g.D;

@@ -15,6 +15,19 @@ __device__ __forceinline__ float flip(float v, unsigned mask)
 
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: a TMA stage never takes this long
 
+// Tile of CTA index i: tiles are visited in column groups kTileGroup tiles
+// wide (row by row inside a group), so the CTAs resident at one time cover a
+// compact patch of the slice whose footprints overlap in L2, rather than a
+// thin strip across the whole slice.
+constexpr int kTileGroup = 16;
+__device__ __forceinline__ int2 tile_of(int i, int tilesX, int tilesY)
+{
+    const int per = kTileGroup * tilesY;
+    const int g = i / per, r = i - g * per;
+    const int w = min(kTileGroup, tilesX - g * kTileGroup);  // the last group may be narrower
+    return make_int2(g * kTileGroup + r % w, r / w);
+}
+
 // Per column-angle geometry with every rounding spelled out:
 //   S = aX cos + aY sin,  T = aY cos - aX sin,  U = D / (D - S),  u = T U + cX
 // (kernel.cu:102-109).  Every kernel evaluates it through this function --
