@@ -288,6 +288,15 @@ int tk_batch_variant(const tk_batch *b);
 /* Forces a tile shape (-1: default); takes effect at the next plan. */
 int tk_batch_select_variant(tk_batch *b, int i);
 
+/* ------------------------------------------------------------ diagnostics
+ * tk_kernel_launches: kernels this library has launched in this process (a
+ * monotonic count, for measuring how many launches a region issued).
+ * tk_measure_fp32_fma_rate: times a bounded FP32 FMA throughput kernel on the
+ * current device (about a millisecond) and writes its rate in TFLOP/s, the
+ * FP32-pipe ceiling the backprojection is measured against.  Synchronous. */
+unsigned long long tk_kernel_launches(void);
+int tk_measure_fp32_fma_rate(double *tflops_out);
+
 /* ------------------------------ FilteredBackProjection mirror (handle) */
 /* One handle = one FilteredBackProjection object (kernel.cuh:82-151).
  * Call order as in FBPG/para_TC.cpp:130-153: setters -> initialize ->

@@ -37,7 +37,7 @@ EXPORTS = [
     "tk_batch_create", "tk_batch_destroy", "tk_batch_set_precision", "tk_batch_submit", "tk_batch_size",
     "tk_batch_workspace_bytes", "tk_batch_plan", "tk_batch_run", "tk_batch_autotune", "tk_batch_variant_count",
     "tk_batch_variant_name", "tk_batch_variant", "tk_batch_select_variant",
-    "tk_half_to_full_fan", "tk_half_to_parallel",
+    "tk_half_to_full_fan", "tk_half_to_parallel", "tk_kernel_launches", "tk_measure_fp32_fma_rate",
 ]
 
 
@@ -139,6 +139,8 @@ def _declare(L):
     L.tk_batch_variant_name.restype = ctypes.c_char_p
     L.tk_batch_variant.argtypes = [vp]
     L.tk_batch_select_variant.argtypes = [vp, ip]
+    L.tk_kernel_launches.restype = ctypes.c_ulonglong
+    L.tk_measure_fp32_fma_rate.argtypes = [ctypes.POINTER(ctypes.c_double)]
     dd = ctypes.c_double
     L.tk_half_to_full_fan.argtypes = [vp, ip, ip, ip, ip, dd, dd, ip, vp, vp]
     L.tk_half_to_parallel.argtypes = [vp, ip, ip, ip, ip, dd, dd, vp, vp]

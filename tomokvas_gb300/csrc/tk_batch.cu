@@ -457,6 +457,7 @@ int enqueue(tk_batch *b, cudaStream_t st)
     int nitems = n, nunits = b->nunits, maxN = b->maxN, slot = b->slot_elems;
     void *args[] = {&items, &nitems, &nunits, &counter, &err, &maxN, &slot};
     TK_CUDA(cudaLaunchKernel(V.fn, dim3((unsigned)b->grid), dim3((unsigned)(V.TX * V.TY)), args, b->smem, st));
+    count_launch();
     return TK_OK;
 }
 

@@ -800,6 +800,7 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
         dim3 block((unsigned)(v->TX * v->TY), 1, 1);
         void *args[] = {&tmap, &P};
         TK_CUDA(cudaLaunchKernel(fn, grid, block, args, smem, stream));
+        count_launch();
     }
     return TK_OK;
 }
@@ -882,6 +883,7 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
         const float *vin = d_vol;
         void *args[] = {&tmap, &P, &vin};
         TK_CUDA(cudaLaunchKernel(fn, grid, dim3(TX * TY), args, smem, stream));
+        count_launch();
     }
     return TK_OK;
 }

@@ -796,6 +796,7 @@ static int launch_filter_typed(const FiltParams &P, int p, cudaStream_t stream, 
     void *args[] = {const_cast<FiltParams *>(&P)};
     TK_CUDA(cudaLaunchKernel(fn, dim3((unsigned)std::max<long long>(grid, 1)), dim3(kFiltThreads), args, smem,
                              stream));
+    count_launch();
     return TK_OK;
 }
 
@@ -863,7 +864,10 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
 
     if (!sixteen) {
         P.q_scale = nullptr;
-        if (d_q_scale) set_scale_kernel<<<1, 1, 0, stream>>>(d_q_scale, 1.f);
+        if (d_q_scale) {
+            set_scale_kernel<<<1, 1, 0, stream>>>(d_q_scale, 1.f);
+            count_launch();
+        }
     } else if (input_type == TK_INPUT_U16 && !ff->dark && !ff->flat) {
         // Scalar flat/dark: |A log(num/den) + B| is bounded without looking at the
         // data, since num in [floor, 65535] and den = max(flat - dark, floor).
@@ -873,6 +877,7 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
         int e = bound > 0 ? (int)std::floor(std::log2((double)kScaleTarget / bound)) : 0;
         e = std::max(-100, std::min(100, e));
         set_scale_kernel<<<1, 1, 0, stream>>>(d_q_scale, (float)std::ldexp(1.0, e));
+        count_launch();
         P.q_scale = d_q_scale;
     } else {
         TK_CUDA(cudaMemsetAsync(d_q_scale, 0, sizeof(float), stream));
@@ -881,6 +886,7 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
         TK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         prescan_kernel<<<sms * 4, 256, 0, stream>>>(L, P.nrows, reinterpret_cast<unsigned *>(d_q_scale));
         scale_finalize_kernel<<<1, 1, 0, stream>>>(d_q_scale, sp.L1K);
+        count_launch(2);  // prescan + finalize
         P.q_scale = d_q_scale;
     }
     TK_CUDA(cudaGetLastError());

@@ -60,6 +60,9 @@ int launch_phantom(const tk_geometry &g, const double *ell, int nell, int layout
 int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ, bool coef, int align, int *BW,
                 int *BH);
 
+// Counts one kernel launch issued by this library (tk_kernel_launches).
+void count_launch(unsigned n = 1);
+
 // Device error word of the current device (allocated on first use).
 unsigned *device_error_word();
 

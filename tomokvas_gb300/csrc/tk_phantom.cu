@@ -96,6 +96,7 @@ int launch_phantom(const tk_geometry &g, const double *ell, int nell, int layout
         for (int i = 0; i < nb; ++i) P.trig[i] = make_float2(cs[b0 + i], sn[b0 + i]);
         dim3 grid((unsigned)((g.W + 127) / 128), (unsigned)g.H, (unsigned)nb);
         phantom_kernel<<<grid, 128, 0, stream>>>(P, b0);
+        count_launch();
         TK_CUDA(cudaGetLastError());
     }
     return TK_OK;

@@ -136,6 +136,7 @@ extern "C" int tk_half_to_full_fan(const float *d_in, int W, int N, int rows, in
     const long long total = (long long)rows * N * (2 * W - 1 - 2 * axis_move);
     half2fullfan_kernel<<<rebin_grid(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         d_in, d_out, W, N, rows, axis_move, D, dfi, flip ? 1 : 0);
+    count_launch();
     TK_CUDA(cudaGetLastError());
     return TK_OK;
 }
@@ -148,6 +149,7 @@ extern "C" int tk_half_to_parallel(const float *d_in, int W, int N, int rows, in
     const long long total = (long long)rows * (N / 2) * (2 * W - 1 - 2 * axis_move);
     half2para_kernel<<<rebin_grid(total), 256, 0, static_cast<cudaStream_t>(stream)>>>(d_in, d_out, W, N, rows,
                                                                                         axis_move, D, dfi);
+    count_launch();
     TK_CUDA(cudaGetLastError());
     return TK_OK;
 }
