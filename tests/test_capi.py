@@ -132,6 +132,11 @@ def test_rebin_argument_checks(tklib):
     assert tklib.tk_half_to_full_fan(p, 8, 10, 1, 2, 5.0, 2 * math.pi / 10, 0, p, None) == _lib.TK_ERR_INVALID
 
 
+def test_diagnostics_without_gpu(tklib):
+    assert tklib.tk_kernel_launches() >= 0
+    assert tklib.tk_measure_fp32_fma_rate(None) == _lib.TK_ERR_INVALID
+
+
 def test_handle_setters_and_state_errors(tklib):
     from tomokvas_gb300 import FilteredBackProjection
 

@@ -388,6 +388,27 @@ def test_handle_chunked_upload_equals_device_path(orc, cuda, prec, raw):
     np.testing.assert_array_equal(vol.cpu().numpy(), ref.cpu().numpy())
 
 
+def test_launch_count_and_fma_rate(cuda, case):
+    """One FDK from uint16 counts with FP16 storage is three launches: the
+    analytic storage scale, the fused filter and one backprojection."""
+    import ctypes
+
+    import torch
+
+    g, G, ell, sino = case
+    raw = counts_u16(np.transpose(sino, (1, 0, 2)), 60000.0, seed=2)
+    d_in = to_dev(raw.view(np.int16), torch)
+    ff = device.flatfield(flat_value=60000.0)
+    L = _lib.load()
+    device.fdk_device(g, d_in, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff, precision=_lib.TK_F16)
+    n0 = L.tk_kernel_launches()
+    device.fdk_device(g, d_in, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff, precision=_lib.TK_F16)
+    assert L.tk_kernel_launches() - n0 == 3
+    r = ctypes.c_double()
+    _lib.check(L.tk_measure_fp32_fma_rate(ctypes.byref(r)))
+    assert 10.0 < r.value < 200.0  # TFLOP/s
+
+
 def test_full_size_1024_sampled_slices(orc, cuda):
     """The 720 x 1024^2 uint16 workload at full size: GPU vs FP64 oracle on
     sampled slices (the oracle filters only the detector rows they need)."""
