@@ -22,9 +22,14 @@ def dev(a, torch):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
+# The forward projector has two forms, picked from the smallest row step of
+# consecutive slices, |scale| D / (D + W/2): "plain" (0.95: atomic-free, two
+# passes by lane parity), "flips_scale" (1.43: atomic-free, one pass) and
+# "fine_voxels" (0.36: shared atomics).
 GEOMS = {
     "plain": dict(W=64, N=72, H=56, vol=(48, 48, 40)),
     "flips_scale": dict(W=60, N=50, H=64, vol=(40, 36, 45), voxel_mm=1.2, dirx=1, dirz=1, rot=0.4),
+    "fine_voxels": dict(W=64, N=40, H=48, vol=(48, 40, 36), voxel_mm=0.3),
 }
 
 
