@@ -40,6 +40,16 @@ CPU_SAMPLE_SLICES = (508, 509, 510, 511, 512, 513, 514, 515)
 RMSE_SLICES = ((480, 512, 544), (1010,))
 
 
+def bp_kernel_name(variant):
+    """Name of the FP16 backprojection variant the chosen form runs (the selected one, else the default)."""
+    from tomokvas_gb300 import _lib
+
+    L = _lib.load()
+    if variant < 0:
+        variant = next(i for i in range(L.tk_bp_variant_count()) if L.tk_bp_variant_precision(i) == _lib.TK_F16)
+    return "bp_" + L.tk_bp_variant_name(variant).decode()
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -64,6 +74,10 @@ def parse():
                          "at the 256^3 and 1024^3 workloads beside ours on the same log sinograms (Ram-Lak), "
                          "with the relative RMSE between the two")
     ap.add_argument("--chunk", type=int, default=64, help="projections per streamed chunk (--outofcore)")
+    ap.add_argument("--items", type=int, default=64, help="with --batch: only the first ITEMS volumes (small case for ncu)")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="with --adjoint: small case for ncu, 120 instead of 360 projections (same 512^3 volume, "
+                         "same row step 1.43)")
     ap.add_argument("--profile-filter", choices=["f32", "f16", "bf16", "f32c"], default=None,
                     help="small case for ncu: the u16 log + Hann filter of 90 x 1024^2 projections into one "
                          "storage format; one untimed and two timed launches")
@@ -245,6 +259,8 @@ def run_ours(args):
         torch.cuda.set_device(0)
     _build.build()
     _lib.load()
+    if args.variant >= 0:  # applies to the backprojections of that variant's storage format
+        _lib.check(_lib.load().tk_bp_select_variant(args.variant))
 
     def barrier():
         if dist:
@@ -347,6 +363,7 @@ def run_ours(args):
         fbp.SetScaleXYZ(g.scale)
         fbp.SetFilter("hann")
         fbp.SetPrecision("f16")
+        fbp.SetPipeline(True)  # as the C++ FilteredBackProjection: reconstruct while the chunks land
         raw_np = raw_h.numpy().view(np.uint16)
 
         parts = {"initialize_s": [], "reconstruction_s": []}
@@ -354,9 +371,9 @@ def run_ours(args):
         def e2e_step(record=False):
             fbp.SetProjectionsU16(raw_np, "projection", flat_value=I0)
             t_a = time.perf_counter()
-            fbp.Initialize()  # upload (chunks filtered as they land)
+            fbp.Initialize()  # upload in 4 angle chunks, each filtered and backprojected as it lands
             t_b = time.perf_counter()
-            fbp.CalculateReconstruction()  # backprojection by Z blocks, D2H into the sink
+            fbp.CalculateReconstruction()  # D2H of each Z block once its last backprojection has run
             if record:
                 parts["initialize_s"].append(t_b - t_a)
                 parts["reconstruction_s"].append(time.perf_counter() - t_b)
@@ -379,7 +396,8 @@ def run_ours(args):
                "upload_ms": timings["h2d_ms"],
                "h2d_bytes_per_step": int(raw.numel() * 2), "d2h_bytes_per_step": int(g.X * g.Y * g.Z * 4),
                "api": "C ABI tk_fdk_* (FilteredBackProjection mirror): u16 projections from pinned host, "
-                      "volume to pinned host via the bin_siz-style block sink, 128-slice blocks"}
+                      "volume to pinned host via the bin_siz-style block sink, 128-slice blocks, pipelined "
+                      "(tk_fdk_set_pipeline)"}
 
     if rank != 0:
         if dist:
@@ -441,7 +459,7 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": launches[_lib.TK_F16],
         "device_error_flags": flags,
-        "roofline": {"bound": "fp32", "kernel": "bp_cimg_kernel<f16,16,16,64,3,packed>",
+        "roofline": {"bound": "fp32", "kernel": bp_kernel_name(args.variant),
                      "achieved": bp_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": bp_tflops / fp32_peak, "traffic": traffic,
                      "flops_per_update": FLOPS_PER_UPDATE, "peak_nominal": PEAK_FP32_NOMINAL,
@@ -549,12 +567,14 @@ def run_adjoint(args):
     import torch
 
     from tomokvas_gb300 import _build, _lib, device
-    from tomokvas_gb300.geometry import config
+    from tomokvas_gb300.geometry import FDKGeometry, config
     from tomokvas_gb300.phantom import random_ellipsoids
 
     _build.build()
     torch.cuda.set_device(0)
     g = config("c4")
+    if args.profile_adjoint:
+        g = FDKGeometry.circular(120, 768, 768, 0.2, 400.0, 800.0, (512, 512, 512), 0.15)
     ell = random_ellipsoids(20, g.fov_radius_cm, g.Z * g.voxel_cm / 2, seed=4)
     p = device.phantom_project(g, ell, _lib.TK_LAYOUT_SINOGRAM)
     gen = torch.Generator(device="cuda").manual_seed(9)
@@ -585,7 +605,7 @@ def run_adjoint(args):
         res[name] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
     lhs = float(torch.sum(vol.double() * y.double()).item())
     rhs = float(torch.sum(p.double() * grad.double()).item())
-    emit({"workload": "fdk_adjoint_512cube_scale1.5_from_360x768sq_f32", "updates": g.updates, **res,
+    emit({"workload": f"fdk_adjoint_512cube_scale1.5_from_{g.N}x768sq_f32", "updates": g.updates, **res,
           "dot_product_rel_err": abs(lhs - rhs) / abs(lhs), "flags": device.device_error_flags()})
     return 0
 
@@ -693,7 +713,7 @@ def run_batch(args):
 
     _build.build()
     torch.cuda.set_device(0)
-    geos = batch_geometries()
+    geos = batch_geometries()[:max(1, args.items)]
     prec = _lib.TK_F16
     ins, vols, wss = [], [], []
     for k, g in enumerate(geos):
@@ -732,7 +752,7 @@ def run_batch(args):
     diff = max(float(np.abs(v[v.shape[0] // 2].cpu().numpy() - r).max() / max(np.abs(r).max(), 1e-30))
                for v, r in zip(vols, ref))
     flags = device.device_error_flags()
-    emit({"workload": "batch_64_uneven_fdk", "metric": "GUPS", "unit": "GUPS", "items": len(geos),
+    emit({"workload": f"batch_{len(geos)}_uneven_fdk", "metric": "GUPS", "unit": "GUPS", "items": len(geos),
           "updates": updates, "storage": "f16 coefficients", "steps": args.steps, "warmup": args.warmup,
           "per_volume": {"ms": ms_single, "gups": updates / (ms_single * 1e-3) / 1e9},
           "batch_eager": {"ms": ms_eager, "gups": updates / (ms_eager * 1e-3) / 1e9},

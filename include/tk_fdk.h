@@ -333,6 +333,21 @@ int tk_fdk_set_input_layout(tk_fdk *h, int layout);
 int tk_fdk_set_filter(tk_fdk *h, int window);
 int tk_fdk_set_precision(tk_fdk *h, int precision);
 int tk_fdk_set_stream(tk_fdk *h, void *stream);
+/* Pipelined mode (off by default; the C++ FilteredBackProjection turns it on).
+ * tk_fdk_initialize uploads the projections in four angle chunks, filters each
+ * chunk as it lands and backprojects the first chunk into a whole-volume
+ * device buffer (Z block by Z block, the reference's block offsets) while the
+ * others upload; it then queues one accumulating launch per Z block over the
+ * remaining angles and returns once the host buffer has been read.
+ * tk_fdk_calculate_reconstruction only delivers the blocks, each copy starting
+ * once its block's launch has run, overlapping the next block's launch.  It applies to
+ * non-collecting runs with N >= 128 whose storage scale is known up front
+ * (FP32 storage, or uint16 counts with scalar flat/dark) and whose volume fits
+ * in device memory beside the projections; otherwise the regular path runs.
+ * The chunk sums change FP32 rounding only.  A setter called after
+ * initialize drops the pipelined volume; tk_fdk_reconstruct_device always
+ * computes its own. */
+int tk_fdk_set_pipeline(tk_fdk *h, int on);
 /* Initialize (kernel.cu:324-428): select the device, allocate, copy the
  * projections to the GPU, build the angle tables. */
 int tk_fdk_initialize(tk_fdk *h);

@@ -19,7 +19,12 @@
 
 class FilteredBackProjection {
 public:
-    FilteredBackProjection() { tk_fdk_create(&h_); }
+    // pipelined: the reference's call sequence always ends in CalculateReconstruction
+    FilteredBackProjection()
+    {
+        tk_fdk_create(&h_);
+        tk_fdk_set_pipeline(h_, 1);
+    }
     ~FilteredBackProjection() { tk_fdk_destroy(h_); }
     FilteredBackProjection(const FilteredBackProjection &) = delete;
     FilteredBackProjection &operator=(const FilteredBackProjection &) = delete;

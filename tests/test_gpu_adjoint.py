@@ -22,10 +22,9 @@ def dev(a, torch):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-# The forward projector has two forms, picked from the smallest row step of
-# consecutive slices, |scale| D / (D + W/2): "plain" (0.95: atomic-free, two
-# passes by lane parity), "flips_scale" (1.43: atomic-free, one pass) and
-# "fine_voxels" (0.36: shared atomics).
+# Row steps of consecutive slices, |scale| D / (D + W/2), below, near and
+# above one detector row: "fine_voxels" (0.36: several slices share a row, the
+# most shared-atomic collisions), "plain" (0.95) and "flips_scale" (1.43).
 GEOMS = {
     "plain": dict(W=64, N=72, H=56, vol=(48, 48, 40)),
     "flips_scale": dict(W=60, N=50, H=64, vol=(40, 36, 45), voxel_mm=1.2, dirx=1, dirz=1, rot=0.4),

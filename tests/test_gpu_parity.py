@@ -356,34 +356,39 @@ def test_reconstruct_to_device_and_precisions(orc, cuda, case):
         assert t["bp_ms"] > 0 and t["filter_ms"] > 0
 
 
-@pytest.mark.parametrize("prec,raw", [("f16", True), ("f32", True), ("f32c", False)])
-def test_handle_chunked_upload_equals_device_path(orc, cuda, prec, raw):
-    """Projection-major input with a storage scale known up front is uploaded in
-    chunks that are filtered as they land (N = 150: chunks of 64, 64, 22); the
-    volume equals tk_fdk_device on the same input bit for bit."""
+@pytest.mark.parametrize("prec,raw,layout", [("f16", True, "projection"), ("f32", True, "projection"),
+                                             ("f32c", False, "projection"), ("f16", True, "sinogram"),
+                                             ("f32", False, "sinogram")])
+def test_handle_chunked_upload_equals_device_path(orc, cuda, prec, raw, layout):
+    """Input with a storage scale known up front is uploaded in chunks that are
+    filtered as they land (N = 150: chunks of 64, 64, 22; a sinogram-major
+    chunk is packed into an [H][nb][W] block by a strided copy); the volume
+    equals tk_fdk_device on the same input bit for bit."""
     import torch
 
     g = small_geometry(W=48, N=150, H=40, vol=(40, 40, 32))
     G = orc.geom_from(g)
     proj = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=3), G, "proj")  # [N][H][W]
+    if layout == "sinogram":
+        proj = np.ascontiguousarray(np.transpose(proj, (1, 0, 2)))
     fbp = FilteredBackProjection(raise_on_error=True)
     fbp.SetSinogramProperties(None, g.W, g.cX, g.N, g.H, g.cZ, g.dfi, g.D, g.tau)
     fbp.SetReconstructionProperties(None, g.X, g.cx, g.Y, g.cy, g.Z, g.cz, g.rot)
     fbp.SetPrecision(prec)
     if raw:
         counts = counts_u16(proj, 60000.0, seed=4)
-        fbp.SetProjectionsU16(counts, "projection", flat_value=60000.0)
+        fbp.SetProjectionsU16(counts, layout, flat_value=60000.0)
         d_in = torch.from_numpy(counts.view(np.int16)).cuda()
         ff, itype = device.flatfield(flat_value=60000.0), _lib.TK_INPUT_U16
     else:
         fbp.SetSinogramProperties(proj, g.W, g.cX, g.N, g.H, g.cZ, g.dfi, g.D, g.tau)
-        fbp.SetInputLayout("projection")
+        fbp.SetInputLayout(layout)
         d_in, ff, itype = torch.from_numpy(proj).cuda(), None, _lib.TK_INPUT_F32
     fbp.Initialize()
     vol = torch.empty((g.Z, g.Y, g.X), dtype=torch.float32, device="cuda")
     fbp.ReconstructToDevice(vol.data_ptr())
     fbp.close()
-    ref = device.fdk_device(g, d_in, itype, _lib.TK_LAYOUT_PROJECTION, ff=ff, precision=_lib.PRECISIONS[prec])
+    ref = device.fdk_device(g, d_in, itype, _lib.LAYOUTS[layout], ff=ff, precision=_lib.PRECISIONS[prec])
     torch.cuda.synchronize()
     np.testing.assert_array_equal(vol.cpu().numpy(), ref.cpu().numpy())
 
@@ -445,3 +450,82 @@ def test_full_size_1024_sampled_slices(orc, cuda):
         del vol
         assert grouped(got) < tol, (prec, grouped(got), rest_err)
     assert device.device_error_flags() == 0
+
+
+def _handle_run(g, data, layout, prec, pipeline, zb, counts=None, after_init=None, window=None):
+    out = VolumeSink(g.X, g.Y, g.Z, zb)
+    fbp = FilteredBackProjection(raise_on_error=True)
+    fbp.SetBlockSize(zb)
+    fbp.SetPipeline(pipeline)
+    fbp.SetSinogramProperties(data, g.W, g.cX, g.N, g.H, g.cZ, g.dfi, g.D, g.tau)
+    fbp.SetReconstructionProperties(out, g.X, g.cx, g.Y, g.cy, g.Z, g.cz, g.rot)
+    fbp.SetScaleXYZ(g.scale)
+    fbp.SetPrecision(prec)
+    if window:
+        fbp.SetFilter(window)
+    if counts is not None:
+        fbp.SetProjectionsU16(counts, layout, flat_value=60000.0)
+    else:
+        fbp.SetInputLayout(layout)
+    L = _lib.load()
+    n0 = L.tk_kernel_launches()
+    fbp.Initialize()
+    if after_init:
+        after_init(fbp)
+    fbp.CalculateReconstruction()
+    launches = L.tk_kernel_launches() - n0
+    fbp.close()
+    return out, launches
+
+
+@pytest.mark.parametrize("vol_shape,zb,prec,raw,layout", [
+    ((40, 40, 40), 16, "f32", False, "projection"),   # blocks 16, 16, 8
+    ((40, 40, 33), 16, "f16", True, "projection"),    # last-slice quirk
+    ((36, 40, 30), 64, "f32c", False, "projection"),  # one block, zb > Z
+    ((40, 40, 40), 16, "f16", True, "sinogram"),      # [H][N][W], packed per chunk by strided copies
+    ((40, 40, 33), 16, "f32", False, "sinogram")])
+def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, layout):
+    """tk_fdk_set_pipeline: Initialize uploads N = 300 projections in four
+    75-angle chunks, filters each as it lands, backprojects the first chunk
+    into the whole volume with the Z-block schedule, then each block over the
+    other 225 angles; CalculateReconstruction only delivers blocks.  The
+    volume equals the regular path's to FP32 rounding of the two-part sums,
+    with the same blocks requested, the same last-slice quirk, and
+    4 x (storage scale + filter) + 2 x (one backprojection per block) launches."""
+    g = small_geometry(W=48, N=300, H=48, vol=vol_shape, zb=zb)
+    G = orc.geom_from(g)
+    proj = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=5), G, "proj")  # [N][H][W]
+    if layout == "sinogram":
+        proj = np.ascontiguousarray(np.transpose(proj, (1, 0, 2)))
+    counts = counts_u16(proj, 60000.0, seed=6) if raw else None
+    data = None if raw else proj
+    reg, _ = _handle_run(g, data, layout, prec, False, zb, counts)
+    pip, launches = _handle_run(g, data, layout, prec, True, zb, counts)
+    nblk = len(orc.zblocks(G))
+    assert launches == 4 * 2 + 2 * nblk
+    assert pip.blocks_requested == reg.blocks_requested
+    assert rel_rmse(pip.volume, reg.volume) < 1e-6
+    assert max_abs(pip.volume, reg.volume) < 1e-5 * np.abs(reg.volume).max()
+    if (g.Z - 1) % zb == 0:
+        assert np.all(pip.volume[-1] == 0) and np.all(reg.volume[-1] == 0)
+    if not raw:  # the FP32 restatement follows the handle's Z-block schedule (last-slice quirk included)
+        sino = proj if layout == "sinogram" else np.ascontiguousarray(np.transpose(proj, (1, 0, 2)))
+        assert rel_rmse(pip.volume, orc.fdk_f32(sino, G)) < (F16_RMSE if prec == "f16" else F32_RMSE)
+
+
+def test_setter_after_pipelined_initialize(orc, cuda):
+    """A setter after Initialize (here the window) drops the pipelined volume
+    and the filtered projections: the sinogram, stored on the device as
+    per-chunk [H][nb][W] blocks, is unpacked and filtered again, and the
+    volume equals a fresh regular run with that window."""
+    g = small_geometry(W=48, N=300, H=48, vol=(40, 40, 40), zb=16)
+    G = orc.geom_from(g)
+    sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=7), G, "sino")
+    hann = lambda fbp: fbp.SetFilter("hann")  # noqa: E731
+    changed, launches = _handle_run(g, sino, "sinogram", "f32", True, 16, after_init=hann)
+    fresh, _ = _handle_run(g, sino, "sinogram", "f32", False, 16, window="hann")
+    nblk = len(orc.zblocks(G))
+    assert launches == 4 * 2 + 2 * nblk + 2 + nblk  # the pipelined pass, then one regular pass
+    # the fresh run filters in even 64-angle chunks, which pair FFT rows as one pass does
+    assert rel_rmse(changed.volume, fresh.volume) < 1e-7
+    assert max_abs(changed.volume, fresh.volume) <= 1e-6 * np.abs(fresh.volume).max()

@@ -33,6 +33,7 @@ EXPORTS = [
     "tk_fdk_set_show_info", "tk_fdk_set_axis_direction", "tk_fdk_set_sinogram_properties",
     "tk_fdk_set_reconstruction_properties", "tk_fdk_set_scale_xyz", "tk_fdk_set_projections_u16",
     "tk_fdk_set_input_layout", "tk_fdk_set_filter", "tk_fdk_set_precision", "tk_fdk_set_stream",
+    "tk_fdk_set_pipeline",
     "tk_fdk_initialize", "tk_fdk_calculate_reconstruction", "tk_fdk_reconstruct_device", "tk_fdk_get_timings",
     "tk_batch_create", "tk_batch_destroy", "tk_batch_set_precision", "tk_batch_submit", "tk_batch_size",
     "tk_batch_workspace_bytes", "tk_batch_plan", "tk_batch_run", "tk_batch_autotune", "tk_batch_variant_count",
@@ -157,7 +158,7 @@ def _declare(L):
         ("tk_fdk_set_scale_xyz", [fp]),
         ("tk_fdk_set_projections_u16", [vp, ip, vp, vp, fp, fp, fp, fp, ip, fp]),
         ("tk_fdk_set_input_layout", [ip]), ("tk_fdk_set_filter", [ip]), ("tk_fdk_set_precision", [ip]),
-        ("tk_fdk_set_stream", [vp]), ("tk_fdk_initialize", []),
+        ("tk_fdk_set_stream", [vp]), ("tk_fdk_set_pipeline", [ip]), ("tk_fdk_initialize", []),
         ("tk_fdk_calculate_reconstruction", [BLOCK_SINK, vp]), ("tk_fdk_reconstruct_device", [vp]),
         ("tk_fdk_get_timings", [ctypes.POINTER(fp)] * 4),
     ]:

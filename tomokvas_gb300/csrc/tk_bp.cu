@@ -341,7 +341,7 @@ __device__ __forceinline__ int2 footprint_origin_z(const BPParams &P, int b, int
     return make_int2(bx, (int)floorf(vmin) - 1);
 }
 
-template <int PREC, int TX, int TY, int TZ, int STAGES, bool PARTIAL, int MINB, bool PACKED = false>
+template <int PREC, int TX, int TY, int TZ, int STAGES, bool PARTIAL, int MINB, int WALK = 0>
 __global__ void __launch_bounds__(TX *TY, MINB)
     bp_cimg_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
@@ -430,9 +430,9 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                                            (uint32_t)(kMagicBits + by0) * row_bytes;
                     const float U2 = __fmul_rn(U, U);
                     if (vlo >= 0.f && vhi <= Hm1)
-                        update_cimg<PREC, TZ, true, PARTIAL, PACKED>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                        update_cimg<PREC, TZ, true, PARTIAL, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                     else
-                        update_cimg<PREC, TZ, false, PARTIAL, PACKED>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                        update_cimg<PREC, TZ, false, PARTIAL, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                 } else {
                     atomicOr(P.err, ERR_BOX_OVERFLOW);
                 }
@@ -604,143 +604,6 @@ __global__ void __launch_bounds__(TX *TY, 2)
 }
 
 // ---------------------------------------------------------------------------
-// Forward projector without atomics (the transpose of bp_tma_kernel, same
-// weights and masks as fp_scatter_kernel).  Lanes are slices: lane l of a
-// warp holds slice z0 + l of the 32 voxel columns the warp owns, so for one
-// column the 32 lanes sit on 32 rows that advance by dv = scale U per lane;
-// with |dv| >= 1 (checked on the host with a margin) they are distinct and
-// the lanes add their row-r terms, then (after __syncwarp) their row-(r+1)
-// terms, with plain shared loads and stores.  For 0.5 <= |dv| < 1 each of
-// the two phases runs as two passes by lane parity.  Each warp adds into
-// its own box, so warps never collide; after the tile's columns a drain sums
-// the eight boxes into the staging box (clearing them) and one TMA reduce adds
-// it to the gradient.  The per-column geometry is computed once by lane j
-// for column j and broadcast with shuffles.
-template <int TX, int TY, bool PARTIAL>
-__global__ void __launch_bounds__(TX *TY, 2)
-    fp_scatter_warp_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P,
-                           const float *__restrict__ vin, int parity_passes)
-{
-    constexpr int NT = TX * TY, NW = NT / 32, TZ = 32;
-    static_assert(NT / NW == 32, "one column per lane");
-    extern __shared__ __align__(128) unsigned char smem[];
-    const int BW = P.BW, BWp = P.BW + 1, BH = P.BH;
-    const int box_elems = (BH * BWp + 31) & ~31;
-    float *staging = reinterpret_cast<float *>(smem);                // 2 x [BH][BW]
-    float *boxes = staging + 2 * (size_t)P.stage_elems;              // NW x [BH][BW + 1]
-    int2 *boxo = reinterpret_cast<int2 *>(boxes + (size_t)NW * box_elems);
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int2 tile = tile_of(blockIdx.x, P.tilesX, P.tilesY);
-    const int x0 = tile.x * TX, y0 = tile.y * TY;
-    const int zc = blockIdx.y * TZ;
-    const int z0 = PARTIAL ? zc : min(zc, P.nz - TZ);
-    const int zlast = PARTIAL ? P.nz - 1 - z0 : TZ - 1;
-    // column of this lane (for the per-column geometry) and of every step j
-    const int cidx = warp * 32 + lane;
-    const int cx = x0 + cidx % TX, cy = y0 + cidx / TX;
-    const float aX = flip(P.scale * ((float)cx + P.dX), P.dirx);
-    const float aY = flip(P.scale * ((float)cy + P.dY), P.diry);
-    const bool cinside = (cx < P.X) && (cy < P.Y);
-    const bool cactive = cinside && (sqrtf(aX * aX + aY * aY) < P.halfW);
-    if (!__syncthreads_or(cactive)) return;  // nothing in this tile projects
-
-    for (int b = tid; b < P.N; b += NT) {
-        int2 o = footprint_origin_z<TX, TY, 4>(P, b, x0, y0, z0, z0 + zlast);
-        o.x = max(o.x, 0);  // still a multiple of 4
-        o.y = max(o.y, 0);
-        boxo[b] = o;
-    }
-    for (int i = tid; i < NW * box_elems; i += NT) boxes[i] = 0.f;
-    // the slice of this lane, and the voxel values of the warp's 32 columns in it (scaled)
-    const int z = lane;
-    const bool zown = z <= zlast && z0 + z >= zc;
-    const float aZ = flip(P.scale * ((float)min(z0 + z, P.nz - 1) + P.zoff), P.dirz);
-    float g[32];
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        const int c = warp * 32 + j;
-        const int x = x0 + c % TX, y = y0 + c / TX;
-        g[j] = 0.f;
-        if (zown && x < P.X && y < P.Y)
-            g[j] = P.fscale * vin[(size_t)(z0 + z) * P.slice_stride + (size_t)y * P.X + x];
-    }
-    const float cZ = P.cZ, Hm1 = P.Hm1;
-    float *mybox = boxes + (size_t)warp * box_elems;
-    __syncthreads();
-
-    for (int b = 0; b < P.N; ++b) {
-        const int bx0 = boxo[b].x, by0 = boxo[b].y;
-        // geometry of this lane's column
-        float U = 0.f, u = -1.f;
-        if (cactive) column_geometry(aX, aY, P.trig[b], P.D, P.cX, U, u);
-        int colok = -1;
-        float fu = 0.f;
-        if (cactive && u >= 0.f && u <= P.Wm1) {
-            const float fla = __fadd_rd(u, kMagic);
-            colok = __float_as_int(fla) - kMagicBits - bx0;
-            fu = u - (fla - kMagic);
-        }
-        const float U2 = __fmul_rn(U, U);
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const int col = __shfl_sync(0xffffffffu, colok, j);
-            if (col < 0) continue;  // uniform: column outside the FOV or the detector
-            const float Uj = __shfl_sync(0xffffffffu, U, j);
-            const float fuj = __shfl_sync(0xffffffffu, fu, j);
-            const float U2j = __shfl_sync(0xffffffffu, U2, j);
-            const float v = slice_v(aZ, Uj, cZ);
-            const bool in = g[j] != 0.f && v >= 0.f && v <= Hm1;
-            const float fl = __fadd_rd(v, kMagic);
-            const float fv = v - (fl - kMagic);
-            const int row = __float_as_int(fl) - kMagicBits - by0;
-            const bool okbox = col + 1 < BW && row >= 0 && row + 1 < BH;
-            if (in && !okbox) atomicOr(P.err, ERR_BOX_OVERFLOW);
-            const bool act = in && okbox;
-            const float w = U2j * g[j];
-            const float w1 = w * fuj, w0 = w - w1;  // columns col, col+1
-            float *r0 = mybox + row * BWp + col;
-            // row r, then row r+1: distinct rows across lanes within a pass
-            for (int pass = 0; pass < parity_passes; ++pass) {
-                if (act && (parity_passes == 1 || (lane & 1) == pass)) {
-                    r0[0] += w0 - w0 * fv;
-                    r0[1] += w1 - w1 * fv;
-                }
-                __syncwarp();
-            }
-            for (int pass = 0; pass < parity_passes; ++pass) {
-                if (act && (parity_passes == 1 || (lane & 1) == pass)) {
-                    r0[BWp] += w0 * fv;
-                    r0[BWp + 1] += w1 * fv;
-                }
-                __syncwarp();
-            }
-        }
-        float *st = staging + (size_t)(b & 1) * P.stage_elems;
-        if (tid == 0 && b >= 2) bulk_wait_group_read<1>();  // the reduce of b-2 has read this staging box
-        __syncthreads();
-        for (int i = tid; i < BH * BW; i += NT) {
-            const int r = i / BW, c = i - r * BW;
-            float sum = 0.f;
-#pragma unroll
-            for (int w2 = 0; w2 < NW; ++w2) {
-                float *a = boxes + (size_t)w2 * box_elems + r * BWp + c;
-                sum += *a;
-                *a = 0.f;
-            }
-            st[i] = sum;
-        }
-        fence_proxy_async_smem();
-        __syncthreads();
-        if (tid == 0) {
-            if (bx0 < (int)P.Wm1 + 1 && by0 < (int)P.Hm1 + 1) tma_reduce_add_3d(&tmap, bx0, by0, b, st);
-            bulk_commit_group();  // one group per projection, empty when the box misses the detector
-        }
-    }
-    if (tid == 0) bulk_wait_group_all();
-}
-
-// ---------------------------------------------------------------------------
 // host side
 
 static PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
@@ -777,9 +640,14 @@ struct BPVariant {
      "cimg<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
 #define TK_BP_CIMG_PK(P, PN, TX, TY, TZ, ST, MB) \
-    {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB, true>), \
-     reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, true>), P, TX, TY, TZ, ST, true, \
+    {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB, 1>), \
+     reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 1>), P, TX, TY, TZ, ST, true, \
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
+// FP16 half-math walk (update_cimg WALK 2): not bit-identical to the FP32 walks
+#define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB) \
+    {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, 2>), \
+     reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, 2>), TK_F16, TX, TY, TZ, ST, \
+     true, "cimg_h2<f16," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
 // The first entry of each storage format is its default (the packed walks:
 // same bits as the scalar ones, fewer issued instructions).
@@ -797,6 +665,7 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 48, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
+    TK_BP_CIMG_H2(16, 16, 64, 3, 2),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
@@ -967,12 +836,6 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     TK_CHECK((long long)tilesX * tilesY < (1ll << 31) && zchunks < 65536, TK_ERR_UNSUPPORTED,
              "volume too large for one launch");
     const bool partial = nz < TZ;
-    // Rows of consecutive slices differ by |dv| = |scale| U >= |scale| D / (D + W/2) inside the FOV:
-    // at least one row (with a margin for rounding) lets the lanes of the atomic-free kernel write
-    // distinct rows in one pass, half a row in two passes by lane parity; below that the atomic
-    // kernel runs.
-    const double dv_min = std::fabs((double)g.scale) * g.D / (g.D + 0.5 * g.W);
-    const int passes = dv_min >= 1.01 ? 1 : (dv_min >= 0.51 ? 2 : 0);
     const void *fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
                              : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>);
 
@@ -1019,25 +882,13 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
         const size_t acc_elems = (size_t)((BH * (BW + 1) + 31) & ~31);  // odd-pitch accumulation box
-        const size_t tail = (size_t)nb * sizeof(int2) + 16;
-        const size_t smem_warp = (2 * (size_t)P.stage_elems + 8 * acc_elems) * sizeof(float) + tail;
-        const float *vin = d_vol;
+        const size_t smem = (2 * (size_t)P.stage_elems + acc_elems) * sizeof(float) + (size_t)nb * sizeof(int2) + 16;
+        TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "forward project: %zu B of shared memory needed", smem);
+        TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         dim3 grid((unsigned)(tilesX * tilesY), partial ? 1u : (unsigned)zchunks, 1);
-        if (passes > 0 && smem_warp <= 227 * 1024) {
-            // atomic-free scatter: warp-private boxes, lanes on distinct rows
-            const void *fw = partial ? reinterpret_cast<const void *>(&fp_scatter_warp_kernel<TX, TY, true>)
-                                     : reinterpret_cast<const void *>(&fp_scatter_warp_kernel<TX, TY, false>);
-            TK_CUDA(cudaFuncSetAttribute(fw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_warp));
-            int pp = passes;
-            void *args[] = {&tmap, &P, &vin, &pp};
-            TK_CUDA(cudaLaunchKernel(fw, grid, dim3(TX * TY), args, smem_warp, stream));
-        } else {
-            const size_t smem = (2 * (size_t)P.stage_elems + acc_elems) * sizeof(float) + tail;
-            TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "forward project: %zu B of shared memory needed", smem);
-            TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            void *args[] = {&tmap, &P, &vin};
-            TK_CUDA(cudaLaunchKernel(fn, grid, dim3(TX * TY), args, smem, stream));
-        }
+        const float *vin = d_vol;
+        void *args[] = {&tmap, &P, &vin};
+        TK_CUDA(cudaLaunchKernel(fn, grid, dim3(TX * TY), args, smem, stream));
         count_launch();
     }
     return TK_OK;

@@ -135,15 +135,65 @@ __device__ __forceinline__ void interp_acc_x2(float aa, float ab, float ba, floa
         : "f"(aa), "f"(ab), "f"(ba), "f"(bb), "f"(fva), "f"(fvb), "f"(wa), "f"(wb));
 }
 
-// PACKED walks two slices per step with packed FP32 (floor/frac, the row
-// interpolation and the accumulation); per voxel it performs exactly the
-// operations of the scalar walk, so both give the same bits.
-template <int PREC, int TZ, bool ALL_IN, bool PARTIAL, bool PACKED = false>
+// acc0 += w.lo * val.lo and acc1 += w.hi * val.hi: FP16 products (exact in
+// FP32) added to FP32 accumulators with one rounding (fma.rn.f32.f16).
+__device__ __forceinline__ void acc_mixed_x2(uint32_t val2, uint32_t w2, float &acc0, float &acc1)
+{
+    asm("{\n\t.reg .b16 vl, vh, wl, wh;\n\t"
+        "mov.b32 {vl, vh}, %2;\n\t"
+        "mov.b32 {wl, wh}, %3;\n\t"
+        "fma.rn.f32.f16 %0, wl, vl, %0;\n\t"
+        "fma.rn.f32.f16 %1, wh, vh, %1;\n\t}"
+        : "+f"(acc0), "+f"(acc1)
+        : "r"(val2), "r"(w2));
+}
+
+// Walks of a column (WALK):
+//   0  scalar FP32, one slice per step;
+//   1  packed FP32, two slices per step (floor/frac, the row interpolation and
+//      the accumulation as f32x2); per voxel exactly the operations of the
+//      scalar walk, so both give the same bits;
+//   2  FP16 storage only, two slices per step: floor/frac in FP32 as above;
+//      the column interpolation of both entries by HFMA2, then the row
+//      interpolation of both slices by one HFMA2 with the fractions rounded
+//      to FP16, and the weight U^2 rounded to FP16 applied by fma.rn.f32.f16
+//      into the FP32 accumulators.  Fewer FP32-pipe operations, FP16
+//      rounding of fv, U^2 and the interpolated sample.
+template <int PREC, int TZ, bool ALL_IN, bool PARTIAL, int WALK = 0>
 __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu,
                                             float U2, float Hm1, int zlast, float (&acc)[TZ])
 {
     const float2 fu2 = pack_fu<PREC>(fu);
-    if constexpr (PACKED && !PARTIAL && (TZ % 2 == 0)) {
+    if constexpr (WALK == 2 && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
+        const __half2 fuh = *reinterpret_cast<const __half2 *>(&fu2.x);
+        const __half2 U2h2 = __float2half2_rn(U2);
+        const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
+#pragma unroll
+        for (int z = 0; z < TZ; z += 2) {
+            const float va = fmaf((float)z, dv, v0), vb = fmaf((float)(z + 1), dv, v0);
+            float fla, flb, fva, fvb;
+            floor_frac_x2(va, vb, fla, flb, fva, fvb);
+            uint32_t loa, hia, lob, hib;
+            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                         : "=r"(loa), "=r"(hia)
+                         : "r"((uint32_t)__float_as_int(fla) * row_bytes + sbase));
+            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                         : "=r"(lob), "=r"(hib)
+                         : "r"((uint32_t)__float_as_int(flb) * row_bytes + sbase));
+            // (A, B) = (Q, dV) + fu (dU, dUV) per slice, then (A_a, A_b) + fv (B_a, B_b)
+            const __half2 ha = __hfma2(*reinterpret_cast<const __half2 *>(&hia), fuh,
+                                       *reinterpret_cast<const __half2 *>(&loa));
+            const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&hib), fuh,
+                                       *reinterpret_cast<const __half2 *>(&lob));
+            const __half2 val = __hfma2(__floats2half2_rn(fva, fvb), __highs2half2(ha, hb), __lows2half2(ha, hb));
+            uint32_t w2 = w_all;
+            if constexpr (!ALL_IN) {  // kernel.cu:130-131
+                w2 = ((va >= 0.f && va <= Hm1) ? (w_all & 0xffffu) : 0u) |
+                     ((vb >= 0.f && vb <= Hm1) ? (w_all & 0xffff0000u) : 0u);
+            }
+            acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), w2, acc[z], acc[z + 1]);
+        }
+    } else if constexpr (WALK >= 1 && !PARTIAL && (TZ % 2 == 0)) {
 #pragma unroll
         for (int z = 0; z < TZ; z += 2) {
             const float va = fmaf((float)z, dv, v0), vb = fmaf((float)(z + 1), dv, v0);

@@ -361,6 +361,14 @@ struct tk_fdk {
     bool initialized = false, filtered = false;
     cudaEvent_t ev[10] = {};
     float t_filter = 0, t_bp = 0, t_h2d = 0, t_d2h = 0;
+    // pipelined mode: the volume is reconstructed during initialize, angle chunk by chunk
+    int pipeline = 0;
+    float *d_vol_full = nullptr;
+    size_t vol_cap = 0;
+    std::vector<cudaEvent_t> ev_blocks;  // last backprojection of each Z block
+    bool reconstructed = false;
+    int pipe_zb = 0;   // Z-block size the pipelined volume was built with
+    int in_chunk = 0;  // > 0: sinogram-major input stored as [H][nb][W] blocks of in_chunk angles
 };
 
 static void release_device(tk_fdk *h)
@@ -375,6 +383,20 @@ static void release_device(tk_fdk *h)
     h->d_dark = h->d_flat = nullptr;
     h->d_block[0] = h->d_block[1] = nullptr;
     h->d_in_cap = h->d_ws_cap = h->dfl_cap = h->block_cap = 0;
+    cudaFree(h->d_vol_full);
+    h->d_vol_full = nullptr;
+    h->vol_cap = 0;
+    for (cudaEvent_t e : h->ev_blocks) cudaEventDestroy(e);
+    h->ev_blocks.clear();
+    h->reconstructed = false;
+    h->in_chunk = 0;
+}
+
+// A setter called after initialize: the filtered projections and a pipelined volume are stale.
+static void invalidate(tk_fdk *h)
+{
+    h->filtered = false;
+    h->reconstructed = false;
 }
 
 static int ensure(void **p, size_t *cap, size_t need)
@@ -474,7 +496,7 @@ extern "C" int tk_fdk_set_sinogram_properties(tk_fdk *h, const float *sinogram, 
     h->g.D = D;
     h->g.tau = tau;
     h->have_sino = true;
-    h->filtered = false;
+    invalidate(h);
     return TK_OK;
 }
 extern "C" int tk_fdk_set_reconstruction_properties(tk_fdk *h, int X, float cx, int Y, float cy, int Z, float cz,
@@ -490,14 +512,14 @@ extern "C" int tk_fdk_set_reconstruction_properties(tk_fdk *h, int X, float cx, 
     h->g.rot = rot;
     if (h->g.scale == 0.f) h->g.scale = 1.f;  // recn.scale default (kernel.cu:237)
     h->have_rec = true;
-    h->filtered = false;
+    invalidate(h);
     return TK_OK;
 }
 extern "C" int tk_fdk_set_scale_xyz(tk_fdk *h, float scale)
 {
     TK_H(h);
     h->g.scale = scale;
-    h->filtered = false;
+    invalidate(h);
     return TK_OK;
 }
 extern "C" int tk_fdk_set_projections_u16(tk_fdk *h, const uint16_t *raw, int layout, const float *dark_hw,
@@ -519,7 +541,7 @@ extern "C" int tk_fdk_set_projections_u16(tk_fdk *h, const uint16_t *raw, int la
     h->ff.B = B;
     h->ff.invert = invert ? 1 : 0;
     h->ff.floor_counts = floor_counts;
-    h->filtered = false;
+    invalidate(h);
     return TK_OK;
 }
 extern "C" int tk_fdk_set_input_layout(tk_fdk *h, int layout)
@@ -527,7 +549,7 @@ extern "C" int tk_fdk_set_input_layout(tk_fdk *h, int layout)
     TK_H(h);
     TK_CHECK(layout == TK_LAYOUT_SINOGRAM || layout == TK_LAYOUT_PROJECTION, TK_ERR_INVALID, "bad layout");
     h->layout = layout;
-    h->filtered = false;
+    invalidate(h);
     return TK_OK;
 }
 extern "C" int tk_fdk_set_filter(tk_fdk *h, int window)
@@ -535,7 +557,7 @@ extern "C" int tk_fdk_set_filter(tk_fdk *h, int window)
     TK_H(h);
     TK_CHECK(window >= TK_WINDOW_RAMLAK && window <= TK_WINDOW_HANN, TK_ERR_INVALID, "bad window %d", window);
     h->window = window;
-    h->filtered = false;
+    invalidate(h);
     return TK_OK;
 }
 extern "C" int tk_fdk_set_precision(tk_fdk *h, int precision)
@@ -543,7 +565,7 @@ extern "C" int tk_fdk_set_precision(tk_fdk *h, int precision)
     TK_H(h);
     TK_CHECK(valid_precision(precision), TK_ERR_INVALID, "bad precision %d", precision);
     h->precision = precision;
-    h->filtered = false;
+    invalidate(h);
     return TK_OK;
 }
 extern "C" int tk_fdk_set_stream(tk_fdk *h, void *stream)
@@ -552,6 +574,14 @@ extern "C" int tk_fdk_set_stream(tk_fdk *h, void *stream)
     TK_CHECK(!h->initialized, TK_ERR_STATE, "set_stream after initialize");
     h->stream = static_cast<cudaStream_t>(stream);
     h->own_stream = false;
+    return TK_OK;
+}
+
+extern "C" int tk_fdk_set_pipeline(tk_fdk *h, int on)
+{
+    TK_H(h);
+    h->pipeline = on ? 1 : 0;
+    h->reconstructed = false;
     return TK_OK;
 }
 
@@ -586,14 +616,52 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
     if (int rc = ensure(&h->d_ws, &h->d_ws_cap, tk_fdk_workspace_bytes(&g, h->precision))) return rc;
     h->t_h2d = h->t_filter = h->t_bp = h->t_d2h = 0;
     TK_CUDA(cudaEventRecord(h->ev[0], h->stream));
-    // Projection-major input whose storage scale is known before the data is
-    // seen (FP32 storage, or uint16 with scalar flat/dark) is copied in chunks
-    // and each chunk is filtered as soon as it has landed, so the upload
-    // overlaps the filter; otherwise one copy, and the filter runs later.
+    // Input whose storage scale is known before the data is seen (FP32
+    // storage, or uint16 with scalar flat/dark) is copied in angle chunks and
+    // each chunk is filtered as soon as it has landed, so the upload overlaps
+    // the filter; otherwise one copy, and the filter runs later.  Sinogram-major
+    // input ([H][N][W]) is packed chunk by chunk into [H][nb][W] blocks by a
+    // strided copy, which the filter reads as a sinogram of nb angles.
     const bool scale_free = !(h->precision == TK_F16 || h->precision == TK_BF16) ||
                             (h->input_type == TK_INPUT_U16 && !h->host_dark && !h->host_flat);
-    const int chunk = 64;
-    const bool overlap = h->layout == TK_LAYOUT_PROJECTION && scale_free && g.N >= 2 * chunk;
+    // Pipelined mode (tk_fdk_set_pipeline), with the Z-block schedule into a whole-volume buffer:
+    // the first of four chunks is backprojected block by block while the other chunks upload;
+    // once every chunk is filtered, each block gets one accumulating launch over the remaining
+    // angles, so blocks complete one after another and each block's copy to the host
+    // (calculate_reconstruction) overlaps the next block's launch.  A volume that does not fit
+    // beside the projections falls back to the regular path.
+    bool pipe = h->pipeline && !h->collecting && scale_free && g.N >= 2 * 64;
+    h->reconstructed = false;
+    if (pipe) {
+        const size_t vbytes = (size_t)g.X * g.Y * std::max(g.Z, 1) * sizeof(float);
+        if (h->vol_cap < vbytes || !h->d_vol_full) {
+            cudaFree(h->d_vol_full);
+            h->d_vol_full = nullptr;
+            h->vol_cap = 0;
+            if (cudaMalloc(reinterpret_cast<void **>(&h->d_vol_full), vbytes) == cudaSuccess) {
+                h->vol_cap = vbytes;
+            } else {
+                (void)cudaGetLastError();
+                h->d_vol_full = nullptr;
+                pipe = false;
+            }
+        }
+    }
+    const int chunk = pipe ? std::max(64, (g.N + 3) / 4) : 64;
+    const bool overlap = scale_free && g.N >= 2 * chunk;
+    int nblk = 0;
+    std::vector<float> zoff;
+    if (pipe) {
+        nblk = tk_zblock_offsets(&g, h->zb, nullptr, 0);
+        zoff.resize((size_t)std::max(nblk, 1));
+        tk_zblock_offsets(&g, h->zb, zoff.data(), nblk);
+        while ((int)h->ev_blocks.size() < nblk) {
+            cudaEvent_t e;
+            TK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            h->ev_blocks.push_back(e);
+        }
+    }
+    h->in_chunk = overlap && h->layout == TK_LAYOUT_SINOGRAM ? chunk : 0;
     if (!overlap)
         TK_CUDA(cudaMemcpyAsync(h->d_in, h->host_in, in_bytes, cudaMemcpyHostToDevice, h->stream));
     if (h->input_type == TK_INPUT_U16) {
@@ -633,12 +701,22 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
         float *d_scale = static_cast<float *>(h->d_ws);
         char *d_q = static_cast<char *>(h->d_ws) + kWsHeader;
         const size_t qframe = filtered_bytes(g, h->precision) / (size_t)g.N;
+        const size_t slab = (size_t)g.X * g.Y;
         TK_CUDA(cudaEventRecord(h->ev[2], h->stream));
         for (int b0 = 0; b0 < g.N; b0 += chunk) {
             const int nb = std::min(chunk, g.N - b0);
             const size_t off = (size_t)b0 * frame;
-            TK_CUDA(cudaMemcpyAsync(static_cast<char *>(h->d_in) + off, static_cast<const char *>(h->host_in) + off,
-                                    (size_t)nb * frame, cudaMemcpyHostToDevice, h->copy_stream));
+            if (h->layout == TK_LAYOUT_PROJECTION) {
+                TK_CUDA(cudaMemcpyAsync(static_cast<char *>(h->d_in) + off,
+                                        static_cast<const char *>(h->host_in) + off, (size_t)nb * frame,
+                                        cudaMemcpyHostToDevice, h->copy_stream));
+            } else {
+                const size_t row = frame / (size_t)g.H;  // one detector row of one angle
+                TK_CUDA(cudaMemcpy2DAsync(static_cast<char *>(h->d_in) + off, (size_t)nb * row,
+                                          static_cast<const char *>(h->host_in) + (size_t)b0 * row,
+                                          (size_t)g.N * row, (size_t)nb * row, (size_t)g.H,
+                                          cudaMemcpyHostToDevice, h->copy_stream));
+            }
             TK_CUDA(cudaEventRecord(h->ev[9], h->copy_stream));
             TK_CUDA(cudaStreamWaitEvent(h->stream, h->ev[9], 0));
             tk_geometry gc = g;
@@ -646,8 +724,32 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
             if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + off, h->input_type, h->layout, &h->ff,
                                        h->window, d_q + (size_t)b0 * qframe, h->precision, d_scale, h->stream))
                 return rc;
+            if (pipe && b0 == 0) {
+                for (int n = 0; n < nblk; ++n) {
+                    int slices = h->zb;
+                    if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;  // kernel.cu:838-840
+                    if (int rc = launch_backproject(gc, d_q, h->precision, d_scale, slices, zoff[n],
+                                                    h->d_vol_full + (size_t)n * h->zb * slab, 0, h->stream, 0))
+                        return rc;
+                }
+            }
+        }
+        if (pipe) {
+            tk_geometry gr = g;
+            gr.N = g.N - chunk;
+            for (int n = 0; n < nblk; ++n) {
+                int slices = h->zb;
+                if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;
+                if (int rc = launch_backproject(gr, d_q + (size_t)chunk * qframe, h->precision, d_scale, slices,
+                                                zoff[n], h->d_vol_full + (size_t)n * h->zb * slab, 1, h->stream,
+                                                chunk))
+                    return rc;
+                TK_CUDA(cudaEventRecord(h->ev_blocks[n], h->stream));
+            }
         }
         TK_CUDA(cudaEventRecord(h->ev[3], h->stream));
+        h->reconstructed = pipe;
+        h->pipe_zb = h->zb;
         TK_CUDA(cudaEventRecord(h->ev[1], h->copy_stream));
         TK_CUDA(cudaStreamSynchronize(h->copy_stream));  // the host buffer is only borrowed until we return
         h->filtered = true;
@@ -661,9 +763,40 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
     return TK_OK;
 }
 
+// Sinogram-major input uploaded in angle chunks lies on the device as [H][nb][W]
+// blocks (tk_fdk_initialize); a setter called after initialize needs it
+// filtered again as one [H][N][W] sinogram, so it is unpacked first.
+static int unpack_input(tk_fdk *h)
+{
+    if (h->in_chunk <= 0) return TK_OK;
+    const tk_geometry &g = h->g;
+    const size_t row = (size_t)g.W * (h->input_type == TK_INPUT_U16 ? 2 : 4);
+    const size_t bytes = row * g.N * g.H;
+    void *flat = nullptr;
+    TK_CUDA(cudaMalloc(&flat, bytes));
+    for (int b0 = 0; b0 < g.N; b0 += h->in_chunk) {
+        const int nb = std::min(h->in_chunk, g.N - b0);
+        const cudaError_t e = cudaMemcpy2DAsync(static_cast<char *>(flat) + (size_t)b0 * row, (size_t)g.N * row,
+                                                static_cast<const char *>(h->d_in) + (size_t)b0 * row * g.H,
+                                                (size_t)nb * row, (size_t)nb * row, (size_t)g.H,
+                                                cudaMemcpyDeviceToDevice, h->stream);
+        if (e != cudaSuccess) {
+            cudaFree(flat);
+            TK_CUDA(e);
+        }
+    }
+    TK_CUDA(cudaStreamSynchronize(h->stream));
+    cudaFree(h->d_in);
+    h->d_in = flat;
+    h->d_in_cap = bytes;
+    h->in_chunk = 0;
+    return TK_OK;
+}
+
 static int run_filter(tk_fdk *h)
 {
     if (h->filtered) return TK_OK;
+    if (int rc = unpack_input(h)) return rc;
     float *d_scale = static_cast<float *>(h->d_ws);
     void *d_q = static_cast<char *>(h->d_ws) + kWsHeader;
     TK_CUDA(cudaEventRecord(h->ev[2], h->stream));
@@ -704,6 +837,28 @@ extern "C" int tk_fdk_calculate_reconstruction(tk_fdk *h, tk_block_sink sink, vo
     std::vector<float> zoff((size_t)std::max(nblk, 1));
     tk_zblock_offsets(&g, zb, zoff.data(), nblk);
     const size_t slab = (size_t)g.X * g.Y;
+    if (h->reconstructed && !h->collecting && h->pipe_zb == zb) {
+        // pipelined: the volume was reconstructed during initialize; block n is copied out once its
+        // last backprojection has run, and lands before block n+1 is requested from the sink
+        cudaEvent_t d2h_done[2] = {h->ev[6], h->ev[7]};
+        float *prev_host = nullptr;
+        for (int n = 0; n < nblk; ++n) {
+            int slices = zb;
+            if ((long long)(n + 1) * zb > g.Z) slices = g.Z - n * zb;  // kernel.cu:838-840
+            if (prev_host) TK_CUDA(cudaEventSynchronize(d2h_done[(n - 1) & 1]));
+            float *host = sink(user, n, 0);
+            TK_CHECK(host, TK_ERR_IO, "block sink returned NULL for block %d", n);
+            TK_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_blocks[n], 0));
+            TK_CUDA(cudaMemcpyAsync(host, h->d_vol_full + (size_t)n * zb * slab, slab * (size_t)slices * sizeof(float),
+                                    cudaMemcpyDeviceToHost, h->copy_stream));
+            TK_CUDA(cudaEventRecord(d2h_done[n & 1], h->copy_stream));
+            prev_host = host;
+        }
+        TK_CUDA(cudaStreamSynchronize(h->copy_stream));
+        TK_CUDA(cudaStreamSynchronize(h->stream));
+        elapsed(h->ev[2], h->ev[3], &h->t_bp);  // filter + backprojection, interleaved by chunk
+        return check_device_flags(h->stream);
+    }
     const size_t block_bytes = slab * zb * sizeof(float);
     if (h->block_cap < block_bytes || !h->d_block[0]) {
         cudaFree(h->d_block[0]);

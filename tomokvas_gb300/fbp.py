@@ -170,6 +170,10 @@ class FilteredBackProjection:
     def SetPrecision(self, precision: str):
         return self._rc(self._L.tk_fdk_set_precision(self._h, _lib.PRECISIONS[precision]))
 
+    def SetPipeline(self, on: bool = True):
+        """Reconstruct during Initialize, chunk by chunk as the projections upload (tk_fdk_set_pipeline)."""
+        return self._rc(self._L.tk_fdk_set_pipeline(self._h, int(bool(on))))
+
     def SetStream(self, stream_handle: int):
         return self._rc(self._L.tk_fdk_set_stream(self._h, ctypes.c_void_p(stream_handle)))
 
