@@ -72,7 +72,9 @@ __device__ __forceinline__ int2 batch_footprint(const BatchItem &I, float2 cs, i
     return make_int2(bx, (int)floorf(vmin) - 1);
 }
 
-template <int PREC, int TX, int TY, int TZ, int STAGES, int MINB, bool PACKED = true>
+// WALK as in update_cimg: 2 is the FP16 half-math walk for TK_F16 and the
+// packed FP32 walk for the other formats (the per-volume defaults).
+template <int PREC, int TX, int TY, int TZ, int STAGES, int MINB, int WALK = 2>
 __global__ void __launch_bounds__(TX *TY, MINB)
     bp_batch_kernel(const BatchItem *__restrict__ items, int nitems, int nunits, int *counter, unsigned *err,
                     int maxN, int slot_elems)
@@ -190,10 +192,10 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                                 update_cimg<PREC, TZ, false, true>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
                         } else {
                             if (all_in)
-                                update_cimg<PREC, TZ, true, false, PACKED>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
+                                update_cimg<PREC, TZ, true, false, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
                                                                            acc);
                             else
-                                update_cimg<PREC, TZ, false, false, PACKED>(sbase, row_bytes, v0, dv, fu, U2, Hm1,
+                                update_cimg<PREC, TZ, false, false, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1,
                                                                             zlast, acc);
                         }
                     } else {

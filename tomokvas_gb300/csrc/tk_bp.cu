@@ -649,11 +649,12 @@ struct BPVariant {
      reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, 2>), TK_F16, TX, TY, TZ, ST, \
      true, "cimg_h2<f16," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
-// The first entry of each storage format is its default (the packed walks:
-// same bits as the scalar ones, fewer issued instructions).
+// The first entry of each storage format is its default: the packed walks
+// (same bits as the scalar ones, fewer issued instructions), and for FP16
+// storage the half-math walk (FP16 row interpolation, FP32 accumulation).
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT_PK(16, 16, 32, 4),
-    TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
+    TK_BP_CIMG_H2(16, 16, 64, 3, 2),
     TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
     TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
     TK_BP_DIRECT(16, 16, 32, 4),
@@ -665,7 +666,7 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 48, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
-    TK_BP_CIMG_H2(16, 16, 64, 3, 2),
+    TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant

@@ -76,6 +76,9 @@ struct LoadParams {
     int in_pitch;   // elements between consecutive input rows of one layout line (W, or Wp)
     int weight_in;  // apply the cosine weight while loading (forward); 0 for the transpose
     float cX, cZ, D;
+    float D2;       // D * D
+    float inv_den;  // 1 / max(flat - dark, floor) for scalar flat/dark
+    int vec;        // rows start 16-byte aligned and span whole 16-byte chunks: chunked loads
 };
 
 struct FiltParams {
@@ -100,12 +103,22 @@ __device__ __forceinline__ long long in_row_offset(const LoadParams &L, long lon
     return L.layout == TK_LAYOUT_SINOGRAM ? ((long long)r * L.N + b) * L.in_pitch : row * (long long)L.in_pitch;
 }
 
-// row[x] *= distance / sqrt(ce*ce + distance*distance + cs*cs)  (kernel.cu:195-199)
-__device__ __forceinline__ float cosine_weight(const LoadParams &L, int r, int x)
+// row[x] *= distance / sqrt(ce*ce + distance*distance + cs*cs)  (kernel.cu:195-199),
+// evaluated as D rsqrt(ce^2 + (cs^2 + D^2)) with the row term cs^2 + D^2
+// formed once per row (within 2 ulp of the IEEE divide and square root).
+__device__ __forceinline__ float weight_row_term(const LoadParams &L, int r)
+{
+    const float cs = (float)r - L.cZ;
+    return fmaf(cs, cs, L.D2);
+}
+__device__ __forceinline__ float cosine_weight_rt(const LoadParams &L, float rt, int x)
 {
     const float ce = (float)x - L.cX;
-    const float cs = (float)r - L.cZ;
-    return L.D / sqrtf(ce * ce + L.D * L.D + cs * cs);
+    return L.D * rsqrtf(fmaf(ce, ce, rt));
+}
+__device__ __forceinline__ float cosine_weight(const LoadParams &L, int r, int x)
+{
+    return cosine_weight_rt(L, weight_row_term(L, r), x);
 }
 
 // Raw sample x of the row at element offset off (counts as float for u16).
@@ -115,43 +128,91 @@ __device__ __forceinline__ float load_raw(const LoadParams &L, long long off, in
                                         : static_cast<const float *>(L.in)[off + x];
 }
 
-// Preprocessing of a raw sample: flat-field + log if raw counts, then the
-// cosine weight (kernel.cu:195-199).
-__device__ __forceinline__ float pre_from_raw(const LoadParams &L, int r, int x, float raw)
+// Preprocessing of a raw sample: flat-field + log if raw counts
+// (rsq_load.cpp:299-325: A log(num / den) + B, num = max(I - dark, floor),
+// den = max(flat - dark, floor); here in FP32 with __logf, absolute error
+// below 4e-7 for transmissions near 1), then the cosine weight (kernel.cu:
+// 195-199).  rt is the row's weight_row_term.
+__device__ __forceinline__ float pre_from_raw(const LoadParams &L, int r, int x, float raw, float rt)
 {
     float val = raw;
     if (L.input_type == TK_INPUT_U16) {
-        const float I = raw;
-        const size_t px = (size_t)r * L.W + x;
-        const float dk = L.dark ? L.dark[px] : L.dark_v;
-        const float fl = L.flat ? L.flat[px] : L.flat_v;
-        const float num = fmaxf(I - dk, L.floor_counts);
-        const float den = fmaxf(fl - dk, L.floor_counts);
-        val = L.A * logf(num / den) + L.B;
+        float t;
+        if (L.dark || L.flat) {
+            const size_t px = (size_t)r * L.W + x;
+            const float dk = L.dark ? L.dark[px] : L.dark_v;
+            const float fl = L.flat ? L.flat[px] : L.flat_v;
+            t = __fdividef(fmaxf(raw - dk, L.floor_counts), fmaxf(fl - dk, L.floor_counts));
+        } else {
+            t = fmaxf(raw - L.dark_v, L.floor_counts) * L.inv_den;
+        }
+        val = fmaf(L.A, __logf(t), L.B);
         if (L.invert) val = -val;
     }
     if (!L.weight_in) return val;
-    return val * cosine_weight(L, r, x);
+    return val * cosine_weight_rt(L, rt, x);
 }
 
 // Preprocessed (log if raw, cosine weighted) sample x of a row.
 __device__ __forceinline__ float load_pre(const LoadParams &L, long long off, int r, int x)
 {
-    float val;
-    if (L.input_type == TK_INPUT_U16) {
-        const float I = (float)static_cast<const uint16_t *>(L.in)[off + x];
-        const size_t px = (size_t)r * L.W + x;
-        const float dk = L.dark ? L.dark[px] : L.dark_v;
-        const float fl = L.flat ? L.flat[px] : L.flat_v;
-        const float num = fmaxf(I - dk, L.floor_counts);
-        const float den = fmaxf(fl - dk, L.floor_counts);
-        val = L.A * logf(num / den) + L.B;
-        if (L.invert) val = -val;
-    } else {
-        val = static_cast<const float *>(L.in)[off + x];
+    return pre_from_raw(L, r, x, load_raw(L, off, x), weight_row_term(L, r));
+}
+
+// Raw samples x0 .. x0+NV-1 of the row at element offset off; samples at or
+// past W read as 0.  With L.vec the run is read with 16-byte loads (the run
+// starts on a 16-byte boundary: x0 is a multiple of NV, NV * element size is
+// a multiple of 16, rows start aligned and the row pitch covers every chunk
+// that starts below W).
+template <int NV>
+__device__ __forceinline__ void load_run(const LoadParams &L, long long off, int x0, bool valid, float (&v)[NV])
+{
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = 0.f;
+    if (!valid) return;
+    if constexpr (NV % 8 == 0) {
+        if (L.vec && L.input_type == TK_INPUT_U16) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(static_cast<const uint16_t *>(L.in) + off + x0);
+#pragma unroll
+            for (int k = 0; k < NV / 8; ++k) {
+                if (x0 + 8 * k < L.W) {
+                    const uint4 q = __ldg(src + k);
+                    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        v[8 * k + 2 * e] = (float)(w[e] & 0xffffu);
+                        v[8 * k + 2 * e + 1] = (float)(w[e] >> 16);
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NV; ++j)
+                if (x0 + j >= L.W) v[j] = 0.f;
+            return;
+        }
     }
-    if (!L.weight_in) return val;
-    return val * cosine_weight(L, r, x);
+    if constexpr (NV % 4 == 0) {
+        if (L.vec && L.input_type == TK_INPUT_F32) {
+            const float4 *src = reinterpret_cast<const float4 *>(static_cast<const float *>(L.in) + off + x0);
+#pragma unroll
+            for (int k = 0; k < NV / 4; ++k) {
+                if (x0 + 4 * k < L.W) {
+                    const float4 q = __ldg(src + k);
+                    v[4 * k] = q.x;
+                    v[4 * k + 1] = q.y;
+                    v[4 * k + 2] = q.z;
+                    v[4 * k + 3] = q.w;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NV; ++j)
+                if (x0 + j >= L.W) v[j] = 0.f;
+            return;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NV; ++j)
+        if (x0 + j < L.W) v[j] = load_raw(L, off, x0 + j);
 }
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
@@ -344,8 +405,7 @@ __host__ __device__ __forceinline__ int fft_threads(int p)
 }
 
 // Shared-memory layout of the filter kernels: twiddle tables, the spectrum
-// Hf (p/2+1 floats), then per group two padded transform buffers and (for
-// coefficient output) the previous filtered row.
+// Hf (p/2+1 floats), then per group two padded transform buffers.
 struct FiltSmem {
     int tw_total, hf_floats, group_bytes, groups;
     __host__ __device__ size_t bytes() const
@@ -353,12 +413,12 @@ struct FiltSmem {
         return (size_t)tw_total * 8 + (size_t)hf_floats * 4 + (size_t)groups * group_bytes;
     }
 };
-__host__ __device__ inline FiltSmem filt_smem(int p, int tw_total, int W, bool coef)
+__host__ __device__ inline FiltSmem filt_smem(int p, int tw_total)
 {
     FiltSmem f;
     f.tw_total = tw_total;
     f.hf_floats = ((p / 2 + 1) + 3) & ~3;  // 16-byte multiple
-    f.group_bytes = 2 * padded_len(p) * 8 + (coef ? ((W + 3) & ~3) * 4 : 0);
+    f.group_bytes = 2 * padded_len(p) * 8;
     f.groups = kFiltThreads / fft_threads(p);
     return f;
 }
@@ -385,7 +445,7 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
     extern __shared__ __align__(16) float2 fsm[];
     constexpr int p = 1 << LG;
     const FFTPlan &pl = P.plan;
-    const FiltSmem lay = filt_smem(p, pl.tw_total, P.L.W, false);
+    const FiltSmem lay = filt_smem(p, pl.tw_total);
     constexpr int TPF = fft_threads_c(p);
     constexpr int G = kFiltThreads / TPF;
     const int grp = threadIdx.x / TPF, t = threadIdx.x - grp * TPF;
@@ -401,8 +461,11 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
     __syncthreads();
 
     // Raw samples of a pair group's two rows, fetched one group ahead so that
-    // their latency overlaps the transforms of the current one.
+    // their latency overlaps the transforms of the current one.  Thread t owns
+    // the run x0 = t NV .. x0 + NV - 1 of each row (NV TPF = p/2 >= W).
     constexpr int NV = (p / 2 + TPF - 1) / TPF;
+    static_assert(NV * TPF >= p / 2, "sample runs must cover the first half of the transform");
+    const int x0 = t * NV;
     float raw_a[NV], raw_b[NV];
     auto fetch = [&](long long pgf) {
         const long long pr = pgf * G + grp;
@@ -411,12 +474,8 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
         int rr;
         const long long oa = vl ? in_row_offset(P.L, 2 * pr, rr) : 0;
         const long long ob = hb ? in_row_offset(P.L, 2 * pr + 1, rr) : 0;
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            const int x = t + i * TPF;
-            raw_a[i] = (vl && x < W) ? load_raw(P.L, oa, x) : 0.f;
-            raw_b[i] = (hb && x < W) ? load_raw(P.L, ob, x) : 0.f;
-        }
+        load_run<NV>(P.L, oa, x0, vl, raw_a);
+        load_run<NV>(P.L, ob, x0, hb, raw_b);
     };
     if ((long long)blockIdx.x * G < P.npairs) fetch(blockIdx.x);
     for (long long pg = blockIdx.x; pg * G < P.npairs; pg += gridDim.x) {
@@ -428,14 +487,16 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
             int r_a = 0, r_b = 0;
             in_row_offset(P.L, ra, r_a);
             if (hasb) in_row_offset(P.L, rb, r_b);
+            const float rta = weight_row_term(P.L, r_a), rtb = weight_row_term(P.L, r_b);
 #pragma unroll
-            for (int i = 0; i < NV; ++i) {
-                const int x = t + i * TPF;
-                if (x < W)
-                    bufA[pidx(x)] = make_float2(pre_from_raw(P.L, r_a, x, raw_a[i]),
-                                                hasb ? pre_from_raw(P.L, r_b, x, raw_b[i]) : 0.f);
+            for (int j = 0; j < NV; ++j) {
+                const int x = x0 + j;
+                if (NV * TPF == p / 2 || x < p / 2)  // short transforms: runs past p/2 are the padding's
+                    bufA[pidx(x)] = x < W ? make_float2(pre_from_raw(P.L, r_a, x, raw_a[j], rta),
+                                                        hasb ? pre_from_raw(P.L, r_b, x, raw_b[j], rtb) : 0.f)
+                                          : make_float2(0.f, 0.f);
             }
-            for (int x = W + t; x < p; x += TPF) bufA[pidx(x)] = make_float2(0.f, 0.f);  // zero padding
+            for (int x = p / 2 + t; x < p; x += TPF) bufA[pidx(x)] = make_float2(0.f, 0.f);  // zero padding
         }
         if ((pg + gridDim.x) * G < P.npairs) fetch(pg + gridDim.x);
         __syncthreads();
@@ -453,14 +514,16 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
         if (valid) {
             int r_a, r_b;
             T *qa = out + out_row_offset(P, ra, r_a);
+            const float rta = weight_row_term(P.L, r_a);
             for (int i = t; i < W; i += TPF) {
-                const float w = P.weight_out ? cosine_weight(P.L, r_a, i) : 1.f;
+                const float w = P.weight_out ? cosine_weight_rt(P.L, rta, i) : 1.f;
                 qa[i] = store_cvt<T>(Q[pidx(i)].x * sigma * w);
             }
             if (hasb) {
                 T *qb = out + out_row_offset(P, rb, r_b);
+                const float rtb = weight_row_term(P.L, r_b);
                 for (int i = t; i < W; i += TPF) {
-                    const float w = P.weight_out ? cosine_weight(P.L, r_b, i) : 1.f;
+                    const float w = P.weight_out ? cosine_weight_rt(P.L, rtb, i) : 1.f;
                     qb[i] = store_cvt<T>(-Q[pidx(i)].y * sigma * w);
                 }
             }
@@ -475,62 +538,40 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
 // A work unit is RC consecutive detector rows of one projection.  The group
 // filters the unit's rows two at a time (plus the first row of the next unit,
 // which the last coefficient row needs) and keeps the previous filtered row in
-// shared memory, so every coefficient row r is formed from filtered rows r
-// and r+1 without another pass over HBM.  Samples outside the detector are 0.
+// registers (each thread holds it at the columns of its own entries), so
+// every coefficient row r is formed from filtered rows r and r+1 without
+// another pass over HBM.  Samples outside the detector are 0.
 
-template <int MODE> struct CoefStore;
-template <> struct CoefStore<TK_F32_COEF> {
-    static __device__ __forceinline__ void put(void *img, size_t idx, float Q, float dU, float dV, float dUV)
-    {
-        static_cast<float4 *>(img)[idx] = make_float4(Q, dU, dV, dUV);
-    }
-};
-template <> struct CoefStore<TK_F16> {
-    static __device__ __forceinline__ void put(void *img, size_t idx, float Q, float dU, float dV, float dUV)
-    {
-        const __half2 lo = __floats2half2_rn(Q, dV), hi = __floats2half2_rn(dU, dUV);
-        uint2 e;
-        e.x = *reinterpret_cast<const uint32_t *>(&lo);
-        e.y = *reinterpret_cast<const uint32_t *>(&hi);
-        static_cast<uint2 *>(img)[idx] = e;
-    }
-};
-template <> struct CoefStore<TK_BF16> {
-    static __device__ __forceinline__ void put(void *img, size_t idx, float Q, float dU, float dV, float dUV)
-    {
-        const __nv_bfloat162 lo = __floats2bfloat162_rn(Q, dV), hi = __floats2bfloat162_rn(dU, dUV);
-        uint2 e;
-        e.x = *reinterpret_cast<const uint32_t *>(&lo);
-        e.y = *reinterpret_cast<const uint32_t *>(&hi);
-        static_cast<uint2 *>(img)[idx] = e;
-    }
-};
-
-// Row accessors over the FFT result (row a = Re * s, row b = -Im * s) and
-// the kept previous row; index W reads as 0.
-struct RowRe {
-    const float2 *q; float s; int W;
-    __device__ __forceinline__ float operator()(int c) const { return c < W ? q[pidx(c)].x * s : 0.f; }
-};
-struct RowNegIm {
-    const float2 *q; float s; int W;
-    __device__ __forceinline__ float operator()(int c) const { return c < W ? -q[pidx(c)].y * s : 0.f; }
-};
-struct RowBuf {
-    const float *q; int W;
-    __device__ __forceinline__ float operator()(int c) const { return c < W ? q[c] : 0.f; }
-};
-struct RowZero {
-    __device__ __forceinline__ float operator()(int) const { return 0.f; }
-};
-
-template <int MODE, typename RA, typename RB>
-__device__ __forceinline__ void emit_coef_row(void *img, size_t row_base, int W, int t, int TPF, RA a, RB b)
+// Coefficient entries of columns c and c+1 of one row (c even, c < W) from
+// the row's filtered values a and the next row's b at c, c+1, c+2 (0 at
+// columns >= W).  The 16-bit formats store both entries with one 16-byte
+// store: their rows hold an even number of entries (Wc), so entry c+1 exists
+// and c starts a 16-byte unit; the FP32 format writes entry c+1 only below W.
+template <int MODE>
+__device__ __forceinline__ void emit_coef_pair(void *img, size_t row_base, int c, int W, const float *a,
+                                               const float *b)
 {
-    for (int c = t; c < W; c += TPF) {
-        const float a0 = a(c), a1 = a(c + 1), b0 = b(c), b1 = b(c + 1);
-        const float dU = a1 - a0;
-        CoefStore<MODE>::put(img, row_base + c, a0, dU, b0 - a0, (b1 - b0) - dU);
+    const float dU0 = a[1] - a[0], dU1 = a[2] - a[1];
+    const float Q0 = a[0], dV0 = b[0] - a[0], dUV0 = (b[1] - b[0]) - dU0;
+    const float Q1 = a[1], dV1 = b[1] - a[1], dUV1 = (b[2] - b[1]) - dU1;
+    if constexpr (MODE == TK_F32_COEF) {
+        float4 *e = static_cast<float4 *>(img) + row_base + c;
+        e[0] = make_float4(Q0, dU0, dV0, dUV0);
+        if (c + 1 < W) e[1] = make_float4(Q1, dU1, dV1, dUV1);
+    } else {
+        uint4 e;
+        if constexpr (MODE == TK_F16) {
+            const __half2 l0 = __floats2half2_rn(Q0, dV0), h0 = __floats2half2_rn(dU0, dUV0);
+            const __half2 l1 = __floats2half2_rn(Q1, dV1), h1 = __floats2half2_rn(dU1, dUV1);
+            e = make_uint4(*reinterpret_cast<const uint32_t *>(&l0), *reinterpret_cast<const uint32_t *>(&h0),
+                           *reinterpret_cast<const uint32_t *>(&l1), *reinterpret_cast<const uint32_t *>(&h1));
+        } else {
+            const __nv_bfloat162 l0 = __floats2bfloat162_rn(Q0, dV0), h0 = __floats2bfloat162_rn(dU0, dUV0);
+            const __nv_bfloat162 l1 = __floats2bfloat162_rn(Q1, dV1), h1 = __floats2bfloat162_rn(dU1, dUV1);
+            e = make_uint4(*reinterpret_cast<const uint32_t *>(&l0), *reinterpret_cast<const uint32_t *>(&h0),
+                           *reinterpret_cast<const uint32_t *>(&l1), *reinterpret_cast<const uint32_t *>(&h1));
+        }
+        *reinterpret_cast<uint4 *>(static_cast<uint2 *>(img) + row_base + c) = e;
     }
 }
 
@@ -540,7 +581,7 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
     extern __shared__ __align__(16) float2 fsm[];
     constexpr int p = 1 << LG;
     const FFTPlan &pl = P.plan;
-    const FiltSmem lay = filt_smem(p, pl.tw_total, P.L.W, true);
+    const FiltSmem lay = filt_smem(p, pl.tw_total);
     constexpr int TPF = fft_threads_c(p);
     constexpr int G = kFiltThreads / TPF;
     const int grp = threadIdx.x / TPF, t = threadIdx.x - grp * TPF;
@@ -548,7 +589,6 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
     float *hf = reinterpret_cast<float *>(fsm + lay.tw_total);
     float2 *bufA = reinterpret_cast<float2 *>(reinterpret_cast<char *>(hf + lay.hf_floats) + (size_t)grp * lay.group_bytes);
     float2 *bufB = bufA + padded_len(p);
-    float *prev = reinterpret_cast<float *>(bufB + padded_len(p));  // W floats
     fill_twiddles(twp, pl);
     for (int k = threadIdx.x; k <= p / 2; k += kFiltThreads) hf[k] = P.Hf[k];
     const float sigma = P.q_scale ? *P.q_scale : 1.f;
@@ -566,9 +606,12 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
         const int npair = valid ? (rend - r0 + 2) / 2 : 0;
         // every group runs the same number of pair steps (CTA-wide barriers inside)
         const int steps = (min(RC, H - 1) + 2) / 2;
-        // Raw samples x = t + i TPF (< W <= p/2) of the next step's two rows,
-        // fetched one step ahead so that their latency overlaps the transforms.
+        // Raw samples x0 .. x0 + NV - 1 (x0 = t NV; NV TPF = p/2 >= W) of the
+        // next step's two rows, fetched one step ahead so that their latency
+        // overlaps the transforms.
         constexpr int NV = (p / 2 + TPF - 1) / TPF;
+        static_assert(NV * TPF >= p / 2, "sample runs must cover the first half of the transform");
+        const int x0 = t * NV;
         float raw_a[NV], raw_b[NV];
         auto fetch = [&](int kk) {
             const bool lv = valid && kk < npair;
@@ -577,27 +620,32 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
             int rr;
             const long long oa = lv ? in_row_offset(P.L, b * H + qa, rr) : 0;
             const long long ob = hb ? in_row_offset(P.L, b * H + qb, rr) : 0;
-#pragma unroll
-            for (int i = 0; i < NV; ++i) {
-                const int x = t + i * TPF;
-                raw_a[i] = (lv && x < W) ? load_raw(P.L, oa, x) : 0.f;
-                raw_b[i] = (hb && x < W) ? load_raw(P.L, ob, x) : 0.f;
-            }
+            load_run<NV>(P.L, oa, x0, lv, raw_a);
+            load_run<NV>(P.L, ob, x0, hb, raw_b);
         };
+        // The previous filtered row (ra - 1) at the columns c, c+1, c+2 of
+        // this thread's column pairs c = 2 (i TPF + t): carried in registers
+        // from one step to the next.
+        constexpr int NPR = NV / 2 > 0 ? NV / 2 : 1;
+        float pv[NPR][3];
+#pragma unroll
+        for (int i = 0; i < NPR; ++i) pv[i][0] = pv[i][1] = pv[i][2] = 0.f;
         fetch(0);
         for (int k = 0; k < steps; ++k) {
             const bool live = valid && k < npair;
             const int ra = r0 + 2 * k, rb = ra + 1;
             const bool hasb = live && rb <= rend;
             if (live) {
+                const float rta = weight_row_term(P.L, ra), rtb = weight_row_term(P.L, rb);
 #pragma unroll
-                for (int i = 0; i < NV; ++i) {
-                    const int x = t + i * TPF;
-                    if (x < W)
-                        bufA[pidx(x)] = make_float2(pre_from_raw(P.L, ra, x, raw_a[i]),
-                                                    hasb ? pre_from_raw(P.L, rb, x, raw_b[i]) : 0.f);
+                for (int j = 0; j < NV; ++j) {
+                    const int x = x0 + j;
+                    if (NV * TPF == p / 2 || x < p / 2)  // short transforms: runs past p/2 are the padding's
+                        bufA[pidx(x)] = x < W ? make_float2(pre_from_raw(P.L, ra, x, raw_a[j], rta),
+                                                            hasb ? pre_from_raw(P.L, rb, x, raw_b[j], rtb) : 0.f)
+                                              : make_float2(0.f, 0.f);
                 }
-                for (int x = W + t; x < p; x += TPF) bufA[pidx(x)] = make_float2(0.f, 0.f);  // zero padding
+                for (int x = p / 2 + t; x < p; x += TPF) bufA[pidx(x)] = make_float2(0.f, 0.f);  // zero padding
             }
             if (k + 1 < steps) fetch(k + 1);
             __syncthreads();
@@ -613,23 +661,35 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
             const float2 *Q = fft_forward_c<LG>(R, Sb, twp, t);
             if (live) {
                 const size_t base = (size_t)b * H;
-                const RowRe rowa{Q, sigma, W};
-                const RowNegIm rowb{Q, sigma, W};
-                if (ra - 1 >= r0)  // prev = row ra-1, next = row ra
-                    emit_coef_row<MODE>(P.out, (base + ra - 1) * Wc, W, t, TPF, RowBuf{prev, W}, rowa);
-                if (ra < r1) {
-                    if (hasb)
-                        emit_coef_row<MODE>(P.out, (base + ra) * Wc, W, t, TPF, rowa, rowb);
-                    else  // row ra is the detector's last row
-                        emit_coef_row<MODE>(P.out, (base + ra) * Wc, W, t, TPF, rowa, RowZero{});
+                const float zero[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+                for (int i = 0; i < NPR; ++i) {
+                    const int c = 2 * (i * TPF + t);
+                    if (c < W) {
+                        // rows ra (Re) and rb (-Im) at c, c+1, c+2; columns >= W read as 0
+                        float a[3], bb[3];
+#pragma unroll
+                        for (int k3 = 0; k3 < 3; ++k3) {
+                            const float2 q = Q[pidx(c + k3)];
+                            const bool in = c + k3 < W;
+                            a[k3] = in ? q.x * sigma : 0.f;
+                            bb[k3] = in ? -q.y * sigma : 0.f;
+                        }
+                        if (ra - 1 >= r0)  // prev = row ra-1, next = row ra
+                            emit_coef_pair<MODE>(P.out, (base + ra - 1) * Wc, c, W, pv[i], a);
+                        if (ra < r1)  // next = row rb, or 0 below the detector's last row
+                            emit_coef_pair<MODE>(P.out, (base + ra) * Wc, c, W, a, hasb ? bb : zero);
+                        if (hasb && rb < r1 && rb == rend)  // detector's last row, nothing follows
+                            emit_coef_pair<MODE>(P.out, (base + rb) * Wc, c, W, bb, zero);
+                        if (hasb) {
+                            pv[i][0] = bb[0];
+                            pv[i][1] = bb[1];
+                            pv[i][2] = bb[2];
+                        }
+                    }
                 }
-                if (hasb && rb < r1 && rb == rend)  // detector's last row, nothing follows
-                    emit_coef_row<MODE>(P.out, (base + rb) * Wc, W, t, TPF, rowb, RowZero{});
             }
-            __syncthreads();
-            if (live && hasb)
-                for (int c = t; c < W; c += TPF) prev[c] = -Q[pidx(c)].y * sigma;
-            __syncthreads();
+            __syncthreads();  // the buffers are rewritten by the next step
         }
     }
 }
@@ -758,6 +818,19 @@ template <int LG> static const void *filter_kernel_lg(int precision)
     return nullptr;
 }
 
+// Derived load parameters: D^2, the scalar flat-field reciprocal, and whether
+// rows can be read in 16-byte chunks (aligned base, row pitch a multiple of
+// 16 bytes, so every chunk that starts below W lies inside its row).
+static void finish_load_params(LoadParams &L)
+{
+    L.D2 = L.D * L.D;
+    L.inv_den = 1.f;
+    if (L.input_type == TK_INPUT_U16 && !L.dark && !L.flat)
+        L.inv_den = 1.f / std::fmax(L.flat_v - L.dark_v, L.floor_counts);
+    const int es = L.input_type == TK_INPUT_U16 ? 2 : 4;
+    L.vec = (reinterpret_cast<uintptr_t>(L.in) % 16 == 0) && ((long long)L.in_pitch * es) % 16 == 0;
+}
+
 static const void *filter_kernel_fn(int precision, int lg)
 {
     switch (lg) {
@@ -782,7 +855,7 @@ static int launch_filter_typed(const FiltParams &P, int p, cudaStream_t stream, 
     const void *fn = filter_kernel_fn(precision, P.lg);
     TK_CHECK(fn, TK_ERR_UNSUPPORTED, "filter: no kernel for pad length %d with this storage", p);
     const int G = kFiltThreads / fft_threads(p);
-    const size_t smem = filt_smem(p, P.plan.tw_total, P.L.W, is_coef(precision)).bytes();
+    const size_t smem = filt_smem(p, P.plan.tw_total).bytes();
     TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "filter: pad length %d needs too much shared memory", p);
     TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, sms = 0, per_sm = 0;
@@ -844,6 +917,7 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
         L.invert = ff->invert ? 1 : 0;
         L.floor_counts = ff->floor_counts;
     }
+    finish_load_params(L);
     const Spectrum &sp = spectrum(g.W, g.tau, window, p);
     P.out = d_q;
     P.out_layout = TK_LAYOUT_PROJECTION;
@@ -922,6 +996,7 @@ int launch_filter_transpose(const tk_geometry &g, const float *d_qbar, int windo
     L.cZ = g.cZ;
     L.D = g.D;
     L.A = 1.f;
+    finish_load_params(L);
     const Spectrum &sp = spectrum(g.W, g.tau, window, p);
     P.out = d_pbar;
     P.out_layout = layout;
