@@ -430,7 +430,7 @@ def run_ours(args):
     _lib.check(L.tk_measure_fp32_fma_rate(ctypes.byref(fma_peak)))
     fp32_peak = fma_peak.value
     traffic = None  # DRAM bytes per backprojection launch, from the committed ncu summary
-    tf = os.path.join(ROOT, "profiles", "bp_cimg_x2_f16_1024cube_dram.md")
+    tf = os.path.join(ROOT, "profiles", "bp_cimg_h2_f16_1024cube_dram.md")
     try:
         for line in open(tf):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -447,7 +447,7 @@ def run_ours(args):
     out = {
         "metric": "GUPS", "value": value, "unit": "GUPS", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms16, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 math, f16-stored filtered projections", "data": "synthetic: seeded 40-ellipsoid phantom, "
+        "dtype": "f16-stored filtered projections, f16 row interpolation, f32 geometry and accumulation", "data": "synthetic: seeded 40-ellipsoid phantom, "
         "Poisson counts I0=60000 (no dataset)", "config": CONFIG,
         "s_per_volume": ms16 * 1e-3,
         "plain": {"value": plain, "unit": "GUPS", "ms_per_step": ms32, "s_per_volume": ms32 * 1e-3,
@@ -760,7 +760,7 @@ def run_batch(args):
           "speedup_graph_vs_per_volume": ms_single / ms_graph, "autotuned_variant": tuned,
           "autotune_ms": tune_ms, "max_rel_diff_vs_per_volume_mid_slices": diff, "flags": flags,
           "detector_widths": sorted({g.W for g in geos}),
-          "data": "synthetic: 64 seeded 20-ellipsoid phantoms, analytic FP32 line integrals (no dataset)"})
+          "data": f"synthetic: {len(geos)} seeded 20-ellipsoid phantoms, analytic FP32 line integrals (no dataset)"})
     b.close()
     return 0
 
