@@ -591,6 +591,22 @@ def run_adjoint(args):
         device.fdk_backward(g, y, workspace=ws, out=grad)
 
     res = {}
+    L = _lib.load()
+    try:  # the column-lane forward projector, timed beside the default
+        _lib.check(L.tk_fp_select_variant(1))
+        for _ in range(args.warmup):
+            bwd()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            bwd()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res["backward_column_lanes"] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
+    finally:
+        _lib.check(L.tk_fp_select_variant(0))
     for name, fn in (("forward", fwd), ("backward", bwd)):
         for _ in range(args.warmup):
             fn()

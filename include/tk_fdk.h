@@ -229,6 +229,11 @@ int tk_bp_variant_count(void);
 const char *tk_bp_variant_name(int i);
 int tk_bp_variant_precision(int i);
 int tk_bp_select_variant(int i);
+/* Forward projector (the scatter of tk_forward_project / tk_fdk_backward):
+ * 0 (default) lanes on 32 consecutive slices of one voxel column, the warp
+ * walking its columns; 1 lanes on 32 voxel columns, each walking its slices.
+ * Same weights and masks; the sums differ by FP32 rounding order only. */
+int tk_fp_select_variant(int i);
 
 /* Analytic cone-beam line integrals of ellipsoids (seeded synthetic input).
  * ell: host array of nell records of 16 doubles: centre[3] (cm), semi-axes[3]

@@ -49,6 +49,27 @@ def test_forward_project_is_transpose_of_backproject(cuda, name):
     assert device.device_error_flags() == 0
 
 
+@pytest.mark.parametrize("name", list(GEOMS))
+def test_forward_projector_forms_agree(cuda, name):
+    """Slice lanes (default) and column lanes scatter the same weights: the
+    projections agree to FP32 rounding of the summation order, including a
+    partial z chunk (Z not a multiple of 32)."""
+    import torch
+
+    L = _lib.load()
+    g = small_geometry(**GEOMS[name])
+    y = np.random.default_rng(4).normal(size=(g.Z, g.Y, g.X)).astype(np.float32)
+    out = []
+    try:
+        for v in (0, 1):
+            _lib.check(L.tk_fp_select_variant(v))
+            out.append(device.forward_project(g, dev(y, torch)).cpu().numpy()[:, :, :g.W])
+    finally:
+        _lib.check(L.tk_fp_select_variant(0))
+    assert rel_rmse(out[0], out[1]) < 1e-6
+    assert device.device_error_flags() == 0
+
+
 @pytest.mark.parametrize("window", ["ramlak", "hann"])
 @pytest.mark.parametrize("layout", ["sinogram", "projection"])
 def test_fdk_dot_product(cuda, window, layout):

@@ -28,7 +28,7 @@ EXPORTS = [
     "tk_filtered_bytes", "tk_fdk_workspace_bytes", "tk_fdk_device", "tk_fdk_device_noalloc",
     "tk_fdk_stream_workspace_bytes", "tk_fdk_stream",
     "tk_forward_project", "tk_filter_transpose", "tk_fdk_forward", "tk_fdk_backward", "tk_phantom_project", "tk_bp_variant_count",
-    "tk_bp_variant_name", "tk_bp_variant_precision", "tk_bp_select_variant", "tk_fdk_create", "tk_fdk_destroy",
+    "tk_bp_variant_name", "tk_bp_variant_precision", "tk_bp_select_variant", "tk_fp_select_variant", "tk_fdk_create", "tk_fdk_destroy",
     "tk_fdk_set_gpu_id", "tk_fdk_set_block_size", "tk_fdk_set_allocation_limit", "tk_fdk_set_collecting",
     "tk_fdk_set_show_info", "tk_fdk_set_axis_direction", "tk_fdk_set_sinogram_properties",
     "tk_fdk_set_reconstruction_properties", "tk_fdk_set_scale_xyz", "tk_fdk_set_projections_u16",
@@ -125,6 +125,7 @@ def _declare(L):
     L.tk_bp_variant_name.restype = ctypes.c_char_p
     L.tk_bp_variant_precision.argtypes = [ip]
     L.tk_bp_select_variant.argtypes = [ip]
+    L.tk_fp_select_variant.argtypes = [ip]
     L.tk_batch_create.argtypes = [ctypes.POINTER(vp)]
     L.tk_batch_destroy.argtypes = [vp]
     L.tk_batch_destroy.restype = None

@@ -604,6 +604,133 @@ __global__ void __launch_bounds__(TX *TY, 2)
 }
 
 // ---------------------------------------------------------------------------
+// Forward projector with slice lanes (the default form; same weights, masks,
+// box and drain as fp_scatter_kernel).  Lane l of warp w holds slice z0 + l
+// of the warp's 32 voxel columns (tile rows 2w and 2w+1), and the warp walks
+// its columns one by one.  The lanes of one shared atomic then sit on the
+// rows of 32 consecutive slices of one column: distinct rows whenever the
+// row step |scale| U is at least one, and with the odd row pitch (BW + 1)
+// distinct banks for rows less than 32 apart.  The column geometry of a
+// projection is computed once per column (lane j for column j) into a
+// per-warp table in shared memory and read back as a broadcast.
+template <int TX, int TY, bool PARTIAL>
+__global__ void __launch_bounds__(TX *TY, 2)
+    fp_scatter_col_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P,
+                          const float *__restrict__ vin)
+{
+    constexpr int NT = TX * TY, NW = NT / 32, TZ = 32;
+    static_assert(TX == 16 && NT == 256, "a warp owns two tile rows of 16 columns");
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int BW = P.BW, BWp = P.BW + 1, BH = P.BH;
+    float *staging = reinterpret_cast<float *>(smem);  // 2 x [BH][BW]
+    float *acc = staging + 2 * (size_t)P.stage_elems;   // [BH][BW + 1]
+    const int acc_elems = (BH * BWp + 31) & ~31;
+    float4 *geo = reinterpret_cast<float4 *>(acc + acc_elems);  // [NW][32] (U, fu, col, U^2)
+    int2 *boxo = reinterpret_cast<int2 *>(geo + NW * 32);
+
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int2 tile = tile_of(blockIdx.x, P.tilesX, P.tilesY);
+    const int x0 = tile.x * TX, y0 = tile.y * TY;
+    const int zc = blockIdx.y * TZ;
+    const int z0 = PARTIAL ? zc : min(zc, P.nz - TZ);
+    const int zlast = PARTIAL ? P.nz - 1 - z0 : TZ - 1;
+    // column `lane` of this warp, for the geometry of each projection
+    const int gx = x0 + (lane & 15), gy = y0 + 2 * w + (lane >> 4);
+    const float gaX = flip(P.scale * ((float)gx + P.dX), P.dirx);
+    const float gaY = flip(P.scale * ((float)gy + P.dY), P.diry);
+    const bool gactive = (gx < P.X) && (gy < P.Y) && (sqrtf(gaX * gaX + gaY * gaY) < P.halfW);
+    if (!__syncthreads_or(gactive)) return;  // nothing in this tile projects
+
+    for (int b = tid; b < P.N; b += NT) {
+        int2 o = footprint_origin_z<TX, TY, 4>(P, b, x0, y0, z0, z0 + zlast);
+        o.x = max(o.x, 0);  // still a multiple of 4
+        o.y = max(o.y, 0);
+        boxo[b] = o;
+    }
+    for (int i = tid; i < BH * BWp; i += NT) acc[i] = 0.f;
+    // this lane's slice of the warp's 32 columns (0 for slices owned by another chunk or past the end)
+    const unsigned act = __ballot_sync(0xffffffffu, gactive);
+    const bool zown = lane <= zlast && z0 + lane >= zc;
+    float g[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int x = x0 + (j & 15), y = y0 + 2 * w + (j >> 4);
+        g[j] = 0.f;
+        if (((act >> j) & 1u) && zown)
+            g[j] = P.fscale * vin[(size_t)(z0 + lane) * P.slice_stride + (size_t)y * P.X + x];
+    }
+    const float aZ = flip(P.scale * ((float)min(z0 + lane, P.nz - 1) + P.zoff), P.dirz);
+    const float aZf = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
+    const float aZl = flip(P.scale * ((float)(z0 + zlast) + P.zoff), P.dirz);
+    const float cZ = P.cZ, Hm1 = P.Hm1;
+    float4 *gw = geo + w * 32;
+    __syncthreads();
+
+    for (int b = 0; b < P.N; ++b) {
+        const int bx0 = boxo[b].x, by0 = boxo[b].y;
+        {
+            float4 e = make_float4(0.f, 0.f, __int_as_float(-1), 0.f);  // col -1: nothing to scatter
+            if (gactive) {
+                float U, u;
+                column_geometry(gaX, gaY, P.trig[b], P.D, P.cX, U, u);
+                if (u >= 0.f && u <= P.Wm1) {
+                    const float fla = __fadd_rd(u, kMagic);
+                    const int col = __float_as_int(fla) - kMagicBits - bx0;
+                    const float fu = u - (fla - kMagic);
+                    const float v0 = slice_v(aZf, U, cZ), vL = slice_v(aZl, U, cZ);
+                    const float vlo = fmaxf(fminf(v0, vL), 0.f), vhi = fminf(fmaxf(v0, vL), Hm1);
+                    if (vlo <= vhi) {
+                        const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) + 1 - by0;
+                        if (col >= 0 && col + 1 < BW && rlo >= 0 && rhi < BH)
+                            e = make_float4(U, fu, __int_as_float(col), __fmul_rn(U, U));
+                        else
+                            atomicOr(P.err, ERR_BOX_OVERFLOW);
+                    }
+                }
+            }
+            gw[lane] = e;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const float4 e = gw[j];  // the same entry for every lane
+            const int col = __float_as_int(e.z);
+            if (col >= 0) {
+                const float v = slice_v(aZ, e.x, cZ);
+                if (g[j] != 0.f && v >= 0.f && v <= Hm1) {
+                    const float fl = __fadd_rd(v, kMagic);
+                    const float fv = v - (fl - kMagic);
+                    const int row = __float_as_int(fl) - kMagicBits - by0;
+                    const float wt = e.w * g[j];
+                    const float w1 = wt * e.y, w0 = wt - w1;  // columns col, col+1
+                    float *r0 = acc + row * BWp + col;
+                    atomicAdd(r0, w0 - w0 * fv);
+                    atomicAdd(r0 + 1, w1 - w1 * fv);
+                    atomicAdd(r0 + BWp, w0 * fv);
+                    atomicAdd(r0 + BWp + 1, w1 * fv);
+                }
+            }
+        }
+        float *st = staging + (size_t)(b & 1) * P.stage_elems;
+        if (tid == 0 && b >= 2) bulk_wait_group_read<1>();  // the reduce of b-2 has read this staging box
+        __syncthreads();  // also: every warp is done with its geometry table
+        for (int i = tid; i < BH * BW; i += NT) {
+            const int r = i / BW, c = i - r * BW;
+            float *a = acc + r * BWp + c;
+            st[i] = *a;
+            *a = 0.f;
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            if (bx0 < (int)P.Wm1 + 1 && by0 < (int)P.Hm1 + 1) tma_reduce_add_3d(&tmap, bx0, by0, b, st);
+            bulk_commit_group();  // one group per projection, empty when the box misses the detector
+        }
+    }
+    if (tid == 0) bulk_wait_group_all();
+}
+
+// ---------------------------------------------------------------------------
 // host side
 
 static PFN_cuTensorMapEncodeTiled_v12000 get_encode_fn()
@@ -670,6 +797,7 @@ static const BPVariant kVariants[] = {
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
+static int g_fp_variant = 0;  // forward projector: 0 slice lanes (fp_scatter_col_kernel), 1 column lanes
 
 static const BPVariant *pick_variant(int precision)
 {
@@ -837,8 +965,11 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     TK_CHECK((long long)tilesX * tilesY < (1ll << 31) && zchunks < 65536, TK_ERR_UNSUPPORTED,
              "volume too large for one launch");
     const bool partial = nz < TZ;
-    const void *fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
-                             : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>);
+    const bool cols = g_fp_variant == 0;
+    const void *fn = cols ? (partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true>)
+                                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false>))
+                          : (partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
+                                     : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>));
 
     static thread_local BPParams P;
     std::memset(&P, 0, sizeof(P));
@@ -883,7 +1014,9 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
         const size_t acc_elems = (size_t)((BH * (BW + 1) + 31) & ~31);  // odd-pitch accumulation box
-        const size_t smem = (2 * (size_t)P.stage_elems + acc_elems) * sizeof(float) + (size_t)nb * sizeof(int2) + 16;
+        const size_t geo_bytes = cols ? (size_t)(TX * TY / 32) * 32 * sizeof(float4) : 0;  // slice-lane form
+        const size_t smem = (2 * (size_t)P.stage_elems + acc_elems) * sizeof(float) + geo_bytes +
+                            (size_t)nb * sizeof(int2) + 16;
         TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "forward project: %zu B of shared memory needed", smem);
         TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         dim3 grid((unsigned)(tilesX * tilesY), partial ? 1u : (unsigned)zchunks, 1);
@@ -912,6 +1045,16 @@ extern "C" int tk_bp_variant_precision(int i)
 {
     if (i < 0 || i >= tk_bp_variant_count()) return -1;
     return tk::kVariants[i].precision;
+}
+
+extern "C" int tk_fp_select_variant(int i)
+{
+    if (i < 0 || i > 1) {
+        tk::set_error("no forward-projector variant %d", i);
+        return TK_ERR_INVALID;
+    }
+    tk::g_fp_variant = i;
+    return TK_OK;
 }
 
 extern "C" int tk_bp_select_variant(int i)
