@@ -231,12 +231,9 @@ int tk_bp_variant_precision(int i);
 int tk_bp_select_variant(int i);
 /* Forward projector (the scatter of tk_forward_project / tk_fdk_backward):
  * 0 (default) lanes on 32 consecutive slices of one voxel column, the warp
- * walking its columns, summing each projection's tile box in 32-bit fixed
- * point (native integer shared atomics; per-tile power-of-two scale,
- * resolution 2^-19 or finer of the tile's largest contribution) where the
- * row step bounds the contributions per cell, else in FP32; 1 lanes on 32
- * voxel columns, each walking its slices, FP32 shared atomics; 2 as 0 with
- * FP32 shared atomics.  Same weights and masks. */
+ * walking its columns; 1 lanes on 32 voxel columns, each walking its slices.
+ * Same weights and masks (FP32 shared atomics); the sums differ by FP32
+ * rounding order only. */
 int tk_fp_select_variant(int i);
 
 /* Analytic cone-beam line integrals of ellipsoids (seeded synthetic input).

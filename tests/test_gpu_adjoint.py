@@ -51,25 +51,22 @@ def test_forward_project_is_transpose_of_backproject(cuda, name):
 
 @pytest.mark.parametrize("name", list(GEOMS))
 def test_forward_projector_forms_agree(cuda, name):
-    """The three forward-projector forms scatter the same weights, including a
-    partial z chunk (Z not a multiple of 32): slice lanes with FP32 atomics
-    (2) and column lanes (1) agree to FP32 rounding of the summation order;
-    the fixed-point box of the default (0) to its resolution (2^-19 or finer
-    of each tile's largest contribution, here below 3e-6 relative RMSE)."""
+    """Slice lanes (default) and column lanes scatter the same weights: the
+    projections agree to FP32 rounding of the summation order, including a
+    partial z chunk (Z not a multiple of 32)."""
     import torch
 
     L = _lib.load()
     g = small_geometry(**GEOMS[name])
     y = np.random.default_rng(4).normal(size=(g.Z, g.Y, g.X)).astype(np.float32)
-    out = {}
+    out = []
     try:
-        for v in (0, 1, 2):
+        for v in (0, 1):
             _lib.check(L.tk_fp_select_variant(v))
-            out[v] = device.forward_project(g, dev(y, torch)).cpu().numpy()[:, :, :g.W]
+            out.append(device.forward_project(g, dev(y, torch)).cpu().numpy()[:, :, :g.W])
     finally:
         _lib.check(L.tk_fp_select_variant(0))
-    assert rel_rmse(out[2], out[1]) < 1e-6
-    assert rel_rmse(out[0], out[1]) < 3e-6
+    assert rel_rmse(out[0], out[1]) < 1e-6
     assert device.device_error_flags() == 0
 
 

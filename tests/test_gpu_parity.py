@@ -478,20 +478,35 @@ def _handle_run(g, data, layout, prec, pipeline, zb, counts=None, after_init=Non
     return out, launches
 
 
+def pipelined_launches(g, nblk, last_slices):
+    """Launches of a pipelined Initialize (tk_fdk_initialize): chunks of
+    max(32, ceil(N/8)) angles, each a storage-scale and a filter launch; the
+    chunks ending by the first half of the angles backprojected block by
+    block; one launch per block over the rest, the last block in two when it
+    holds at least 128 slices."""
+    chunk = max(32, -(-g.N // 8))
+    nch = -(-g.N // chunk)
+    major_end = min(g.N - chunk, chunk * ((nch + 1) // 2))
+    major = sum(1 for b0 in range(0, g.N, chunk) if b0 + min(chunk, g.N - b0) <= major_end)
+    split = 1 if (last_slices // 2) // 64 * 64 > 0 else 0
+    return 2 * nch + major * nblk + nblk + split
+
+
 @pytest.mark.parametrize("vol_shape,zb,prec,raw,layout", [
     ((40, 40, 40), 16, "f32", False, "projection"),   # blocks 16, 16, 8
     ((40, 40, 33), 16, "f16", True, "projection"),    # last-slice quirk
     ((36, 40, 30), 64, "f32c", False, "projection"),  # one block, zb > Z
+    ((40, 40, 128), 128, "f16", True, "projection"),  # the last block's launch split at 64 slices
     ((40, 40, 40), 16, "f16", True, "sinogram"),      # [H][N][W], packed per chunk by strided copies
     ((40, 40, 33), 16, "f32", False, "sinogram")])
 def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, layout):
-    """tk_fdk_set_pipeline: Initialize uploads N = 300 projections in four
-    75-angle chunks, filters each as it lands, backprojects the first chunk
-    into the whole volume with the Z-block schedule, then each block over the
-    other 225 angles; CalculateReconstruction only delivers blocks.  The
-    volume equals the regular path's to FP32 rounding of the two-part sums,
-    with the same blocks requested, the same last-slice quirk, and
-    4 x (storage scale + filter) + 2 x (one backprojection per block) launches."""
+    """tk_fdk_set_pipeline: Initialize uploads N = 300 projections in 38-angle
+    chunks, filters each as it lands, backprojects the chunks of the first
+    152 angles into the whole volume with the Z-block schedule as they land,
+    then each block over the other 148 angles; CalculateReconstruction only
+    delivers blocks.  The volume equals the regular path's to FP32 rounding of
+    the partial sums, with the same blocks requested, the same last-slice
+    quirk, and the launches of that schedule."""
     g = small_geometry(W=48, N=300, H=48, vol=vol_shape, zb=zb)
     G = orc.geom_from(g)
     proj = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=5), G, "proj")  # [N][H][W]
@@ -502,7 +517,8 @@ def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, la
     reg, _ = _handle_run(g, data, layout, prec, False, zb, counts)
     pip, launches = _handle_run(g, data, layout, prec, True, zb, counts)
     nblk = len(orc.zblocks(G))
-    assert launches == 4 * 2 + 2 * nblk
+    last = g.Z - (nblk - 1) * zb if nblk * zb > g.Z else zb
+    assert launches == pipelined_launches(g, nblk, last)
     assert pip.blocks_requested == reg.blocks_requested
     assert rel_rmse(pip.volume, reg.volume) < 1e-6
     assert max_abs(pip.volume, reg.volume) < 1e-5 * np.abs(reg.volume).max()
@@ -525,7 +541,7 @@ def test_setter_after_pipelined_initialize(orc, cuda):
     changed, launches = _handle_run(g, sino, "sinogram", "f32", True, 16, after_init=hann)
     fresh, _ = _handle_run(g, sino, "sinogram", "f32", False, 16, window="hann")
     nblk = len(orc.zblocks(G))
-    assert launches == 4 * 2 + 2 * nblk + 2 + nblk  # the pipelined pass, then one regular pass
+    assert launches == pipelined_launches(g, nblk, 16) + 2 + nblk  # the pipelined pass, then a regular one
     # the fresh run filters in even 64-angle chunks, which pair FFT rows as one pass does
     assert rel_rmse(changed.volume, fresh.volume) < 1e-7
     assert max_abs(changed.volume, fresh.volume) <= 1e-6 * np.abs(fresh.volume).max()

@@ -613,19 +613,10 @@ __global__ void __launch_bounds__(TX *TY, 2)
 // distinct banks for rows less than 32 apart.  The column geometry of a
 // projection is computed once per column (lane j for column j) into a
 // per-warp table in shared memory and read back as a broadcast.
-//
-// FIXED: the box accumulates integers (shared-memory FP32 atomic add is a
-// load / compare-and-swap loop; integer add is one native atomic).  Each CTA
-// scales its contributions x by s = 2^e, rounded to nearest with one FMA
-// against 1.5 * 2^23, where e makes the tile's largest possible contribution
-// max|g| * u2max fit 2^min(30 - cbits, 22): with at most 2^cbits
-// contributions to one cell of one projection (cbits from the row step, on
-// the host), no cell sum can overflow, and the resolution is 2^-(22..19) of
-// the largest contribution.  The drain converts the sums back (times 1/s).
-template <int TX, int TY, bool PARTIAL, bool FIXED>
+template <int TX, int TY, bool PARTIAL>
 __global__ void __launch_bounds__(TX *TY, 2)
     fp_scatter_col_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P,
-                          const float *__restrict__ vin, float u2max, int cbits)
+                          const float *__restrict__ vin)
 {
     constexpr int NT = TX * TY, NW = NT / 32, TZ = 32;
     static_assert(TX == 16 && NT == 256, "a warp owns two tile rows of 16 columns");
@@ -673,30 +664,7 @@ __global__ void __launch_bounds__(TX *TY, 2)
     const float aZl = flip(P.scale * ((float)(z0 + zlast) + P.zoff), P.dirz);
     const float cZ = P.cZ, Hm1 = P.Hm1;
     float4 *gw = geo + w * 32;
-    __shared__ float s_gmax[NW];
-    if constexpr (FIXED) {
-        float m = 0.f;
-#pragma unroll
-        for (int j = 0; j < 32; ++j) m = fmaxf(m, fabsf(g[j]));
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) s_gmax[w] = m;
-    }
     __syncthreads();
-    float fx_s = 0.f, fx_inv = 0.f;  // FIXED: x -> round(x fx_s); sums back by fx_inv
-    if constexpr (FIXED) {
-        float m = 0.f;
-#pragma unroll
-        for (int k = 0; k < NW; ++k) m = fmaxf(m, s_gmax[k]);
-        const float cmax = m * u2max;
-        if (cmax > 0.f) {
-            int ex;
-            frexpf(cmax, &ex);  // cmax < 2^ex
-            const int e = max(-126, min(126, min(30 - cbits, 22) - ex));
-            fx_s = ldexpf(1.f, e);
-            fx_inv = ldexpf(1.f, -e);
-        }
-    }
-    int *acci = reinterpret_cast<int *>(acc);
 
     for (int b = 0; b < P.N; ++b) {
         const int bx0 = boxo[b].x, by0 = boxo[b].y;
@@ -735,19 +703,11 @@ __global__ void __launch_bounds__(TX *TY, 2)
                     const int row = __float_as_int(fl) - kMagicBits - by0;
                     const float wt = e.w * g[j];
                     const float w1 = wt * e.y, w0 = wt - w1;  // columns col, col+1
-                    const int o = row * BWp + col;
-                    if constexpr (FIXED) {
-                        atomicAdd(acci + o, __float_as_int(fmaf(w0 - w0 * fv, fx_s, kMagic)) - kMagicBits);
-                        atomicAdd(acci + o + 1, __float_as_int(fmaf(w1 - w1 * fv, fx_s, kMagic)) - kMagicBits);
-                        atomicAdd(acci + o + BWp, __float_as_int(fmaf(w0 * fv, fx_s, kMagic)) - kMagicBits);
-                        atomicAdd(acci + o + BWp + 1, __float_as_int(fmaf(w1 * fv, fx_s, kMagic)) - kMagicBits);
-                    } else {
-                        float *r0 = acc + o;
-                        atomicAdd(r0, w0 - w0 * fv);
-                        atomicAdd(r0 + 1, w1 - w1 * fv);
-                        atomicAdd(r0 + BWp, w0 * fv);
-                        atomicAdd(r0 + BWp + 1, w1 * fv);
-                    }
+                    float *r0 = acc + row * BWp + col;
+                    atomicAdd(r0, w0 - w0 * fv);
+                    atomicAdd(r0 + 1, w1 - w1 * fv);
+                    atomicAdd(r0 + BWp, w0 * fv);
+                    atomicAdd(r0 + BWp + 1, w1 * fv);
                 }
             }
         }
@@ -756,14 +716,9 @@ __global__ void __launch_bounds__(TX *TY, 2)
         __syncthreads();  // also: every warp is done with its geometry table
         for (int i = tid; i < BH * BW; i += NT) {
             const int r = i / BW, c = i - r * BW;
-            const int k = r * BWp + c;
-            if constexpr (FIXED) {
-                st[i] = (float)acci[k] * fx_inv;
-                acci[k] = 0;
-            } else {
-                st[i] = acc[k];
-                acc[k] = 0.f;
-            }
+            float *a = acc + r * BWp + c;
+            st[i] = *a;
+            *a = 0.f;
         }
         fence_proxy_async_smem();
         __syncthreads();
@@ -848,8 +803,7 @@ static const BPVariant kVariants[] = {
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
-static int g_fp_variant = 0;  // forward projector: 0 slice lanes (fixed point where bounded), 1 column lanes,
-                              // 2 slice lanes with FP32 atomics
+static int g_fp_variant = 0;  // forward projector: 0 slice lanes (fp_scatter_col_kernel), 1 column lanes
 
 static const BPVariant *pick_variant(int precision)
 {
@@ -1017,35 +971,12 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     TK_CHECK((long long)tilesX * tilesY < (1ll << 31) && zchunks < 65536, TK_ERR_UNSUPPORTED,
              "volume too large for one launch");
     const bool partial = nz < TZ;
-    // Slice lanes (variants 0 and 2) or column lanes (1).  Variant 0 accumulates in fixed point when
-    // at most 2^12 contributions can reach one cell of one projection from one tile:
-    //  - the columns whose u falls in a 2-pixel band lie between two rays from the source, a strip
-    //    at most w = 2 / (U_min |scale|) voxels wide; a 16 x 16 grid holds at most
-    //    16 (floor(sqrt(2) w) + 1) points of such a strip (per grid line, floor(w / max(|cos|,
-    //    |sin|)) + 1 points), and at most 256;
-    //  - per column, the slices whose row falls in a 2-row band, at most floor(2 / dv_min) + 2,
-    //    dv_min = |scale| U_min the smallest row step;
-    //  with U_min = D / (D + W/2) over the FOV.
-    const bool cols = g_fp_variant != 1;
-    const double hw = 0.5 * g.W, umin = g.D / (g.D + hw);
-    const double dv_min = std::max(std::fabs((double)g.scale) * umin, 1e-6);
-    const double ncols = std::min(256.0, 16.0 * (std::floor(std::sqrt(2.0) * 2.0 / dv_min) + 1.0));
-    const double count = ncols * (std::floor(2.0 / dv_min) + 2.0);
-    int cbits = 0;
-    while ((double)(1 << cbits) < count && cbits < 30) ++cbits;
-    const bool fixed = g_fp_variant == 0 && cbits <= 12;
-    // |S| < W/2 for every voxel column inside the FOV, so U < D / (D - W/2)
-    const float u2max = (float)(1.0001 * (g.D / (g.D - hw)) * (g.D / (g.D - hw)));
-    const void *fn;
-    if (!cols)
-        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
-                     : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>);
-    else if (fixed)
-        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, true>)
-                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, true>);
-    else
-        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, false>)
-                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, false>);
+    // slice lanes (variant 0, the default) or column lanes (1)
+    const bool cols = g_fp_variant == 0;
+    const void *fn = cols ? (partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true>)
+                                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false>))
+                          : (partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
+                                     : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>));
 
     static thread_local BPParams P;
     std::memset(&P, 0, sizeof(P));
@@ -1097,11 +1028,8 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
         TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         dim3 grid((unsigned)(tilesX * tilesY), partial ? 1u : (unsigned)zchunks, 1);
         const float *vin = d_vol;
-        float u2 = u2max;
-        int cb = cbits;
-        void *args_cols[] = {&tmap, &P, &vin, &u2, &cb};
-        void *args_rows[] = {&tmap, &P, &vin};
-        TK_CUDA(cudaLaunchKernel(fn, grid, dim3(TX * TY), cols ? args_cols : args_rows, smem, stream));
+        void *args[] = {&tmap, &P, &vin};
+        TK_CUDA(cudaLaunchKernel(fn, grid, dim3(TX * TY), args, smem, stream));
         count_launch();
     }
     return TK_OK;
@@ -1128,7 +1056,7 @@ extern "C" int tk_bp_variant_precision(int i)
 
 extern "C" int tk_fp_select_variant(int i)
 {
-    if (i < 0 || i > 2) {
+    if (i < 0 || i > 1) {
         tk::set_error("no forward-projector variant %d", i);
         return TK_ERR_INVALID;
     }

@@ -368,6 +368,8 @@ struct tk_fdk {
     std::vector<cudaEvent_t> ev_blocks;  // last backprojection of each Z block
     bool reconstructed = false;
     int pipe_zb = 0;   // Z-block size the pipelined volume was built with
+    int pipe_split = 0;      // > 0: the last block's first pipe_split slices complete at ev_last_half
+    cudaEvent_t ev_last_half = nullptr;
     int in_chunk = 0;  // > 0: sinogram-major input stored as [H][nb][W] blocks of in_chunk angles
 };
 
@@ -388,6 +390,8 @@ static void release_device(tk_fdk *h)
     h->vol_cap = 0;
     for (cudaEvent_t e : h->ev_blocks) cudaEventDestroy(e);
     h->ev_blocks.clear();
+    if (h->ev_last_half) cudaEventDestroy(h->ev_last_half);
+    h->ev_last_half = nullptr;
     h->reconstructed = false;
     h->in_chunk = 0;
 }
@@ -625,11 +629,13 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
     const bool scale_free = !(h->precision == TK_F16 || h->precision == TK_BF16) ||
                             (h->input_type == TK_INPUT_U16 && !h->host_dark && !h->host_flat);
     // Pipelined mode (tk_fdk_set_pipeline), with the Z-block schedule into a whole-volume buffer:
-    // the first of four chunks is backprojected block by block while the other chunks upload;
-    // once every chunk is filtered, each block gets one accumulating launch over the remaining
-    // angles, so blocks complete one after another and each block's copy to the host
-    // (calculate_reconstruction) overlaps the next block's launch.  A volume that does not fit
-    // beside the projections falls back to the regular path.
+    // the projections upload in chunks of N/8; the chunks of the first half of the angles are
+    // backprojected block by block as they land (this covers the rest of the upload); once every
+    // chunk is filtered, each block gets one accumulating launch over the second half, so blocks
+    // complete one after another and each block's copy to the host (calculate_reconstruction)
+    // overlaps the next block's launch.  The last block's launch is split at a multiple of 64
+    // slices (same bits as one launch) so that half of its copy overlaps the other half.  A
+    // volume that does not fit beside the projections falls back to the regular path.
     bool pipe = h->pipeline && !h->collecting && scale_free && g.N >= 2 * 64;
     h->reconstructed = false;
     if (pipe) {
@@ -647,7 +653,9 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
             }
         }
     }
-    const int chunk = pipe ? std::max(64, (g.N + 3) / 4) : 64;
+    const int chunk = pipe ? std::max(32, (g.N + 7) / 8) : 64;
+    const int nchunks = (g.N + chunk - 1) / chunk;
+    const int major_end = std::min(g.N - chunk, chunk * ((nchunks + 1) / 2));  // first-half angles
     const bool overlap = scale_free && g.N >= 2 * chunk;
     int nblk = 0;
     std::vector<float> zoff;
@@ -724,26 +732,43 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
             if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + off, h->input_type, h->layout, &h->ff,
                                        h->window, d_q + (size_t)b0 * qframe, h->precision, d_scale, h->stream))
                 return rc;
-            if (pipe && b0 == 0) {
+            if (pipe && b0 + nb <= major_end) {
                 for (int n = 0; n < nblk; ++n) {
                     int slices = h->zb;
                     if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;  // kernel.cu:838-840
-                    if (int rc = launch_backproject(gc, d_q, h->precision, d_scale, slices, zoff[n],
-                                                    h->d_vol_full + (size_t)n * h->zb * slab, 0, h->stream, 0))
+                    if (int rc = launch_backproject(gc, d_q + (size_t)b0 * qframe, h->precision, d_scale, slices,
+                                                    zoff[n], h->d_vol_full + (size_t)n * h->zb * slab, b0 > 0,
+                                                    h->stream, b0))
                         return rc;
                 }
             }
         }
+        h->pipe_split = 0;
         if (pipe) {
             tk_geometry gr = g;
-            gr.N = g.N - chunk;
+            gr.N = g.N - major_end;
+            const void *qr = d_q + (size_t)major_end * qframe;
             for (int n = 0; n < nblk; ++n) {
                 int slices = h->zb;
                 if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;
-                if (int rc = launch_backproject(gr, d_q + (size_t)chunk * qframe, h->precision, d_scale, slices,
-                                                zoff[n], h->d_vol_full + (size_t)n * h->zb * slab, 1, h->stream,
-                                                chunk))
+                float *vb = h->d_vol_full + (size_t)n * h->zb * slab;
+                const int split = n == nblk - 1 ? (slices / 2) / 64 * 64 : 0;
+                if (split > 0) {
+                    if (!h->ev_last_half)
+                        TK_CUDA(cudaEventCreateWithFlags(&h->ev_last_half, cudaEventDisableTiming));
+                    if (int rc = launch_backproject(gr, qr, h->precision, d_scale, split, zoff[n], vb, 1, h->stream,
+                                                    major_end))
+                        return rc;
+                    TK_CUDA(cudaEventRecord(h->ev_last_half, h->stream));
+                    if (int rc = launch_backproject(gr, qr, h->precision, d_scale, slices - split,
+                                                    zoff[n] + (float)split, vb + (size_t)split * slab, 1, h->stream,
+                                                    major_end))
+                        return rc;
+                    h->pipe_split = split;
+                } else if (int rc = launch_backproject(gr, qr, h->precision, d_scale, slices, zoff[n], vb, 1,
+                                                       h->stream, major_end)) {
                     return rc;
+                }
                 TK_CUDA(cudaEventRecord(h->ev_blocks[n], h->stream));
             }
         }
@@ -848,9 +873,18 @@ extern "C" int tk_fdk_calculate_reconstruction(tk_fdk *h, tk_block_sink sink, vo
             if (prev_host) TK_CUDA(cudaEventSynchronize(d2h_done[(n - 1) & 1]));
             float *host = sink(user, n, 0);
             TK_CHECK(host, TK_ERR_IO, "block sink returned NULL for block %d", n);
+            const float *src = h->d_vol_full + (size_t)n * zb * slab;
+            int done = 0;  // slices already queued
+            if (n == nblk - 1 && h->pipe_split > 0 && h->pipe_split < slices) {
+                TK_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_last_half, 0));
+                TK_CUDA(cudaMemcpyAsync(host, src, slab * (size_t)h->pipe_split * sizeof(float),
+                                        cudaMemcpyDeviceToHost, h->copy_stream));
+                done = h->pipe_split;
+            }
             TK_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_blocks[n], 0));
-            TK_CUDA(cudaMemcpyAsync(host, h->d_vol_full + (size_t)n * zb * slab, slab * (size_t)slices * sizeof(float),
-                                    cudaMemcpyDeviceToHost, h->copy_stream));
+            TK_CUDA(cudaMemcpyAsync(host + (size_t)done * slab, src + (size_t)done * slab,
+                                    slab * (size_t)(slices - done) * sizeof(float), cudaMemcpyDeviceToHost,
+                                    h->copy_stream));
             TK_CUDA(cudaEventRecord(d2h_done[n & 1], h->copy_stream));
             prev_host = host;
         }
