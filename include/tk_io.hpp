@@ -8,6 +8,9 @@
 //                        block-sink contract of FilteredBackProjection
 //                        (bin_siz, FBPG/mucat_file.cpp:430-793)
 //   tk_io::Settings      setting.xml (LoadSetting/SaveSetting, FBPG/para_TC.cpp:180-303)
+//   tk_io::RsqFile       Scanco .RSQ raw counts with per-row dark/flat rows and the
+//                        beam-hardening line (rsq, FBPG/rsq_load.h:13-59,
+//                        FBPG/rsq_load.cpp:68-82, 185-227, 488-548)
 //
 // The derived scan geometry (distance in pixels, angle step, reconstruction
 // size clamps, rotation offset of clockwise scans) is computed with the
@@ -27,6 +30,7 @@
 #include <sstream>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 namespace tk_io {
@@ -194,6 +198,154 @@ private:
     CraHeader h_;
     float distance_ = 0.f, delta_fi_ = 0.f;
     int active_ = 0;
+};
+
+// ------------------------------------------------------------------ .RSQ
+
+// The 512-byte header block of an RSQ file (ima_data_type, rsq_load.h:13-48),
+// little-endian 32-bit fields at their offsets in the block.
+struct RsqHeader {
+    char check[17] = {};
+    int data_type = 0, nr_of_bytes = 0, nr_of_blocks = 0, patient_index = 0, scanner_id = 0;
+    int creation_date[2] = {0, 0};
+    int dimx_p = 0, dimy_p = 0, dimz_p = 0, dimx_um = 0, dimy_um = 0, dimz_um = 0;
+    int slice_thickness_um = 0, slice_increment_um = 0, slice_1_pos_um = 0;
+    int min_data_value = 0, max_data_value = 0, mu_scaling = 0;
+    int nr_of_samples = 0, nr_of_projections = 0, scandist_um = 0, scanner_type = 0, sampletime_us = 0;
+    int index_measurement = 0, site = 0, reference_line_um = 0, recon_alg = 0;
+    char name[41] = {};
+    int energy = 0, intensity = 0;
+    int data_offset = 0;  // in 512-byte blocks
+};
+
+// Beam-hardening correction "Corr at X0 X1 X2: Y0 Y1 Y2" (152 bytes at file
+// offset 3432) and its line y = A log(x) + B through the first and third
+// points (rsq_load.cpp:538-542).  A and B are the flat-field step's A and B
+// (tk_flatfield, tk_fdk_set_projections_u16).
+struct BeamHardening {
+    int X[3] = {0, 0, 0};
+    double Y[3] = {0, 0, 0};
+    double A = 1.0, B = 0.0;
+    bool parsed = false;
+};
+
+inline bool ParseBeamHardening(const char *text, BeamHardening &bh)
+{
+    BeamHardening t;
+    if (std::sscanf(text, "Corr at %d %d %d: %lf %lf %lf", &t.X[0], &t.X[1], &t.X[2], &t.Y[0], &t.Y[1], &t.Y[2]) !=
+            6 ||
+        t.X[2] == t.X[0])
+        return false;
+    t.A = (t.Y[2] - t.Y[0]) / (t.X[2] - t.X[0]);
+    t.B = t.Y[0] - t.A * t.X[0];
+    t.parsed = true;
+    bh = t;
+    return true;
+}
+
+// An RSQ file: the header block, the beam-hardening text, and from
+// header_offset (3584, rsq_load.cpp:12) one block per detector row of
+// (sin_y + 2) x sin_x uint16 counts: the dark row, the flat row, then the
+// row's sin_y projections (rsq_load.cpp:283-325).  The sizes are the
+// caller's (the reference's defaults: 1024 x 2000); the number of rows in the
+// file follows from its size (rsq_load.cpp:80-82).
+class RsqFile {
+public:
+    explicit RsqFile(std::string path, int sin_x = 1024, int sin_y = 2000,
+                     unsigned long long header_offset = 3584)
+        : path_(std::move(path)), sin_x_(sin_x), sin_y_(sin_y), offset_(header_offset)
+    {
+    }
+
+    // Reads the header block, the beam-hardening text and the file size.
+    // 0 on success, -1 if the file cannot be read.
+    int LoadHeader()
+    {
+        FILE *f = std::fopen(path_.c_str(), "rb");
+        if (!f) return -1;
+        unsigned char blk[512];
+        char bh[153] = {};
+        const bool ok = std::fread(blk, 1, 512, f) == 512 && fseeko(f, 3432, SEEK_SET) == 0 &&
+                        std::fread(bh, 1, 152, f) == 152 && fseeko(f, 0, SEEK_END) == 0;
+        const long long size = ok ? (long long)ftello(f) : -1;
+        std::fclose(f);
+        if (!ok || size < 0) return -1;
+        file_size_ = (unsigned long long)size;
+        auto i32 = [&](int off) {
+            int32_t v;
+            std::memcpy(&v, blk + off, 4);
+            return (int)v;
+        };
+        RsqHeader h;
+        std::memcpy(h.check, blk, 16);
+        int *fields1[] = {&h.data_type, &h.nr_of_bytes, &h.nr_of_blocks, &h.patient_index, &h.scanner_id,
+                          &h.creation_date[0], &h.creation_date[1]};
+        for (int k = 0; k < 7; ++k) *fields1[k] = i32(16 + 4 * k);
+        int *fields2[] = {&h.dimx_p, &h.dimy_p, &h.dimz_p, &h.dimx_um, &h.dimy_um, &h.dimz_um,
+                          &h.slice_thickness_um, &h.slice_increment_um, &h.slice_1_pos_um, &h.min_data_value,
+                          &h.max_data_value, &h.mu_scaling, &h.nr_of_samples, &h.nr_of_projections,
+                          &h.scandist_um, &h.scanner_type, &h.sampletime_us, &h.index_measurement, &h.site,
+                          &h.reference_line_um, &h.recon_alg};
+        for (int k = 0; k < 21; ++k) *fields2[k] = i32(44 + 4 * k);
+        std::memcpy(h.name, blk + 128, 40);
+        h.energy = i32(168);
+        h.intensity = i32(172);
+        h.data_offset = i32(508);
+        header_ = h;
+        ParseBeamHardening(bh, bh_);
+        return 0;
+    }
+
+    const RsqHeader &header() const { return header_; }
+    const BeamHardening &beam_hardening() const { return bh_; }
+    int sin_x() const { return sin_x_; }
+    int sin_y() const { return sin_y_; }
+    // Detector rows in the file (CalculateNumOfSinograms, rsq_load.cpp:80-82).
+    unsigned long long NumOfSinograms() const
+    {
+        const unsigned long long row = (unsigned long long)sin_x_ * (sin_y_ + 2) * 2;
+        return file_size_ > offset_ ? (file_size_ - offset_) / row : 0;
+    }
+
+    // Detector rows [first, last] (LoadImages(first, last), rsq_load.cpp:185-227):
+    // raw counts [n][sin_y][sin_x] (the engine's sinogram-major layout, H = n,
+    // N = sin_y, W = sin_x) and each row's dark and flat rows as float
+    // [n][sin_x] (the per-pixel maps of tk_fdk_set_projections_u16).  0 on
+    // success, -1 on a bad range or a short read.
+    int Load(unsigned first, unsigned last, uint16_t *raw, float *dark, float *flat) const
+    {
+        if (last < first || last >= NumOfSinograms()) return -1;
+        const size_t W = (size_t)sin_x_, rows = (size_t)sin_y_ + 2;
+        FILE *f = std::fopen(path_.c_str(), "rb");
+        if (!f) return -1;
+        const unsigned long long off = offset_ + (unsigned long long)first * rows * W * 2;
+        if (fseeko(f, (off_t)off, SEEK_SET) != 0) {
+            std::fclose(f);
+            return -1;
+        }
+        std::vector<uint16_t> blk(rows * W);
+        for (unsigned r = 0; r + first <= last; ++r) {
+            if (std::fread(blk.data(), 2, blk.size(), f) != blk.size()) {
+                std::fclose(f);
+                return -1;
+            }
+            for (size_t x = 0; x < W; ++x) {
+                dark[r * W + x] = (float)blk[x];
+                flat[r * W + x] = (float)blk[W + x];
+            }
+            std::memcpy(raw + (size_t)r * sin_y_ * W, blk.data() + 2 * W, (size_t)sin_y_ * W * 2);
+        }
+        std::fclose(f);
+        return 0;
+    }
+
+private:
+    std::string path_;
+    int sin_x_, sin_y_;
+    unsigned long long offset_;
+    unsigned long long file_size_ = 0;
+    RsqHeader header_;
+    BeamHardening bh_;
 };
 
 // ------------------------------------------------------------ .bin/.siz

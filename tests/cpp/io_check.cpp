@@ -4,6 +4,9 @@
 //                                                     projections [N][H][W] and [H][N][W] to files
 //   io_check binsiz DIR NAME X Y Z ZB SCANBLOCKS    -> writes two passes (second one collecting)
 //   io_check settings FILE [SAVE_TO]                -> JSON of the parsed settings
+//   io_check rsq FILE SINX SINY FIRST LAST RAW DARK FLAT -> JSON of the header and the
+//                                                     beam-hardening line; rows FIRST..LAST
+//                                                     (raw u16, dark and flat f32) to files
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -75,6 +78,35 @@ int main(int argc, char **argv)
             errors = w.errors();
         }
         std::printf("{\"errors\": %d}\n", errors);
+        return 0;
+    }
+    if (!std::strcmp(argv[1], "rsq") && argc == 10) {
+        tk_io::RsqFile r(argv[2], std::atoi(argv[3]), std::atoi(argv[4]));
+        if (r.LoadHeader()) {
+            std::printf("{\"rc\": -1}\n");
+            return 0;
+        }
+        const unsigned first = (unsigned)std::atoi(argv[5]), last = (unsigned)std::atoi(argv[6]);
+        const size_t n = last >= first ? last - first + 1 : 0, W = (size_t)r.sin_x(), N = (size_t)r.sin_y();
+        std::vector<uint16_t> raw(n * N * W);
+        std::vector<float> dark(n * W), flat(n * W);
+        const int lrc = r.Load(first, last, raw.data(), dark.data(), flat.data());
+        if (!lrc) {
+            FILE *f = std::fopen(argv[7], "wb");
+            if (!f) return 3;
+            std::fwrite(raw.data(), 2, raw.size(), f);
+            std::fclose(f);
+            if (write_file(argv[8], dark) || write_file(argv[9], flat)) return 3;
+        }
+        const tk_io::RsqHeader &h = r.header();
+        const tk_io::BeamHardening &b = r.beam_hardening();
+        std::printf("{\"rc\": 0, \"load\": %d, \"sinograms\": %llu, \"check\": \"%s\", \"samples\": %d, "
+                    "\"projections\": %d, \"dim\": [%d, %d, %d], \"data_offset\": %d, \"energy\": %d, "
+                    "\"name\": \"%s\", \"bh_parsed\": %d, \"bh_x\": [%d, %d, %d], \"bh_y\": [%.17g, %.17g, %.17g], "
+                    "\"A\": %.17g, \"B\": %.17g}\n",
+                    lrc, (unsigned long long)r.NumOfSinograms(), h.check, h.nr_of_samples, h.nr_of_projections,
+                    h.dimx_p, h.dimy_p, h.dimz_p, h.data_offset, h.energy, h.name, (int)b.parsed, b.X[0], b.X[1],
+                    b.X[2], b.Y[0], b.Y[1], b.Y[2], b.A, b.B);
         return 0;
     }
     if (!std::strcmp(argv[1], "settings") && (argc == 3 || argc == 4)) {

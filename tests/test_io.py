@@ -6,7 +6,10 @@ derived geometry is compared with a restatement of cra_con's float/int
 arithmetic (FBPG/mucat_file.cpp:139-161), the loaded frames with the data
 written (clockwise scans reversed, second scan block offset), the volume
 file with the values written (two passes, the second collecting), and
-setting.xml parsing with LoadSetting's defaults (FBPG/para_TC.cpp:180-260).
+setting.xml parsing with LoadSetting's defaults (FBPG/para_TC.cpp:180-260),
+and .RSQ raw scans: the header block, the beam-hardening line A, B
+(FBPG/rsq_load.cpp:538-542) and the per-row dark, flat and projection rows
+(FBPG/rsq_load.cpp:185-227, 299-325).
 """
 import json
 import math
@@ -16,7 +19,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from tomokvas_gb300.scanfile import cra_derived, read_binsiz, write_cra
+from tomokvas_gb300.scanfile import cra_derived, read_binsiz, write_cra, write_rsq
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -102,3 +105,28 @@ def test_settings(io_check, tmp_path):
     d = run(io_check, "settings", tmp_path / "none.xml")
     assert d == {"found": 0, "GPUId": 0, "GPUmemLimit": 5120, "GPUAllocLimit": 1024, "VerticalCenter": 0,
                  "NoOfSlicesInOneBlock": 16, "x": 0, "y": 0, "z": 0, "WaitForEnter": 1}
+
+
+def test_rsq_header_beam_hardening_and_rows(io_check, tmp_path):
+    rows, N, W = 5, 12, 16
+    rng = np.random.default_rng(7)
+    counts = rng.integers(100, 60000, size=(rows, N, W), dtype=np.uint16)
+    dark = rng.integers(0, 50, size=(rows, W), dtype=np.uint16)
+    flat = rng.integers(50000, 65000, size=(rows, W), dtype=np.uint16)
+    path = tmp_path / "scan.rsq"
+    write_rsq(str(path), counts, dark, flat, bh_x=(120, 260, 410), bh_y=(0.85, 1.9, 3.2),
+              name="phantom", header=dict(energy=45000, dimz_um=777))
+    r = run(io_check, "rsq", path, W, N, 1, 3, tmp_path / "raw.u16", tmp_path / "d.f32", tmp_path / "f.f32")
+    assert r["rc"] == 0 and r["load"] == 0 and r["sinograms"] == rows
+    assert r["check"] == "CTDATA-HEADER_V1" and r["name"] == "phantom" and r["energy"] == 45000
+    assert r["samples"] == W and r["projections"] == rows and r["dim"] == [W, N, rows]
+    assert r["bh_parsed"] == 1 and r["bh_x"] == [120, 260, 410] and r["bh_y"] == [0.85, 1.9, 3.2]
+    A = (3.2 - 0.85) / (410 - 120)  # the line through the first and third points
+    assert r["A"] == pytest.approx(A, rel=1e-15) and r["B"] == pytest.approx(0.85 - A * 120, rel=1e-15)
+    raw = np.fromfile(tmp_path / "raw.u16", dtype=np.uint16).reshape(3, N, W)
+    np.testing.assert_array_equal(raw, counts[1:4])  # rows 1..3, sinogram-major [H][N][W]
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "d.f32", dtype=np.float32).reshape(3, W), dark[1:4])
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "f.f32", dtype=np.float32).reshape(3, W), flat[1:4])
+    bad = run(io_check, "rsq", path, W, N, 2, rows, tmp_path / "x", tmp_path / "y", tmp_path / "z")
+    assert bad["load"] == -1  # past the last row
+    assert run(io_check, "rsq", tmp_path / "absent.rsq", W, N, 0, 0, "a", "b", "c")["rc"] == -1

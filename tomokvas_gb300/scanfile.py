@@ -8,6 +8,10 @@ order.  read_binsiz: the volume a bin_siz-style writer produced
 (FBPG/mucat_file.cpp:430-520): "X Y Z 0" in .siz, float32 [Z][Y][X] in .bin.
 cra_geometry: the engine parameters the reference's driver derives from a
 .CRA header (FBPG/para_TC.cpp:48-142 with cra_con's float arithmetic).
+write_rsq: a Scanco-style .RSQ raw scan in the layout rsq reads
+(FBPG/rsq_load.h:13-59, FBPG/rsq_load.cpp:185-227, 488-548): the 512-byte
+header block, the beam-hardening text at byte 3432, and from byte 3584 one
+block per detector row (dark row, flat row, the row's projections) of uint16.
 """
 from __future__ import annotations
 
@@ -16,7 +20,12 @@ import os
 
 import numpy as np
 
+import struct
+
 from .geometry import FDKGeometry
+
+RSQ_DATA_OFFSET = 3584  # rsq_load.cpp:12
+RSQ_BH_OFFSET = 3432    # rsq_load.cpp:506
 
 
 def write_cra(directory: str, name: str, projections, sample_spacing_um: float, distance_cm: float,
@@ -89,3 +98,43 @@ def cra_geometry(sample_spacing_um, distance_cm, detector_x, detector_z, n_proj,
                        tau=float(np.float32(sample_spacing_um)) * 0.0001, X=rx, Y=rx, Z=rz,
                        cx=(rx - 1) / 2.0, cy=(rx - 1) / 2.0, cz=0.0, rot=float(np.float32(rot)),
                        scale=1.0 / scale, dirx=dirs[0], diry=dirs[1], dirz=dirs[2], zb=zb)
+
+
+def write_rsq(path: str, counts, dark, flat, bh_x=(100, 200, 300), bh_y=(1.0, 2.0, 3.0), name: str = "synthetic",
+              header: dict | None = None) -> None:
+    """counts: [rows][N][W] uint16 (each detector row's projections); dark, flat:
+    [rows][W] uint16.  bh_x, bh_y: the three beam-hardening correction points.
+    header: ima_data_type fields by name (rsq_load.h:13-48); the others are 0."""
+    counts = np.ascontiguousarray(counts, dtype="<u2")
+    dark = np.ascontiguousarray(dark, dtype="<u2")
+    flat = np.ascontiguousarray(flat, dtype="<u2")
+    rows, n, w = counts.shape
+    fields = dict(nr_of_samples=w, nr_of_projections=rows, dimx_p=w, dimy_p=n, dimz_p=rows,
+                  data_offset=(RSQ_DATA_OFFSET - 512) // 512)
+    fields.update(header or {})
+    names1 = ["data_type", "nr_of_bytes", "nr_of_blocks", "patient_index", "scanner_id", "creation_date0",
+              "creation_date1"]
+    names2 = ["dimx_p", "dimy_p", "dimz_p", "dimx_um", "dimy_um", "dimz_um", "slice_thickness_um",
+              "slice_increment_um", "slice_1_pos_um", "min_data_value", "max_data_value", "mu_scaling",
+              "nr_of_samples", "nr_of_projections", "scandist_um", "scanner_type", "sampletime_us",
+              "index_measurement", "site", "reference_line_um", "recon_alg"]
+    blk = bytearray(512)
+    blk[0:16] = b"CTDATA-HEADER_V1"
+    for k, f in enumerate(names1):
+        struct.pack_into("<i", blk, 16 + 4 * k, int(fields.get(f, 0)))
+    for k, f in enumerate(names2):
+        struct.pack_into("<i", blk, 44 + 4 * k, int(fields.get(f, 0)))
+    blk[128:168] = name.encode()[:40].ljust(40, b"\0")
+    struct.pack_into("<i", blk, 168, int(fields.get("energy", 0)))
+    struct.pack_into("<i", blk, 172, int(fields.get("intensity", 0)))
+    struct.pack_into("<i", blk, 508, int(fields["data_offset"]))
+    head = bytearray(RSQ_DATA_OFFSET)
+    head[0:512] = blk
+    bh = "Corr at %d %d %d:  %.6f %.6f %.6f" % (*bh_x, *bh_y)
+    head[RSQ_BH_OFFSET:RSQ_BH_OFFSET + 152] = bh.encode().ljust(152, b"\0")
+    with open(path, "wb") as f:
+        f.write(head)
+        for r in range(rows):
+            f.write(dark[r].tobytes())
+            f.write(flat[r].tobytes())
+            f.write(counts[r].tobytes())
