@@ -364,8 +364,11 @@ int tk_fdk_initialize(tk_fdk *h);
 int tk_fdk_calculate_reconstruction(tk_fdk *h, tk_block_sink sink, void *user);
 /* Whole volume into a device buffer d_vol[Z][Y][X] (all Z slices). */
 int tk_fdk_reconstruct_device(tk_fdk *h, float *d_vol);
-/* Seconds spent in the stages of the last call (filter, backprojection,
- * transfers), measured with CUDA events. */
+/* Milliseconds spent in the stages of the last initialize + reconstruction,
+ * measured with CUDA events: the filter, the backprojection (filter and
+ * backprojection together in the pipelined mode, where they interleave), the
+ * upload, and d2h_ms, the part of the block copies to the host that runs after
+ * the last backprojection (the copies before it overlap the computation). */
 int tk_fdk_get_timings(tk_fdk *h, float *filter_ms, float *bp_ms, float *h2d_ms, float *d2h_ms);
 
 #ifdef __cplusplus

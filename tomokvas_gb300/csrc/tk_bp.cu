@@ -775,11 +775,6 @@ struct BPVariant {
     {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, 2>), \
      reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, 2>), TK_F16, TX, TY, TZ, ST, \
      true, "cimg_h2<f16," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
-// the same with per-slice row interpolation on half-broadcast operands (WALK 3)
-#define TK_BP_CIMG_H3(TX, TY, TZ, ST, MB) \
-    {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, 3>), \
-     reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, 3>), TK_F16, TX, TY, TZ, ST, \
-     true, "cimg_h3<f16," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
 // The first entry of each storage format is its default: the packed walks
 // (same bits as the scalar ones, fewer issued instructions), and for FP16
@@ -799,7 +794,6 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
-    TK_BP_CIMG_H3(16, 16, 64, 3, 2),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant

@@ -148,17 +148,6 @@ __device__ __forceinline__ void acc_mixed_x2(uint32_t val2, uint32_t w2, float &
         : "r"(val2), "r"(w2));
 }
 
-// acc += w.lo * val.lo (FP16 product exact in FP32, one rounding).
-__device__ __forceinline__ void acc_mixed(uint32_t val2, uint32_t w2, float &acc)
-{
-    asm("{\n\t.reg .b16 vl, vh, wl, wh;\n\t"
-        "mov.b32 {vl, vh}, %1;\n\t"
-        "mov.b32 {wl, wh}, %2;\n\t"
-        "fma.rn.f32.f16 %0, wl, vl, %0;\n\t}"
-        : "+f"(acc)
-        : "r"(val2), "r"(w2));
-}
-
 // Walks of a column (WALK):
 //   0  scalar FP32, one slice per step;
 //   1  packed FP32, two slices per step (floor/frac, the row interpolation and
@@ -169,46 +158,15 @@ __device__ __forceinline__ void acc_mixed(uint32_t val2, uint32_t w2, float &acc
 //      interpolation of both slices by one HFMA2 with the fractions rounded
 //      to FP16, and the weight U^2 rounded to FP16 applied by fma.rn.f32.f16
 //      into the FP32 accumulators.  Fewer FP32-pipe operations, FP16
-//      rounding of fv, U^2 and the interpolated sample;
-//   3  as 2, but the row interpolation is one HFMA2 per slice on the
-//      half-broadcast operands of that slice's entry (no half-word permutes).
+//      rounding of fv, U^2 and the interpolated sample.  (One HFMA2 per slice on
+//      half-broadcast operands instead of the two permutes measured 0.6 %
+//      slower: it needs more registers and spills at 128.)
 template <int PREC, int TZ, bool ALL_IN, bool PARTIAL, int WALK = 0>
 __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu,
                                             float U2, float Hm1, int zlast, float (&acc)[TZ])
 {
     const float2 fu2 = pack_fu<PREC>(fu);
-    if constexpr (WALK == 3 && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
-        const __half2 fuh = *reinterpret_cast<const __half2 *>(&fu2.x);
-        const __half2 U2h2 = __float2half2_rn(U2);
-        const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
-#pragma unroll
-        for (int z = 0; z < TZ; z += 2) {
-            const float va = fmaf((float)z, dv, v0), vb = fmaf((float)(z + 1), dv, v0);
-            float fla, flb, fva, fvb;
-            floor_frac_x2(va, vb, fla, flb, fva, fvb);
-            uint32_t loa, hia, lob, hib;
-            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
-                         : "=r"(loa), "=r"(hia)
-                         : "r"((uint32_t)__float_as_int(fla) * row_bytes + sbase));
-            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
-                         : "=r"(lob), "=r"(hib)
-                         : "r"((uint32_t)__float_as_int(flb) * row_bytes + sbase));
-            const __half2 ha = __hfma2(*reinterpret_cast<const __half2 *>(&hia), fuh,
-                                       *reinterpret_cast<const __half2 *>(&loa));
-            const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&hib), fuh,
-                                       *reinterpret_cast<const __half2 *>(&lob));
-            const __half2 fv2 = __floats2half2_rn(fva, fvb);
-            const __half2 vala = __hfma2(__high2half2(ha), __low2half2(fv2), __low2half2(ha));
-            const __half2 valb = __hfma2(__high2half2(hb), __high2half2(fv2), __low2half2(hb));
-            uint32_t wa = w_all, wb = w_all;
-            if constexpr (!ALL_IN) {  // kernel.cu:130-131
-                wa = (va >= 0.f && va <= Hm1) ? w_all : 0u;
-                wb = (vb >= 0.f && vb <= Hm1) ? w_all : 0u;
-            }
-            acc_mixed(*reinterpret_cast<const uint32_t *>(&vala), wa, acc[z]);
-            acc_mixed(*reinterpret_cast<const uint32_t *>(&valb), wb, acc[z + 1]);
-        }
-    } else if constexpr (WALK == 2 && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
+    if constexpr (WALK == 2 && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
         const __half2 fuh = *reinterpret_cast<const __half2 *>(&fu2.x);
         const __half2 U2h2 = __float2half2_rn(U2);
         const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);

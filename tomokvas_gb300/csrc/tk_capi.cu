@@ -866,6 +866,7 @@ extern "C" int tk_fdk_calculate_reconstruction(tk_fdk *h, tk_block_sink sink, vo
         // pipelined: the volume was reconstructed during initialize; block n is copied out once its
         // last backprojection has run, and lands before block n+1 is requested from the sink
         cudaEvent_t d2h_done[2] = {h->ev[6], h->ev[7]};
+        TK_CUDA(cudaEventRecord(h->ev[4], h->stream));  // every backprojection queued by initialize has run
         float *prev_host = nullptr;
         for (int n = 0; n < nblk; ++n) {
             int slices = zb;
@@ -888,9 +889,11 @@ extern "C" int tk_fdk_calculate_reconstruction(tk_fdk *h, tk_block_sink sink, vo
             TK_CUDA(cudaEventRecord(d2h_done[n & 1], h->copy_stream));
             prev_host = host;
         }
+        TK_CUDA(cudaEventRecord(h->ev[5], h->copy_stream));
         TK_CUDA(cudaStreamSynchronize(h->copy_stream));
         TK_CUDA(cudaStreamSynchronize(h->stream));
         elapsed(h->ev[2], h->ev[3], &h->t_bp);  // filter + backprojection, interleaved by chunk
+        elapsed(h->ev[4], h->ev[5], &h->t_d2h);  // the copies' tail after the last backprojection
         return check_device_flags(h->stream);
     }
     const size_t block_bytes = slab * zb * sizeof(float);
@@ -941,6 +944,7 @@ extern "C" int tk_fdk_calculate_reconstruction(tk_fdk *h, tk_block_sink sink, vo
     TK_CUDA(cudaStreamSynchronize(h->copy_stream));
     TK_CUDA(cudaStreamSynchronize(h->stream));
     if (h->filtered) elapsed(h->ev[2], h->ev[3], &h->t_filter);
+    if (nblk > 0) elapsed(bp_done[(nblk - 1) & 1], d2h_done[(nblk - 1) & 1], &h->t_d2h);  // the last copy's tail
     return check_device_flags(h->stream);
 }
 
