@@ -341,10 +341,10 @@ int tk_fdk_set_precision(tk_fdk *h, int precision);
 int tk_fdk_set_stream(tk_fdk *h, void *stream);
 /* Pipelined mode (off by default; the C++ FilteredBackProjection turns it on).
  * tk_fdk_initialize uploads the projections in chunks of N/8 angles, filters
- * each chunk as it lands and backprojects the chunks of the first half of the
- * angles into a whole-volume device buffer (Z block by Z block, the
+ * each chunk as it lands and backprojects the chunks of the first quarter of
+ * the angles into a whole-volume device buffer (Z block by Z block, the
  * reference's block offsets) as they land; it then queues one accumulating
- * launch per Z block over the second half (the last block's in two parts) and
+ * launch per Z block over the rest (the last block's in two parts) and
  * returns once the host buffer has been read.
  * tk_fdk_calculate_reconstruction only delivers the blocks, each copy starting
  * once its block's launch has run, overlapping the next block's launch.  It applies to

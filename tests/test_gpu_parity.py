@@ -481,12 +481,12 @@ def _handle_run(g, data, layout, prec, pipeline, zb, counts=None, after_init=Non
 def pipelined_launches(g, nblk, last_slices):
     """Launches of a pipelined Initialize (tk_fdk_initialize): chunks of
     max(32, ceil(N/8)) angles, each a storage-scale and a filter launch; the
-    chunks ending by the first half of the angles backprojected block by
+    chunks ending by the first quarter of the angles backprojected block by
     block; one launch per block over the rest, the last block in two when it
     holds at least 128 slices."""
     chunk = max(32, -(-g.N // 8))
     nch = -(-g.N // chunk)
-    major_end = min(g.N - chunk, chunk * ((nch + 1) // 2))
+    major_end = min(g.N - chunk, chunk * max(1, (nch + 2) // 4))
     major = sum(1 for b0 in range(0, g.N, chunk) if b0 + min(chunk, g.N - b0) <= major_end)
     split = 1 if (last_slices // 2) // 64 * 64 > 0 else 0
     return 2 * nch + major * nblk + nblk + split
@@ -502,8 +502,8 @@ def pipelined_launches(g, nblk, last_slices):
 def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, layout):
     """tk_fdk_set_pipeline: Initialize uploads N = 300 projections in 38-angle
     chunks, filters each as it lands, backprojects the chunks of the first
-    152 angles into the whole volume with the Z-block schedule as they land,
-    then each block over the other 148 angles; CalculateReconstruction only
+    76 angles into the whole volume with the Z-block schedule as they land,
+    then each block over the other 224 angles; CalculateReconstruction only
     delivers blocks.  The volume equals the regular path's to FP32 rounding of
     the partial sums, with the same blocks requested, the same last-slice
     quirk, and the launches of that schedule."""

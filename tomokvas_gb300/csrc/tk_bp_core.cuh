@@ -118,6 +118,17 @@ __device__ __forceinline__ void floor_frac_x2(float va, float vb, float &fla, fl
         : "=f"(fla), "=f"(flb), "=f"(fva), "=f"(fvb)
         : "f"(va), "f"(vb), "f"(kMagic));
 }
+// (va, vb) += (d, d) as one add.rn.f32x2.
+__device__ __forceinline__ void add_pair(float &va, float &vb, float d)
+{
+    asm("{\n\t.reg .b64 V, D;\n\t"
+        "mov.b64 V, {%0, %1};\n\t"
+        "mov.b64 D, {%2, %2};\n\t"
+        "add.rn.f32x2 V, V, D;\n\t"
+        "mov.b64 {%0, %1}, V;\n\t}"
+        : "+f"(va), "+f"(vb)
+        : "f"(d));
+}
 // acc_i = fma(w_i, fma(fv_i, b_i, a_i), acc_i) for i = 0, 1 as two fma.rn.f32x2.
 __device__ __forceinline__ void interp_acc_x2(float aa, float ab, float ba, float bb, float fva, float fvb, float wa,
                                               float wb, float &acc0, float &acc1)
@@ -158,7 +169,10 @@ __device__ __forceinline__ void acc_mixed_x2(uint32_t val2, uint32_t w2, float &
 //      interpolation of both slices by one HFMA2 with the fractions rounded
 //      to FP16, and the weight U^2 rounded to FP16 applied by fma.rn.f32.f16
 //      into the FP32 accumulators.  Fewer FP32-pipe operations, FP16
-//      rounding of fv, U^2 and the interpolated sample.  (One HFMA2 per slice on
+//      rounding of fv, U^2 and the interpolated sample;
+//   4  as 2, but the row coordinates of a pair are advanced by (2 dv, 2 dv)
+//      with one add.f32x2 and set exactly, fmaf(z, dv, v0), every 16 pairs
+//      (drift below 16 half-ulps of v between them).  (One HFMA2 per slice on
 //      half-broadcast operands instead of the two permutes measured 0.6 %
 //      slower: it needs more registers and spills at 128.)
 template <int PREC, int TZ, bool ALL_IN, bool PARTIAL, int WALK = 0>
@@ -166,13 +180,25 @@ __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, 
                                             float U2, float Hm1, int zlast, float (&acc)[TZ])
 {
     const float2 fu2 = pack_fu<PREC>(fu);
-    if constexpr (WALK == 2 && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
+    if constexpr ((WALK == 2 || WALK == 4) && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
         const __half2 fuh = *reinterpret_cast<const __half2 *>(&fu2.x);
         const __half2 U2h2 = __float2half2_rn(U2);
         const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
+        const float dv2 = 2.f * dv;
+        float ra = v0, rb = v0;
 #pragma unroll
         for (int z = 0; z < TZ; z += 2) {
-            const float va = fmaf((float)z, dv, v0), vb = fmaf((float)(z + 1), dv, v0);
+            float va, vb;
+            if (WALK == 2 || z % 32 == 0) {
+                va = fmaf((float)z, dv, v0);
+                vb = fmaf((float)(z + 1), dv, v0);
+            } else {
+                add_pair(ra, rb, dv2);
+                va = ra;
+                vb = rb;
+            }
+            ra = va;
+            rb = vb;
             float fla, flb, fva, fvb;
             floor_frac_x2(va, vb, fla, flb, fva, fvb);
             uint32_t loa, hia, lob, hib;

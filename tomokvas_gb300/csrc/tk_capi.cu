@@ -629,9 +629,9 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
     const bool scale_free = !(h->precision == TK_F16 || h->precision == TK_BF16) ||
                             (h->input_type == TK_INPUT_U16 && !h->host_dark && !h->host_flat);
     // Pipelined mode (tk_fdk_set_pipeline), with the Z-block schedule into a whole-volume buffer:
-    // the projections upload in chunks of N/8; the chunks of the first half of the angles are
+    // the projections upload in chunks of N/8; the chunks of the first quarter of the angles are
     // backprojected block by block as they land (this covers the rest of the upload); once every
-    // chunk is filtered, each block gets one accumulating launch over the second half, so blocks
+    // chunk is filtered, each block gets one accumulating launch over the rest, so blocks
     // complete one after another and each block's copy to the host (calculate_reconstruction)
     // overlaps the next block's launch.  The last block's launch is split at a multiple of 64
     // slices (same bits as one launch) so that half of its copy overlaps the other half.  A
@@ -655,7 +655,9 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
     }
     const int chunk = pipe ? std::max(32, (g.N + 7) / 8) : 64;
     const int nchunks = (g.N + chunk - 1) / chunk;
-    const int major_end = std::min(g.N - chunk, chunk * ((nchunks + 1) / 2));  // first-half angles
+    // first quarter of the angles: at 1024^3 its 60 ms of backprojection covers the rest of a slow
+    // (25 GB/s) upload, and the three quarters left give the block copies 180 ms to overlap
+    const int major_end = std::min(g.N - chunk, chunk * std::max(1, (nchunks + 2) / 4));
     const bool overlap = scale_free && g.N >= 2 * chunk;
     int nblk = 0;
     std::vector<float> zoff;
