@@ -771,10 +771,6 @@ struct BPVariant {
      reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 1>), P, TX, TY, TZ, ST, true, \
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 // FP16 half-math walk (update_cimg WALK 2): not bit-identical to the FP32 walks
-#define TK_BP_CIMG_H4(TX, TY, TZ, ST, MB) \
-    {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, 4>), \
-     reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, 4>), TK_F16, TX, TY, TZ, ST, \
-     true, "cimg_h4<f16," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 #define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB) \
     {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, 2>), \
      reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, 2>), TK_F16, TX, TY, TZ, ST, \
@@ -798,7 +794,6 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
-    TK_BP_CIMG_H4(16, 16, 64, 3, 2),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant

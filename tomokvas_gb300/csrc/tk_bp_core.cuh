@@ -164,15 +164,15 @@ __device__ __forceinline__ void acc_mixed_x2(uint32_t val2, uint32_t w2, float &
 //   1  packed FP32, two slices per step (floor/frac, the row interpolation and
 //      the accumulation as f32x2); per voxel exactly the operations of the
 //      scalar walk, so both give the same bits;
-//   2  FP16 storage only, two slices per step: floor/frac in FP32 as above;
+//   2  FP16 storage only, two slices per step: the pair's row coordinates
+//      advanced by (2 dv, 2 dv) with one add.f32x2 and set exactly,
+//      fmaf(z, dv, v0), every 16 pairs (drift below 16 half-ulps of v between
+//      them); floor/frac in FP32 as above;
 //      the column interpolation of both entries by HFMA2, then the row
 //      interpolation of both slices by one HFMA2 with the fractions rounded
 //      to FP16, and the weight U^2 rounded to FP16 applied by fma.rn.f32.f16
 //      into the FP32 accumulators.  Fewer FP32-pipe operations, FP16
-//      rounding of fv, U^2 and the interpolated sample;
-//   4  as 2, but the row coordinates of a pair are advanced by (2 dv, 2 dv)
-//      with one add.f32x2 and set exactly, fmaf(z, dv, v0), every 16 pairs
-//      (drift below 16 half-ulps of v between them).  (One HFMA2 per slice on
+//      rounding of fv, U^2 and the interpolated sample.  (One HFMA2 per slice on
 //      half-broadcast operands instead of the two permutes measured 0.6 %
 //      slower: it needs more registers and spills at 128.)
 template <int PREC, int TZ, bool ALL_IN, bool PARTIAL, int WALK = 0>
@@ -180,7 +180,7 @@ __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, 
                                             float U2, float Hm1, int zlast, float (&acc)[TZ])
 {
     const float2 fu2 = pack_fu<PREC>(fu);
-    if constexpr ((WALK == 2 || WALK == 4) && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
+    if constexpr (WALK == 2 && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
         const __half2 fuh = *reinterpret_cast<const __half2 *>(&fu2.x);
         const __half2 U2h2 = __float2half2_rn(U2);
         const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
@@ -189,7 +189,7 @@ __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, 
 #pragma unroll
         for (int z = 0; z < TZ; z += 2) {
             float va, vb;
-            if (WALK == 2 || z % 32 == 0) {
+            if (z % 32 == 0) {
                 va = fmaf((float)z, dv, v0);
                 vb = fmaf((float)(z + 1), dv, v0);
             } else {
