@@ -116,10 +116,6 @@ __device__ __forceinline__ float cosine_weight_rt(const LoadParams &L, float rt,
     const float ce = (float)x - L.cX;
     return L.D * rsqrtf(fmaf(ce, ce, rt));
 }
-__device__ __forceinline__ float cosine_weight(const LoadParams &L, int r, int x)
-{
-    return cosine_weight_rt(L, weight_row_term(L, r), x);
-}
 
 // Raw sample x of the row at element offset off (counts as float for u16).
 __device__ __forceinline__ float load_raw(const LoadParams &L, long long off, int x)
