@@ -370,6 +370,9 @@ struct tk_fdk {
     int pipe_zb = 0;   // Z-block size the pipelined volume was built with
     int pipe_split = 0;      // > 0: the last block's first pipe_split slices complete at ev_last_half
     cudaEvent_t ev_last_half = nullptr;
+    // odd Z blocks run on a second stream, so one block's launch fills the tail of another's
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_filt = nullptr, ev_join = nullptr;
     int in_chunk = 0;  // > 0: sinogram-major input stored as [H][nb][W] blocks of in_chunk angles
 };
 
@@ -392,6 +395,14 @@ static void release_device(tk_fdk *h)
     h->ev_blocks.clear();
     if (h->ev_last_half) cudaEventDestroy(h->ev_last_half);
     h->ev_last_half = nullptr;
+    if (h->ev_filt) cudaEventDestroy(h->ev_filt);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    h->ev_filt = h->ev_join = nullptr;
+    if (h->aux_stream) {
+        cudaStreamSynchronize(h->aux_stream);
+        cudaStreamDestroy(h->aux_stream);
+    }
+    h->aux_stream = nullptr;
     h->reconstructed = false;
     h->in_chunk = 0;
 }
@@ -662,6 +673,9 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
     int nblk = 0;
     std::vector<float> zoff;
     if (pipe) {
+        if (!h->aux_stream) TK_CUDA(cudaStreamCreateWithFlags(&h->aux_stream, cudaStreamNonBlocking));
+        if (!h->ev_filt) TK_CUDA(cudaEventCreateWithFlags(&h->ev_filt, cudaEventDisableTiming));
+        if (!h->ev_join) TK_CUDA(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
         nblk = tk_zblock_offsets(&g, h->zb, nullptr, 0);
         zoff.resize((size_t)std::max(nblk, 1));
         tk_zblock_offsets(&g, h->zb, zoff.data(), nblk);
@@ -735,12 +749,16 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
                                        h->window, d_q + (size_t)b0 * qframe, h->precision, d_scale, h->stream))
                 return rc;
             if (pipe && b0 + nb <= major_end) {
+                if (nblk > 1) {  // the odd blocks' stream waits for this chunk's filter
+                    TK_CUDA(cudaEventRecord(h->ev_filt, h->stream));
+                    TK_CUDA(cudaStreamWaitEvent(h->aux_stream, h->ev_filt, 0));
+                }
                 for (int n = 0; n < nblk; ++n) {
                     int slices = h->zb;
                     if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;  // kernel.cu:838-840
                     if (int rc = launch_backproject(gc, d_q + (size_t)b0 * qframe, h->precision, d_scale, slices,
                                                     zoff[n], h->d_vol_full + (size_t)n * h->zb * slab, b0 > 0,
-                                                    h->stream, b0))
+                                                    (n & 1) ? h->aux_stream : h->stream, b0))
                         return rc;
                 }
             }
@@ -750,28 +768,37 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
             tk_geometry gr = g;
             gr.N = g.N - major_end;
             const void *qr = d_q + (size_t)major_end * qframe;
+            if (nblk > 1) {  // the odd blocks' stream waits for the last filter
+                TK_CUDA(cudaEventRecord(h->ev_filt, h->stream));
+                TK_CUDA(cudaStreamWaitEvent(h->aux_stream, h->ev_filt, 0));
+            }
             for (int n = 0; n < nblk; ++n) {
                 int slices = h->zb;
                 if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;
                 float *vb = h->d_vol_full + (size_t)n * h->zb * slab;
+                cudaStream_t bs = (n & 1) ? h->aux_stream : h->stream;  // every launch of block n
                 const int split = n == nblk - 1 ? (slices / 2) / 64 * 64 : 0;
                 if (split > 0) {
                     if (!h->ev_last_half)
                         TK_CUDA(cudaEventCreateWithFlags(&h->ev_last_half, cudaEventDisableTiming));
-                    if (int rc = launch_backproject(gr, qr, h->precision, d_scale, split, zoff[n], vb, 1, h->stream,
+                    if (int rc = launch_backproject(gr, qr, h->precision, d_scale, split, zoff[n], vb, 1, bs,
                                                     major_end))
                         return rc;
-                    TK_CUDA(cudaEventRecord(h->ev_last_half, h->stream));
+                    TK_CUDA(cudaEventRecord(h->ev_last_half, bs));
                     if (int rc = launch_backproject(gr, qr, h->precision, d_scale, slices - split,
-                                                    zoff[n] + (float)split, vb + (size_t)split * slab, 1, h->stream,
+                                                    zoff[n] + (float)split, vb + (size_t)split * slab, 1, bs,
                                                     major_end))
                         return rc;
                     h->pipe_split = split;
-                } else if (int rc = launch_backproject(gr, qr, h->precision, d_scale, slices, zoff[n], vb, 1,
-                                                       h->stream, major_end)) {
+                } else if (int rc = launch_backproject(gr, qr, h->precision, d_scale, slices, zoff[n], vb, 1, bs,
+                                                       major_end)) {
                     return rc;
                 }
-                TK_CUDA(cudaEventRecord(h->ev_blocks[n], h->stream));
+                TK_CUDA(cudaEventRecord(h->ev_blocks[n], bs));
+            }
+            if (nblk > 1) {  // later work on the stream sees both streams' launches
+                TK_CUDA(cudaEventRecord(h->ev_join, h->aux_stream));
+                TK_CUDA(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
             }
         }
         TK_CUDA(cudaEventRecord(h->ev[3], h->stream));
