@@ -291,6 +291,28 @@ def test_u16_per_pixel_flat_dark(orc, cuda, case):
     assert rel_rmse(vol.cpu().numpy(), v64) < noisy_tol(rest)
 
 
+@pytest.mark.parametrize("W,layout", [(63, "projection"), (127, "sinogram"), (64, "sinogram")])
+def test_u16_filter_stage_any_width(orc, cuda, W, layout):
+    """The u16 load of the filter: 16-byte runs of 8 counts where rows are
+    16-byte aligned (W = 64), one count at a time otherwise (odd W), in both
+    layouts; the filtered rows equal the FP32 restatement of log, weight and
+    filter (rsq flat field with dark, beam-hardening line and invert)."""
+    import torch
+
+    g = small_geometry(W=W, N=10, H=12, vol=(16, 16, 8))
+    G = orc.geom_from(g)
+    rng = np.random.default_rng(W)
+    raw = rng.integers(200, 60000, size=(g.N, g.H, g.W), dtype=np.uint16)  # [N][H][W]
+    src = raw if layout == "projection" else np.ascontiguousarray(np.transpose(raw, (1, 0, 2)))
+    ff = device.flatfield(flat_value=61000.0, dark_value=120.0, A=1.3, B=0.05, invert=True, floor_counts=0.5)
+    q, _ = device.filter_projections(g, to_dev(src.view(np.int16), torch), _lib.TK_INPUT_U16,
+                                     _lib.LAYOUTS[layout], ff=ff, window=_lib.TK_WINDOW_HANN)
+    torch.cuda.synchronize()
+    p = orc.log_u16(raw, np.float32(61000.0), np.float32(120.0), A=1.3, B=0.05, invert=True)  # [H][N][W]
+    q_ref = orc.filter_f32(orc.weight_f32(p, G), G, "hann")
+    assert rel_rmse(q.cpu().numpy()[:, :, :g.W], np.transpose(q_ref, (1, 0, 2))) < 2e-6
+
+
 def test_handle_block_schedule_matches_restatement(orc, cuda):
     """FilteredBackProjection mirror with a bin_siz-like sink, Z=255 / ZB=30
     (inexact reference Z centring) and the last-slice quirk case Z=33 / ZB=16."""
