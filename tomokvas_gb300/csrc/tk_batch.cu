@@ -288,6 +288,11 @@ struct tk_batch {
     // graph
     cudaStream_t cap = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    // the items' filters run on several streams forked from the run's stream (parallel branches
+    // of the captured graph): most items are too small to fill the GPU one after another
+    std::vector<cudaStream_t> fstreams;
+    std::vector<cudaEvent_t> fdone;
+    cudaEvent_t fork = nullptr;
 };
 
 namespace {
@@ -440,15 +445,35 @@ int build_tables(tk_batch *b, int vi, cudaStream_t st)
 }
 
 // Filters of every item, then the persistent backprojection.
+constexpr int kFilterStreams = 8;
+
 int enqueue(tk_batch *b, cudaStream_t st)
 {
     const int n = (int)b->in.size();
     float *scales = reinterpret_cast<float *>(b->ws + b->off_scale);
+    const int K = std::min(n, kFilterStreams);
+    if (!b->fork) TK_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    while ((int)b->fstreams.size() < K) {
+        cudaStream_t s;
+        cudaEvent_t e;
+        TK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        TK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->fstreams.push_back(s);
+        b->fdone.push_back(e);
+    }
+    // item i's filter chain (storage scale, filter) on stream i mod K; each item writes only its
+    // own coefficient image and scale, so the chains are independent
+    TK_CUDA(cudaEventRecord(b->fork, st));
+    for (int k = 0; k < K; ++k) TK_CUDA(cudaStreamWaitEvent(b->fstreams[k], b->fork, 0));
     for (int i = 0; i < n; ++i) {
         const auto &it = b->in[i];
         if (int rc = launch_filter(it.g, it.d_in, it.input_type, it.layout, it.has_ff ? &it.ff : nullptr, it.window,
-                                   b->ws + b->off_q[i], b->precision, scales + i, st))
+                                   b->ws + b->off_q[i], b->precision, scales + i, b->fstreams[i % K]))
             return rc;
+    }
+    for (int k = 0; k < K; ++k) {
+        TK_CUDA(cudaEventRecord(b->fdone[k], b->fstreams[k]));
+        TK_CUDA(cudaStreamWaitEvent(st, b->fdone[k], 0));
     }
     int *counter = reinterpret_cast<int *>(b->ws);
     TK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
@@ -477,6 +502,12 @@ extern "C" void tk_batch_destroy(tk_batch *b)
 {
     if (!b) return;
     drop_graph(b);
+    for (cudaStream_t s : b->fstreams) {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    for (cudaEvent_t e : b->fdone) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->cap) cudaStreamDestroy(b->cap);
     delete b;
 }
