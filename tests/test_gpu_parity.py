@@ -500,18 +500,25 @@ def _handle_run(g, data, layout, prec, pipeline, zb, counts=None, after_init=Non
     return out, launches
 
 
-def pipelined_launches(g, nblk, last_slices):
+def pipelined_launches(g, nblk, last_slices, zoff=None):
     """Launches of a pipelined Initialize (tk_fdk_initialize): chunks of
     max(32, ceil(N/8)) angles, each a storage-scale and a filter launch; the
     chunks ending by the first quarter of the angles backprojected block by
-    block; one launch per block over the rest, the last block in two when it
-    holds at least 128 slices."""
+    block, or in one launch over all blocks when the blocks' slice
+    coordinates are those of one launch (float32 arithmetic) and the blocks
+    start on 64-slice boundaries; one launch per block over the rest, the
+    last block in two when it holds at least 128 slices."""
     chunk = max(32, -(-g.N // 8))
     nch = -(-g.N // chunk)
     major_end = min(g.N - chunk, chunk * max(1, (nch + 2) // 4))
     major = sum(1 for b0 in range(0, g.N, chunk) if b0 + min(chunk, g.N - b0) <= major_end)
     split = 1 if (last_slices // 2) // 64 * 64 > 0 else 0
-    return 2 * nch + major * nblk + nblk + split
+    merged = False
+    if zoff is not None and g.zb % 64 == 0:
+        f = np.float32
+        merged = all(f(z) + f(zoff[n]) == f(n * g.zb + z) + f(zoff[0])
+                     for n in range(nblk) for z in range(min(g.zb, g.Z - n * g.zb)))
+    return 2 * nch + major * (1 if merged else nblk) + nblk + split
 
 
 @pytest.mark.parametrize("vol_shape,zb,prec,raw,layout", [
@@ -519,6 +526,7 @@ def pipelined_launches(g, nblk, last_slices):
     ((40, 40, 33), 16, "f16", True, "projection"),    # last-slice quirk
     ((36, 40, 30), 64, "f32c", False, "projection"),  # one block, zb > Z
     ((40, 40, 128), 128, "f16", True, "projection"),  # the last block's launch split at 64 slices
+    ((40, 40, 256), 128, "f16", True, "projection"),  # two blocks: first quarter in one launch
     ((40, 40, 40), 16, "f16", True, "sinogram"),      # [H][N][W], packed per chunk by strided copies
     ((40, 40, 33), 16, "f32", False, "sinogram")])
 def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, layout):
@@ -538,9 +546,10 @@ def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, la
     data = None if raw else proj
     reg, _ = _handle_run(g, data, layout, prec, False, zb, counts)
     pip, launches = _handle_run(g, data, layout, prec, True, zb, counts)
-    nblk = len(orc.zblocks(G))
+    zoff = orc.zblocks(G)
+    nblk = len(zoff)
     last = g.Z - (nblk - 1) * zb if nblk * zb > g.Z else zb
-    assert launches == pipelined_launches(g, nblk, last)
+    assert launches == pipelined_launches(g, nblk, last, zoff)
     assert pip.blocks_requested == reg.blocks_requested
     assert rel_rmse(pip.volume, reg.volume) < 1e-6
     assert max_abs(pip.volume, reg.volume) < 1e-5 * np.abs(reg.volume).max()

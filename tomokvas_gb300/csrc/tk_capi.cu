@@ -685,6 +685,21 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
             h->ev_blocks.push_back(e);
         }
     }
+    // The first-quarter chunks are backprojected in one launch over all blocks when that is the
+    // same arithmetic as one launch per block: every slice's coordinate (float)z + zoff[n] equals
+    // (float)(n zb + z) + zoff[0], and the blocks start on 64-slice z-chunk boundaries.
+    int merged_slices = 0;
+    if (pipe && h->zb % 64 == 0) {
+        bool same = true;
+        for (int n = 0; n < nblk && same; ++n) {
+            int slices = h->zb;
+            if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;
+            for (int z = 0; z < slices && same; ++z)
+                same = (float)z + zoff[n] == (float)(n * h->zb + z) + zoff[0];
+            merged_slices += slices;
+        }
+        if (!same) merged_slices = 0;
+    }
     h->in_chunk = overlap && h->layout == TK_LAYOUT_SINOGRAM ? chunk : 0;
     if (!overlap)
         TK_CUDA(cudaMemcpyAsync(h->d_in, h->host_in, in_bytes, cudaMemcpyHostToDevice, h->stream));
@@ -748,7 +763,11 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
             if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + off, h->input_type, h->layout, &h->ff,
                                        h->window, d_q + (size_t)b0 * qframe, h->precision, d_scale, h->stream))
                 return rc;
-            if (pipe && b0 + nb <= major_end) {
+            if (pipe && b0 + nb <= major_end && merged_slices > 0) {
+                if (int rc = launch_backproject(gc, d_q + (size_t)b0 * qframe, h->precision, d_scale, merged_slices,
+                                                zoff[0], h->d_vol_full, b0 > 0, h->stream, b0))
+                    return rc;
+            } else if (pipe && b0 + nb <= major_end) {
                 if (nblk > 1) {  // the odd blocks' stream waits for this chunk's filter
                     TK_CUDA(cudaEventRecord(h->ev_filt, h->stream));
                     TK_CUDA(cudaStreamWaitEvent(h->aux_stream, h->ev_filt, 0));
