@@ -181,6 +181,39 @@ def test_every_bp_variant_matches_oracle(orc, cuda, case):
         check(L.tk_bp_select_variant(-1))
 
 
+@pytest.mark.parametrize("Z", [40, 10])  # a moved-down last z chunk; a chunk shorter than 16 slices
+def test_quarter_turn_kernel(orc, cuda, Z):
+    """FP16 storage on a square, centred, unflipped volume with N divisible by
+    4 runs the quarter-turn kernel (one geometry for four tiles and four
+    projections); it meets the FP16 bound against FP64 and stays within FP16
+    rounding of the general FP16 walk.  An x flip breaks the symmetry: the
+    general walk runs, bit for bit."""
+    import torch
+
+    L = _lib.load()
+    names = [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
+    h2 = next(i for i, n in enumerate(names) if n.startswith("cimg_h2<f16"))
+    for flip in (0, 1):
+        g = small_geometry(W=64, N=120, H=64, vol=(64, 64, Z), dirx=flip)
+        G = orc.geom_from(g)
+        sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=11), G, "sino")
+        d_in = to_dev(sino, torch)
+        vols = []
+        try:
+            for sel in (-1, h2):
+                _lib.check(L.tk_bp_select_variant(sel))
+                vols.append(device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy())
+        finally:
+            _lib.check(L.tk_bp_select_variant(-1))
+        assert device.device_error_flags() == 0
+        if flip:
+            np.testing.assert_array_equal(vols[0], vols[1])
+        else:
+            assert not np.array_equal(vols[0], vols[1])  # a different kernel ran
+            assert rel_rmse(vols[0], orc.fdk_f64(sino, G)) < F16_RMSE
+            assert rel_rmse(vols[0], vols[1]) < 2e-4
+
+
 def test_packed_variants_equal_scalar(orc, cuda, case):
     """The *_x2 variants walk two slices per step with packed FP32 but do the
     same IEEE operations per voxel as the scalar walk: identical bits."""

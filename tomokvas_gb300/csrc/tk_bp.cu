@@ -472,6 +472,186 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 }
 
 // ---------------------------------------------------------------------------
+// Quarter-turn backprojector (FP16 coefficient images): a circular scan of a
+// square, centred, unflipped volume maps onto itself under a quarter turn.
+// Voxel column (x, y) at angle beta and the column R(x, y) = (X-1-y, x) at
+// beta + 90 degrees have the same S, T, U and u (S' = -aY (-sin) + aX cos = S,
+// T' = aX (-sin) + aY cos = T), so one column geometry, one row coordinate
+// and one floor / fraction / address per slice pair serve four
+// (column, projection) pairs: tile T at projection q and its turns R^k(T) at
+// q + k N/4.  A CTA owns one orbit {T, R(T), R^2(T), R^3(T)} of 16x16-column
+// tiles (T in the first quadrant) and 16 slices; each quarter-turn step
+// stages four boxes at the same footprint origin (projections q + k N/4),
+// one TMA load each on one mbarrier, in slots of CAPB bytes (immediate load
+// offsets).  The walk is update_cimg's FP16 walk 2 with four loads and four
+// accumulator sets per slice pair.  Used when the host has checked that the
+// tabulated angles q + k N/4 are within 1e-5 rad of beta_q + k pi/2.
+template <int CAPB, int STAGES, bool PARTIAL>
+__global__ void __launch_bounds__(256, 2)
+    bp_quad_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
+{
+    constexpr int TX = 16, TY = 16, TZ = 16, NT = TX * TY, ES = 8;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int NQ = P.N / 4;  // quarter-turn steps; projections q + k NQ
+    int2 *boxo = reinterpret_cast<int2 *>(smem + (size_t)STAGES * 4 * CAPB);
+    uint64_t *full = reinterpret_cast<uint64_t *>(boxo + NQ);
+    volatile int &s_abort = *reinterpret_cast<int *>(full + STAGES);
+
+    const int tid = threadIdx.x;
+    const int lx = tid % TX, ly = tid / TX;
+    const int half = P.tilesX / 2;  // tiles per side of a quadrant
+    const int2 tile = tile_of(blockIdx.x, half, half);
+    const int x0 = tile.x * TX, y0 = tile.y * TY;
+    const int zc = blockIdx.y * TZ;
+    const int z0 = PARTIAL ? zc : min(zc, P.nz - TZ);
+    const int zlast = PARTIAL ? P.nz - 1 - z0 : TZ - 1;
+    const int x = x0 + lx, y = y0 + ly;
+    const float aX = P.scale * ((float)x + P.dX);
+    const float aY = P.scale * ((float)y + P.dY);
+    const bool active = sqrtf(aX * aX + aY * aY) < P.halfW;  // the same for the four turned columns
+    const int Xm1 = P.X - 1;
+    // column R^k(x, y) as a volume offset
+    const size_t colk[4] = {(size_t)y * P.X + x, (size_t)x * P.X + (Xm1 - y), (size_t)(Xm1 - y) * P.X + (Xm1 - x),
+                            (size_t)(Xm1 - x) * P.X + y};
+
+    if (!__syncthreads_or(active)) {  // the orbit lies outside the FOV cylinder
+        for (int z = max(zc - z0, 0); z <= zlast; ++z)
+            for (int k = 0; k < 4; ++k) {
+                float *dst = P.vol + (size_t)(z0 + z) * P.slice_stride + colk[k];
+                *dst = P.accumulate ? 0.f + *dst : 0.f;
+            }
+        return;
+    }
+
+    for (int q = tid; q < NQ; q += NT) boxo[q] = footprint_origin_z<TX, TY, 2>(P, q, x0, y0, z0, z0 + zlast);
+    if (tid == 0) {
+        s_abort = 0;
+        for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+        prefetch_tensormap(&tmap);
+    }
+    __syncthreads();
+    const uint32_t box_bytes = (uint32_t)(P.BW * P.BH * ES);
+    const uint32_t smem0 = smem_u32(smem);
+    auto issue = [&](int q, int s) {  // the four boxes of step q into stage s
+        mbar_arrive_expect_tx(&full[s], 4 * box_bytes);
+        for (int k = 0; k < 4; ++k)
+            tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, boxo[q].x * (ES / 4), boxo[q].y, q + k * NQ,
+                        &full[s]);
+    };
+    if (tid == 0)
+        for (int s = 0; s < STAGES && s < NQ; ++s) issue(s, s);
+
+    const float aZ0 = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
+    const float daZ = flip(P.scale, P.dirz);
+    float acc[4][TZ];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int z = 0; z < TZ; ++z) acc[k][z] = 0.f;
+
+    const float cZ = P.cZ, Hm1 = P.Hm1;
+    const uint32_t row_bytes = (uint32_t)P.BW * ES;
+    int q = 0;
+    for (; q < NQ; ++q) {
+        const int s = q % STAGES;
+        const uint32_t parity = (uint32_t)(q / STAGES) & 1u;
+        const bool got = mbar_wait_bounded(&full[s], parity, kWaitLimitNs);
+        if (!got) {
+            atomicOr(P.err, ERR_WAIT_TIMEOUT);
+            s_abort = 1;
+        }
+        if (active && got) {
+            float U, u;
+            column_geometry(aX, aY, P.trig[q], P.D, P.cX, U, u);
+            if (u >= 0.f && u <= P.Wm1) {  // column inside the detector (kernel.cu:127-128)
+                const int bx0 = boxo[q].x, by0 = boxo[q].y;
+                const float fla = __fadd_rd(u, kMagic);
+                const int col = __float_as_int(fla) - kMagicBits - bx0;
+                const float fu = u - (fla - kMagic);
+                const float v0 = slice_v(aZ0, U, cZ);
+                const float dv = __fmul_rn(daZ, U);
+                const float vL = fmaf((float)zlast, dv, v0);
+                const float vlo = fminf(v0, vL), vhi = fmaxf(v0, vL);
+                const int rlo = (int)floorf(vlo) - by0, rhi = (int)floorf(vhi) - by0;
+                if (col >= 0 && col < P.BW && rlo >= 0 && rhi < P.BH) {
+                    const uint32_t sbase = smem0 + (uint32_t)(s * 4) * CAPB + (uint32_t)col * ES -
+                                           (uint32_t)(kMagicBits + by0) * row_bytes;
+                    const float U2 = __fmul_rn(U, U);
+                    const __half2 fuh = __float2half2_rn(fu);
+                    const __half2 U2h2 = __float2half2_rn(U2);
+                    const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
+                    const bool all_in = vlo >= 0.f && vhi <= Hm1;
+#pragma unroll
+                    for (int z = 0; z < TZ; z += 2) {
+                        if (PARTIAL && z > zlast) break;
+                        // past the chunk's last slice (a partial chunk ending on an even slice) the
+                        // pair's second slice repeats the first, whose rows are inside the box, at weight 0
+                        const bool bin = !PARTIAL || z + 1 <= zlast;
+                        const float va = fmaf((float)z, dv, v0);
+                        const float vb = bin ? fmaf((float)(z + 1), dv, v0) : va;
+                        float fla2, flb2, fva, fvb;
+                        floor_frac_x2(va, vb, fla2, flb2, fva, fvb);
+                        const uint32_t ra = (uint32_t)__float_as_int(fla2) * row_bytes + sbase;
+                        const uint32_t rb = (uint32_t)__float_as_int(flb2) * row_bytes + sbase;
+                        const __half2 fv2 = __floats2half2_rn(fva, fvb);
+                        uint32_t w2 = w_all;
+                        if (!all_in)  // kernel.cu:130-131
+                            w2 = ((va >= 0.f && va <= Hm1) ? (w_all & 0xffffu) : 0u) |
+                                 ((vb >= 0.f && vb <= Hm1) ? (w_all & 0xffff0000u) : 0u);
+                        if (!bin) w2 &= 0xffffu;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            uint32_t loa, hia, lob, hib;
+                            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                                         : "=r"(loa), "=r"(hia)
+                                         : "r"(ra + (uint32_t)(k * CAPB)));
+                            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                                         : "=r"(lob), "=r"(hib)
+                                         : "r"(rb + (uint32_t)(k * CAPB)));
+                            const __half2 ha = __hfma2(*reinterpret_cast<const __half2 *>(&hia), fuh,
+                                                       *reinterpret_cast<const __half2 *>(&loa));
+                            const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&hib), fuh,
+                                                       *reinterpret_cast<const __half2 *>(&lob));
+                            const __half2 val = __hfma2(fv2, __highs2half2(ha, hb), __lows2half2(ha, hb));
+                            acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), w2, acc[k][z], acc[k][z + 1]);
+                        }
+                    }
+                } else {
+                    atomicOr(P.err, ERR_BOX_OVERFLOW);
+                }
+            }
+        }
+        __syncthreads();  // every thread is done with stage s
+        if (s_abort) break;
+        if (tid == 0 && q + STAGES < NQ) issue(q + STAGES, s);
+    }
+
+    if (s_abort) {
+        if (tid == 0) {
+            const int issued = min(NQ, q + STAGES);
+            for (int k = q; k < issued; ++k)
+                mbar_wait_bounded(&full[k % STAGES], (uint32_t)(k / STAGES) & 1u, 100000000ull);
+        }
+        __syncthreads();
+        return;
+    }
+
+    const float fs = P.q_scale ? P.fscale / *P.q_scale : P.fscale;
+#pragma unroll
+    for (int z = 0; z < TZ; ++z) {
+        if (z <= zlast && z0 + z >= zc) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float r = active ? acc[k][z] * fs : 0.f;
+                float *dst = P.vol + (size_t)(z0 + z) * P.slice_stride + colk[k];
+                *dst = P.accumulate ? r + *dst : r;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Forward projector: the exact transpose of the bilinear backprojector
 // (bp_tma_kernel, the FP32-sample storage that tk_fdk_forward uses).
 //
@@ -753,7 +933,10 @@ struct BPVariant {
     int precision, TX, TY, TZ, STAGES;
     bool coef;  // coefficient image (bp_cimg_kernel) or raw FP32 samples (bp_tma_kernel)
     const char *name;
+    bool quad = false;  // bp_quad_kernel: needs the quarter-turn symmetry (quad_eligible)
 };
+
+constexpr int kQuadCap = 8192;  // bytes per staged box of the quarter-turn kernel
 
 #define TK_BP_DIRECT(TX, TY, TZ, ST) \
     {reinterpret_cast<const void *>(&bp_tma_kernel<StoreF32, TX, TY, TZ, ST, 2>), nullptr, TK_F32, TX, TY, TZ, ST, \
@@ -770,6 +953,11 @@ struct BPVariant {
     {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB, 1>), \
      reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 1>), P, TX, TY, TZ, ST, true, \
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
+// quarter-turn FP16 kernel (same walk as WALK 2), for symmetric scans only
+#define TK_BP_QUAD(ST) \
+    {reinterpret_cast<const void *>(&bp_quad_kernel<kQuadCap, ST, false>), \
+     reinterpret_cast<const void *>(&bp_quad_kernel<kQuadCap, ST, true>), TK_F16, 16, 16, 16, ST, true, \
+     "quad<f16,16,16,16," #ST ",occ2>", true}
 // FP16 half-math walk (update_cimg WALK 2): not bit-identical to the FP32 walks
 #define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB) \
     {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, 2>), \
@@ -781,6 +969,7 @@ struct BPVariant {
 // storage the half-math walk (FP16 row interpolation, FP32 accumulation).
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT_PK(16, 16, 32, 4),
+    TK_BP_QUAD(3),
     TK_BP_CIMG_H2(16, 16, 64, 3, 2),
     TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
     TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
@@ -840,6 +1029,27 @@ int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ
     return TK_OK;
 }
 
+// The quarter-turn kernel's conditions: a square volume of whole 32-column
+// tile pairs centred on the axis (cx = cy = (X-1)/2 exactly, so a turn maps
+// voxel coordinates onto each other exactly), no x/y flip, all angles in one
+// launch with projection q + k N/4 at beta_q + k pi/2 to within 1e-5 rad
+// (angles as build_trig forms them; 1e-5 rad is 0.01 pixel at 1000 pixels
+// from the axis), and a box that fits its slot.
+static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0)
+{
+    if (g.X != g.Y || g.X % 32 != 0 || g.dirx || g.diry) return false;
+    if (g.cx != g.cy || g.cx != (float)(0.5 * (g.X - 1))) return false;
+    if (g.N % 4 != 0 || g.N > kMaxParamProj) return false;
+    const int nq = g.N / 4;
+    auto beta = [&](int b) { return (double)(float)((float)(angle0 + b) * g.dfi + g.rot); };
+    for (int q = 0; q < nq; ++q)
+        for (int k = 1; k < 4; ++k)
+            if (std::fabs(beta(q + k * nq) - beta(q) - k * (M_PI / 2)) > 1e-5) return false;
+    int BW = 0, BH = 0;
+    if (bp_box_dims(g, nz, zoff, 16, 16, 16, true, 2, &BW, &BH) != TK_OK) return false;
+    return BW * BH * 8 <= kQuadCap;
+}
+
 int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale, int nz,
                        float zoff, float *d_vol, int accumulate, cudaStream_t stream, int angle0)
 {
@@ -852,6 +1062,17 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     if (nz == 0) return TK_OK;
     const BPVariant *v = pick_variant(precision);
     TK_CHECK(v, TK_ERR_INVALID, "backproject: unknown precision %d", precision);
+    if (v->quad && !quad_eligible(g, nz, zoff, angle0)) {  // the format's general walk instead
+        const BPVariant *w = nullptr;
+        for (const auto &c : kVariants)
+            if (c.precision == precision && !c.quad) {
+                w = &c;
+                break;
+            }
+        v = w;
+        TK_CHECK(v, TK_ERR_INVALID, "backproject: no general variant for precision %d", precision);
+    }
+    const bool quad = v->quad;
     auto encode = get_encode_fn();
     TK_CHECK(encode, TK_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
 
@@ -927,11 +1148,13 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
 
-        size_t smem = (size_t)v->STAGES * P.stage_elems * ES;
+        size_t smem = quad ? (size_t)v->STAGES * 4 * kQuadCap : (size_t)v->STAGES * P.stage_elems * ES;
         smem += (size_t)nb * sizeof(int2) + (size_t)v->STAGES * sizeof(uint64_t) + 16;
         TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "backproject: %zu B of shared memory needed", smem);
         TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        dim3 grid((unsigned)(tilesX * tilesY), partial ? 1u : (unsigned)zchunks, 1);
+        // the quarter-turn kernel: one CTA per orbit of four tiles (a first-quadrant tile)
+        const unsigned ntiles = quad ? (unsigned)((tilesX / 2) * (tilesY / 2)) : (unsigned)(tilesX * tilesY);
+        dim3 grid(ntiles, partial ? 1u : (unsigned)zchunks, 1);
         dim3 block((unsigned)(v->TX * v->TY), 1, 1);
         void *args[] = {&tmap, &P};
         TK_CUDA(cudaLaunchKernel(fn, grid, block, args, smem, stream));
