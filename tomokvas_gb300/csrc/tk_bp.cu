@@ -478,23 +478,25 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // beta + 90 degrees have the same S, T, U and u (S' = -aY (-sin) + aX cos = S,
 // T' = aX (-sin) + aY cos = T), so one column geometry, one row coordinate
 // and one floor / fraction / address per slice pair serve four
-// (column, projection) pairs: tile T at projection q and its turns R^k(T) at
-// q + k N/4.  A CTA owns one orbit {T, R(T), R^2(T), R^3(T)} of 16x16-column
-// tiles (T in the first quadrant) and 16 slices; each quarter-turn step
-// stages four boxes at the same footprint origin (projections q + k N/4),
+// (column, projection) pairs: column c of tile T at projection q and its
+// turns R^k(c) at projection (q + k N/4) mod N.  A CTA owns one orbit
+// {T, R(T), R^2(T), R^3(T)} of 16x16-column tiles (T in the first quadrant)
+// and 16 slices, and steps through all N projections q; over the steps each
+// of the four columns sees every projection once.  Step q stages four boxes
+// at T's footprint origin in projection q (projections (q + k N/4) mod N),
 // one TMA load each on one mbarrier, in slots of CAPB bytes (immediate load
 // offsets).  The walk is update_cimg's FP16 walk 2 with four loads and four
 // accumulator sets per slice pair.  Used when the host has checked that the
-// tabulated angles q + k N/4 are within 1e-5 rad of beta_q + k pi/2.
+// tabulated angles (q + k N/4) mod N are within 1e-5 rad of beta_q + k pi/2.
 template <int CAPB, int STAGES, bool PARTIAL>
 __global__ void __launch_bounds__(256, 2)
     bp_quad_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
     constexpr int TX = 16, TY = 16, TZ = 16, NT = TX * TY, ES = 8;
     extern __shared__ __align__(128) unsigned char smem[];
-    const int NQ = P.N / 4;  // quarter-turn steps; projections q + k NQ
+    const int NQ = P.N / 4;  // a quarter turn in projections
     int2 *boxo = reinterpret_cast<int2 *>(smem + (size_t)STAGES * 4 * CAPB);
-    uint64_t *full = reinterpret_cast<uint64_t *>(boxo + NQ);
+    uint64_t *full = reinterpret_cast<uint64_t *>(boxo + P.N);
     volatile int &s_abort = *reinterpret_cast<int *>(full + STAGES);
 
     const int tid = threadIdx.x;
@@ -523,7 +525,7 @@ __global__ void __launch_bounds__(256, 2)
         return;
     }
 
-    for (int q = tid; q < NQ; q += NT) boxo[q] = footprint_origin_z<TX, TY, 2>(P, q, x0, y0, z0, z0 + zlast);
+    for (int q = tid; q < P.N; q += NT) boxo[q] = footprint_origin_z<TX, TY, 2>(P, q, x0, y0, z0, z0 + zlast);
     if (tid == 0) {
         s_abort = 0;
         for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
@@ -535,12 +537,14 @@ __global__ void __launch_bounds__(256, 2)
     const uint32_t smem0 = smem_u32(smem);
     auto issue = [&](int q, int s) {  // the four boxes of step q into stage s
         mbar_arrive_expect_tx(&full[s], 4 * box_bytes);
-        for (int k = 0; k < 4; ++k)
-            tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, boxo[q].x * (ES / 4), boxo[q].y, q + k * NQ,
-                        &full[s]);
+        for (int k = 0; k < 4; ++k) {
+            int pk = q + k * NQ;
+            if (pk >= P.N) pk -= P.N;
+            tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, boxo[q].x * (ES / 4), boxo[q].y, pk, &full[s]);
+        }
     };
     if (tid == 0)
-        for (int s = 0; s < STAGES && s < NQ; ++s) issue(s, s);
+        for (int s = 0; s < STAGES && s < P.N; ++s) issue(s, s);
 
     const float aZ0 = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
     const float daZ = flip(P.scale, P.dirz);
@@ -553,7 +557,7 @@ __global__ void __launch_bounds__(256, 2)
     const float cZ = P.cZ, Hm1 = P.Hm1;
     const uint32_t row_bytes = (uint32_t)P.BW * ES;
     int q = 0;
-    for (; q < NQ; ++q) {
+    for (; q < P.N; ++q) {
         const int s = q % STAGES;
         const uint32_t parity = (uint32_t)(q / STAGES) & 1u;
         const bool got = mbar_wait_bounded(&full[s], parity, kWaitLimitNs);
@@ -624,12 +628,12 @@ __global__ void __launch_bounds__(256, 2)
         }
         __syncthreads();  // every thread is done with stage s
         if (s_abort) break;
-        if (tid == 0 && q + STAGES < NQ) issue(q + STAGES, s);
+        if (tid == 0 && q + STAGES < P.N) issue(q + STAGES, s);
     }
 
     if (s_abort) {
         if (tid == 0) {
-            const int issued = min(NQ, q + STAGES);
+            const int issued = min(P.N, q + STAGES);
             for (int k = q; k < issued; ++k)
                 mbar_wait_bounded(&full[k % STAGES], (uint32_t)(k / STAGES) & 1u, 100000000ull);
         }
@@ -1032,7 +1036,7 @@ int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ
 // The quarter-turn kernel's conditions: a square volume of whole 32-column
 // tile pairs centred on the axis (cx = cy = (X-1)/2 exactly, so a turn maps
 // voxel coordinates onto each other exactly), no x/y flip, all angles in one
-// launch with projection q + k N/4 at beta_q + k pi/2 to within 1e-5 rad
+// launch with projection (q + k N/4) mod N at beta_q + k pi/2 (mod 2 pi) to within 1e-5 rad
 // (angles as build_trig forms them; 1e-5 rad is 0.01 pixel at 1000 pixels
 // from the axis), and a box that fits its slot.
 static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0)
@@ -1042,9 +1046,11 @@ static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0)
     if (g.N % 4 != 0 || g.N > kMaxParamProj) return false;
     const int nq = g.N / 4;
     auto beta = [&](int b) { return (double)(float)((float)(angle0 + b) * g.dfi + g.rot); };
-    for (int q = 0; q < nq; ++q)
-        for (int k = 1; k < 4; ++k)
-            if (std::fabs(beta(q + k * nq) - beta(q) - k * (M_PI / 2)) > 1e-5) return false;
+    for (int q = 0; q < g.N; ++q)
+        for (int k = 1; k < 4; ++k) {
+            const double d = std::remainder(beta((q + k * nq) % g.N) - beta(q) - k * (M_PI / 2), 2 * M_PI);
+            if (std::fabs(d) > 1e-5) return false;
+        }
     int BW = 0, BH = 0;
     if (bp_box_dims(g, nz, zoff, 16, 16, 16, true, 2, &BW, &BH) != TK_OK) return false;
     return BW * BH * 8 <= kQuadCap;
