@@ -586,9 +586,12 @@ __global__ void __launch_bounds__(256, 2)
                     const __half2 U2h2 = __float2half2_rn(U2);
                     const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
                     const bool all_in = vlo >= 0.f && vhi <= Hm1;
-#pragma unroll
-                    for (int z = 0; z < TZ; z += 2) {
-                        if (PARTIAL && z > zlast) break;
+                    // software-pipelined: pair p+1's coordinates, fractions and eight loads are issued
+                    // before pair p's arithmetic, so the loads' latency overlaps it
+                    uint32_t e[2][4][4];  // [buffer][k][lo a, hi a, lo b, hi b]
+                    __half2 fvp[2];
+                    uint32_t wp[2];
+                    auto fetch = [&](int z, int bi) {
                         // past the chunk's last slice (a partial chunk ending on an even slice) the
                         // pair's second slice repeats the first, whose rows are inside the box, at weight 0
                         const bool bin = !PARTIAL || z + 1 <= zlast;
@@ -598,27 +601,37 @@ __global__ void __launch_bounds__(256, 2)
                         floor_frac_x2(va, vb, fla2, flb2, fva, fvb);
                         const uint32_t ra = (uint32_t)__float_as_int(fla2) * row_bytes + sbase;
                         const uint32_t rb = (uint32_t)__float_as_int(flb2) * row_bytes + sbase;
-                        const __half2 fv2 = __floats2half2_rn(fva, fvb);
+                        fvp[bi] = __floats2half2_rn(fva, fvb);
                         uint32_t w2 = w_all;
                         if (!all_in)  // kernel.cu:130-131
                             w2 = ((va >= 0.f && va <= Hm1) ? (w_all & 0xffffu) : 0u) |
                                  ((vb >= 0.f && vb <= Hm1) ? (w_all & 0xffff0000u) : 0u);
                         if (!bin) w2 &= 0xffffu;
+                        wp[bi] = w2;
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
-                            uint32_t loa, hia, lob, hib;
                             asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
-                                         : "=r"(loa), "=r"(hia)
+                                         : "=r"(e[bi][k][0]), "=r"(e[bi][k][1])
                                          : "r"(ra + (uint32_t)(k * CAPB)));
                             asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
-                                         : "=r"(lob), "=r"(hib)
+                                         : "=r"(e[bi][k][2]), "=r"(e[bi][k][3])
                                          : "r"(rb + (uint32_t)(k * CAPB)));
-                            const __half2 ha = __hfma2(*reinterpret_cast<const __half2 *>(&hia), fuh,
-                                                       *reinterpret_cast<const __half2 *>(&loa));
-                            const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&hib), fuh,
-                                                       *reinterpret_cast<const __half2 *>(&lob));
-                            const __half2 val = __hfma2(fv2, __highs2half2(ha, hb), __lows2half2(ha, hb));
-                            acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), w2, acc[k][z], acc[k][z + 1]);
+                        }
+                    };
+                    fetch(0, 0);
+#pragma unroll
+                    for (int z = 0; z < TZ; z += 2) {
+                        if (PARTIAL && z > zlast) break;
+                        const int bi = (z / 2) & 1;
+                        if (z + 2 < TZ && (!PARTIAL || z + 2 <= zlast)) fetch(z + 2, bi ^ 1);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            const __half2 ha = __hfma2(*reinterpret_cast<const __half2 *>(&e[bi][k][1]), fuh,
+                                                       *reinterpret_cast<const __half2 *>(&e[bi][k][0]));
+                            const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&e[bi][k][3]), fuh,
+                                                       *reinterpret_cast<const __half2 *>(&e[bi][k][2]));
+                            const __half2 val = __hfma2(fvp[bi], __highs2half2(ha, hb), __lows2half2(ha, hb));
+                            acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), wp[bi], acc[k][z], acc[k][z + 1]);
                         }
                     }
                 } else {
