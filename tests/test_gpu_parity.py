@@ -533,24 +533,32 @@ def _handle_run(g, data, layout, prec, pipeline, zb, counts=None, after_init=Non
     return out, launches
 
 
-def pipelined_launches(g, nblk, last_slices, zoff=None):
-    """Launches of a pipelined Initialize (tk_fdk_initialize): chunks of
+def pipelined_launches(g, nblk, last_slices, zoff=None, quad=False):
+    """Launches of a pipelined Initialize (tk_fdk_initialize).  Chunks of
     max(32, ceil(N/8)) angles, each a storage-scale and a filter launch; the
     chunks ending by the first quarter of the angles backprojected block by
     block, or in one launch over all blocks when the blocks' slice
     coordinates are those of one launch (float32 arithmetic) and the blocks
     start on 64-slice boundaries; one launch per block over the rest, the
-    last block in two when it holds at least 128 slices."""
-    chunk = max(32, -(-g.N // 8))
-    nch = -(-g.N // chunk)
-    major_end = min(g.N - chunk, chunk * max(1, (nch + 2) // 4))
-    major = sum(1 for b0 in range(0, g.N, chunk) if b0 + min(chunk, g.N - b0) <= major_end)
+    last block in two when it holds at least 128 slices.  With the
+    quarter-turn kernel (quad): C chunks (the first of 8, 6, 5, 4, 3 that
+    divides N/4) of four N/(4C)-angle ranges a quarter turn apart, each range
+    a storage-scale and a filter launch; the first (C + 2) // 4 chunks
+    backprojected together once filtered (one launch, or one per block when
+    not merged), the rest per block as above."""
     split = 1 if (last_slices // 2) // 64 * 64 > 0 else 0
     merged = False
     if zoff is not None and g.zb % 64 == 0:
         f = np.float32
         merged = all(f(z) + f(zoff[n]) == f(n * g.zb + z) + f(zoff[0])
                      for n in range(nblk) for z in range(min(g.zb, g.Z - n * g.zb)))
+    if quad:
+        C = next(c for c in (8, 6, 5, 4, 3) if (g.N // 4) % c == 0)
+        return 8 * C + (1 if merged else nblk) + nblk + split
+    chunk = max(32, -(-g.N // 8))
+    nch = -(-g.N // chunk)
+    major_end = min(g.N - chunk, chunk * max(1, (nch + 2) // 4))
+    major = sum(1 for b0 in range(0, g.N, chunk) if b0 + min(chunk, g.N - b0) <= major_end)
     return 2 * nch + major * (1 if merged else nblk) + nblk + split
 
 
@@ -561,7 +569,10 @@ def pipelined_launches(g, nblk, last_slices, zoff=None):
     ((40, 40, 128), 128, "f16", True, "projection"),  # the last block's launch split at 64 slices
     ((40, 40, 256), 128, "f16", True, "projection"),  # two blocks: first quarter in one launch
     ((40, 40, 40), 16, "f16", True, "sinogram"),      # [H][N][W], packed per chunk by strided copies
-    ((40, 40, 33), 16, "f32", False, "sinogram")])
+    ((40, 40, 33), 16, "f32", False, "sinogram"),
+    ((64, 64, 128), 128, "f16", True, "projection"),  # quarter-turn kernel: 5 chunks of 4 x 15 angles
+    ((64, 64, 256), 128, "f16", True, "projection"),  # quarter-turn, first chunk in one launch
+    ((64, 64, 40), 16, "f16", True, "sinogram")])     # quarter-turn, blocks on two streams
 def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, layout):
     """tk_fdk_set_pipeline: Initialize uploads N = 300 projections in 38-angle
     chunks, filters each as it lands, backprojects the chunks of the first
@@ -569,7 +580,10 @@ def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, la
     then each block over the other 224 angles; CalculateReconstruction only
     delivers blocks.  The volume equals the regular path's to FP32 rounding of
     the partial sums, with the same blocks requested, the same last-slice
-    quirk, and the launches of that schedule."""
+    quirk, and the launches of that schedule.  Square 64-voxel FP16 volumes
+    take the quarter-turn schedule: 5 chunks of four 15-angle ranges a quarter
+    turn apart, filtered on their own stream, the first backprojected once
+    filtered."""
     g = small_geometry(W=48, N=300, H=48, vol=vol_shape, zb=zb)
     G = orc.geom_from(g)
     proj = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=5), G, "proj")  # [N][H][W]
@@ -582,7 +596,8 @@ def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, la
     zoff = orc.zblocks(G)
     nblk = len(zoff)
     last = g.Z - (nblk - 1) * zb if nblk * zb > g.Z else zb
-    assert launches == pipelined_launches(g, nblk, last, zoff)
+    quad = prec == "f16" and vol_shape[0] == vol_shape[1] == 64
+    assert launches == pipelined_launches(g, nblk, last, zoff, quad)
     assert pip.blocks_requested == reg.blocks_requested
     assert rel_rmse(pip.volume, reg.volume) < 1e-6
     assert max_abs(pip.volume, reg.volume) < 1e-5 * np.abs(reg.volume).max()

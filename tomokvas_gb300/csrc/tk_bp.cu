@@ -54,6 +54,7 @@ struct BPParams {
     double halfW;               // W / 2. (kernel.cu:100)
     float fscale;               // dfi * (1/p)  (kernel.cu:113)
     const float *q_scale;       // device storage scale of the filtered projections, or null (= 1)
+    int qbase, qlen;  // quarter-turn kernel: steps q = qbase + (t mod qlen) + (t / qlen) N/4, t < 4 qlen
     float2 trig[kMaxParamProj]; // (cos, sin) per projection (kernel.cu:430-441)
 };
 
@@ -481,9 +482,11 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // (column, projection) pairs: column c of tile T at projection q and its
 // turns R^k(c) at projection (q + k N/4) mod N.  A CTA owns one orbit
 // {T, R(T), R^2(T), R^3(T)} of 16x16-column tiles (T in the first quadrant)
-// and 16 slices, and steps through all N projections q; over the steps each
-// of the four columns sees every projection once.  Step q stages four boxes
-// at T's footprint origin in projection q (projections (q + k N/4) mod N),
+// and 16 slices, and steps through the projections q of an angle set closed
+// under quarter turns (all N, or the quarter-turn images of one range
+// [qbase, qbase + qlen)); over the steps each of the four columns sees every
+// projection of the set once.  Step q stages four boxes at T's footprint
+// origin in projection q (projections (q + k N/4) mod N),
 // one TMA load each on one mbarrier, in slots of CAPB bytes (immediate load
 // offsets).  The walk is update_cimg's FP16 walk 2 with four loads and four
 // accumulator sets per slice pair.  Used when the host has checked that the
@@ -495,8 +498,10 @@ __global__ void __launch_bounds__(256, 2)
     constexpr int TX = 16, TY = 16, TZ = 16, NT = TX * TY, ES = 8;
     extern __shared__ __align__(128) unsigned char smem[];
     const int NQ = P.N / 4;  // a quarter turn in projections
+    const int steps = 4 * P.qlen;
     int2 *boxo = reinterpret_cast<int2 *>(smem + (size_t)STAGES * 4 * CAPB);
-    uint64_t *full = reinterpret_cast<uint64_t *>(boxo + P.N);
+    uint64_t *full = reinterpret_cast<uint64_t *>(boxo + steps);
+    auto qof = [&](int t) { return P.qbase + t % P.qlen + (t / P.qlen) * NQ; };
     volatile int &s_abort = *reinterpret_cast<int *>(full + STAGES);
 
     const int tid = threadIdx.x;
@@ -525,7 +530,7 @@ __global__ void __launch_bounds__(256, 2)
         return;
     }
 
-    for (int q = tid; q < P.N; q += NT) boxo[q] = footprint_origin_z<TX, TY, 2>(P, q, x0, y0, z0, z0 + zlast);
+    for (int t = tid; t < steps; t += NT) boxo[t] = footprint_origin_z<TX, TY, 2>(P, qof(t), x0, y0, z0, z0 + zlast);
     if (tid == 0) {
         s_abort = 0;
         for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
@@ -535,16 +540,24 @@ __global__ void __launch_bounds__(256, 2)
     __syncthreads();
     const uint32_t box_bytes = (uint32_t)(P.BW * P.BH * ES);
     const uint32_t smem0 = smem_u32(smem);
-    auto issue = [&](int q, int s) {  // the four boxes of step q into stage s
+    int qi = P.qbase, ri = 0;  // qof of the next step to issue (thread 0), kept by increments
+    auto issue = [&](int t, int s) {  // the four boxes of step t (projection qi) into stage s
         mbar_arrive_expect_tx(&full[s], 4 * box_bytes);
+        const int q = qi;
+        if (++ri == P.qlen) {
+            ri = 0;
+            qi += NQ - P.qlen + 1;
+        } else {
+            ++qi;
+        }
         for (int k = 0; k < 4; ++k) {
             int pk = q + k * NQ;
             if (pk >= P.N) pk -= P.N;
-            tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, boxo[q].x * (ES / 4), boxo[q].y, pk, &full[s]);
+            tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, boxo[t].x * (ES / 4), boxo[t].y, pk, &full[s]);
         }
     };
     if (tid == 0)
-        for (int s = 0; s < STAGES && s < P.N; ++s) issue(s, s);
+        for (int s = 0; s < STAGES && s < steps; ++s) issue(s, s);
 
     const float aZ0 = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
     const float daZ = flip(P.scale, P.dirz);
@@ -556,10 +569,11 @@ __global__ void __launch_bounds__(256, 2)
 
     const float cZ = P.cZ, Hm1 = P.Hm1;
     const uint32_t row_bytes = (uint32_t)P.BW * ES;
-    int q = 0;
-    for (; q < P.N; ++q) {
-        const int s = q % STAGES;
-        const uint32_t parity = (uint32_t)(q / STAGES) & 1u;
+    int t = 0;
+    int qt = P.qbase, rt = 0;  // qof(t), kept by increments: t mod qlen in rt
+    for (; t < steps; ++t) {
+        const int s = t % STAGES;
+        const uint32_t parity = (uint32_t)(t / STAGES) & 1u;
         const bool got = mbar_wait_bounded(&full[s], parity, kWaitLimitNs);
         if (!got) {
             atomicOr(P.err, ERR_WAIT_TIMEOUT);
@@ -567,9 +581,9 @@ __global__ void __launch_bounds__(256, 2)
         }
         if (active && got) {
             float U, u;
-            column_geometry(aX, aY, P.trig[q], P.D, P.cX, U, u);
+            column_geometry(aX, aY, P.trig[qt], P.D, P.cX, U, u);
             if (u >= 0.f && u <= P.Wm1) {  // column inside the detector (kernel.cu:127-128)
-                const int bx0 = boxo[q].x, by0 = boxo[q].y;
+                const int bx0 = boxo[t].x, by0 = boxo[t].y;
                 const float fla = __fadd_rd(u, kMagic);
                 const int col = __float_as_int(fla) - kMagicBits - bx0;
                 const float fu = u - (fla - kMagic);
@@ -641,13 +655,19 @@ __global__ void __launch_bounds__(256, 2)
         }
         __syncthreads();  // every thread is done with stage s
         if (s_abort) break;
-        if (tid == 0 && q + STAGES < P.N) issue(q + STAGES, s);
+        if (tid == 0 && t + STAGES < steps) issue(t + STAGES, s);
+        if (++rt == P.qlen) {
+            rt = 0;
+            qt += NQ - P.qlen + 1;
+        } else {
+            ++qt;
+        }
     }
 
     if (s_abort) {
         if (tid == 0) {
-            const int issued = min(P.N, q + STAGES);
-            for (int k = q; k < issued; ++k)
+            const int issued = min(steps, t + STAGES);
+            for (int k = t; k < issued; ++k)
                 mbar_wait_bounded(&full[k % STAGES], (uint32_t)(k / STAGES) & 1u, 100000000ull);
         }
         __syncthreads();
@@ -1069,8 +1089,12 @@ static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0)
     return BW * BH * 8 <= kQuadCap;
 }
 
-int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale, int nz,
-                       float zoff, float *d_vol, int accumulate, cudaStream_t stream, int angle0)
+// qlen < 0: the variant the precision picks (the quarter-turn kernel over all
+// angles when the geometry allows it); qlen > 0: the quarter-turn kernel over
+// the quarter-turn images of angles [qbase, qbase + qlen) only.
+static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale, int nz,
+                          float zoff, float *d_vol, int accumulate, cudaStream_t stream, int angle0, int qbase,
+                          int qlen)
 {
     if (int rc = validate_geometry(&g)) return rc;
     TK_CHECK(d_q && d_vol, TK_ERR_INVALID, "backproject: null device pointer");
@@ -1081,7 +1105,17 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     if (nz == 0) return TK_OK;
     const BPVariant *v = pick_variant(precision);
     TK_CHECK(v, TK_ERR_INVALID, "backproject: unknown precision %d", precision);
-    if (v->quad && !quad_eligible(g, nz, zoff, angle0)) {  // the format's general walk instead
+    if (qlen > 0) {  // the quarter-turn kernel on a quarter-turn-closed angle subset
+        v = nullptr;
+        for (const auto &c : kVariants)
+            if (c.precision == precision && c.quad) {
+                v = &c;
+                break;
+            }
+        TK_CHECK(v && quad_eligible(g, nz, zoff, angle0), TK_ERR_UNSUPPORTED,
+                 "backproject: no quarter-turn symmetry for this geometry");
+        TK_CHECK(qbase >= 0 && qbase + qlen <= g.N / 4, TK_ERR_INVALID, "backproject: angle range outside a quarter");
+    } else if (v->quad && !quad_eligible(g, nz, zoff, angle0)) {  // the format's general walk instead
         const BPVariant *w = nullptr;
         for (const auto &c : kVariants)
             if (c.precision == precision && !c.quad) {
@@ -1145,6 +1179,8 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
     // result *= delta_f * scaling, with scaling = 1/p (kernel.cu:113, 575)
     P.fscale = g.dfi * (1.f / (float)p);
     P.q_scale = (precision == TK_F16 || precision == TK_BF16) ? d_q_scale : nullptr;
+    P.qbase = qlen > 0 ? qbase : 0;
+    P.qlen = qlen > 0 ? qlen : g.N / 4;
 
     const bool partial = v->coef && nz < v->TZ;
     const void *fn = partial ? v->fn_partial : v->fn;
@@ -1168,6 +1204,7 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
 
         size_t smem = quad ? (size_t)v->STAGES * 4 * kQuadCap : (size_t)v->STAGES * P.stage_elems * ES;
+        // (the quarter-turn kernel keeps 4 qlen <= nb footprint origins)
         smem += (size_t)nb * sizeof(int2) + (size_t)v->STAGES * sizeof(uint64_t) + 16;
         TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "backproject: %zu B of shared memory needed", smem);
         TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1180,6 +1217,26 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
         count_launch();
     }
     return TK_OK;
+}
+
+int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale, int nz,
+                       float zoff, float *d_vol, int accumulate, cudaStream_t stream, int angle0)
+{
+    return launch_bp_impl(g, d_q, precision, d_q_scale, nz, zoff, d_vol, accumulate, stream, angle0, 0, -1);
+}
+
+bool backproject_quarter_ok(const tk_geometry &g, int precision, int nz, float zoff)
+{
+    if (precision != TK_F16 || nz <= 0) return false;
+    const BPVariant *v = pick_variant(precision);  // honours a selected variant
+    return v && v->quad && quad_eligible(g, nz, zoff, 0);
+}
+
+int launch_backproject_quarter(const tk_geometry &g, const void *d_q, const float *d_q_scale, int nz, float zoff,
+                               float *d_vol, int accumulate, cudaStream_t stream, int qbase, int qlen)
+{
+    TK_CHECK(qlen > 0, TK_ERR_INVALID, "backproject: empty angle range");
+    return launch_bp_impl(g, d_q, TK_F16, d_q_scale, nz, zoff, d_vol, accumulate, stream, 0, qbase, qlen);
 }
 
 int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, float zoff, float *d_qbar,

@@ -372,6 +372,8 @@ struct tk_fdk {
     cudaEvent_t ev_last_half = nullptr;
     // odd Z blocks run on a second stream, so one block's launch fills the tail of another's
     cudaStream_t aux_stream = nullptr;
+    // quarter-turn schedule: the chunks' filters run on their own stream, beside the first launch
+    cudaStream_t filt_stream = nullptr;
     cudaEvent_t ev_filt = nullptr, ev_join = nullptr;
     int in_chunk = 0;  // > 0: sinogram-major input stored as [H][nb][W] blocks of in_chunk angles
 };
@@ -403,6 +405,11 @@ static void release_device(tk_fdk *h)
         cudaStreamDestroy(h->aux_stream);
     }
     h->aux_stream = nullptr;
+    if (h->filt_stream) {
+        cudaStreamSynchronize(h->filt_stream);
+        cudaStreamDestroy(h->filt_stream);
+    }
+    h->filt_stream = nullptr;
     h->reconstructed = false;
     h->in_chunk = 0;
 }
@@ -700,7 +707,38 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
         }
         if (!same) merged_slices = 0;
     }
-    h->in_chunk = overlap && h->layout == TK_LAYOUT_SINOGRAM ? chunk : 0;
+    // Quarter-turn schedule (the FP16 quarter-turn kernel applies to every launch it needs): chunk c
+    // holds the four ranges [c qL + k N/4, + qL), qC chunks of N/4 (the first of 8, 6, 5, 4, 3 that
+    // divides N/4), filtered on their own stream as they land; once the first qE = (qC + 2) / 4
+    // chunks (a quarter to a third of the angles) are filtered, one launch backprojects them while
+    // the other chunks land and filter beside it; then one launch per block over the rest.
+    int qC = 0, qL = 0, qE = 0;
+    if (pipe && g.N % 4 == 0) {
+        for (int c : {8, 6, 5, 4, 3})
+            if ((g.N / 4) % c == 0) {
+                qC = c;
+                break;
+            }
+        bool ok = qC > 0;
+        for (int n = 0; n < nblk && ok; ++n) {
+            int slices = h->zb;
+            if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;
+            ok = backproject_quarter_ok(g, h->precision, slices, zoff[n]);
+            const int split = n == nblk - 1 ? (slices / 2) / 64 * 64 : 0;
+            if (ok && split > 0)
+                ok = backproject_quarter_ok(g, h->precision, split, zoff[n]) &&
+                     backproject_quarter_ok(g, h->precision, slices - split, zoff[n] + (float)split);
+        }
+        if (ok && merged_slices > 0) ok = backproject_quarter_ok(g, h->precision, merged_slices, zoff[0]);
+        if (ok) {
+            qL = g.N / 4 / qC;
+            qE = (qC + 2) / 4;
+            if (!h->filt_stream) TK_CUDA(cudaStreamCreateWithFlags(&h->filt_stream, cudaStreamNonBlocking));
+        } else {
+            qC = 0;
+        }
+    }
+    h->in_chunk = overlap && h->layout == TK_LAYOUT_SINOGRAM ? (qC > 0 ? qL : chunk) : 0;
     if (!overlap)
         TK_CUDA(cudaMemcpyAsync(h->d_in, h->host_in, in_bytes, cudaMemcpyHostToDevice, h->stream));
     if (h->input_type == TK_INPUT_U16) {
@@ -742,55 +780,94 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
         const size_t qframe = filtered_bytes(g, h->precision) / (size_t)g.N;
         const size_t slab = (size_t)g.X * g.Y;
         TK_CUDA(cudaEventRecord(h->ev[2], h->stream));
-        for (int b0 = 0; b0 < g.N; b0 += chunk) {
-            const int nb = std::min(chunk, g.N - b0);
-            const size_t off = (size_t)b0 * frame;
-            if (h->layout == TK_LAYOUT_PROJECTION) {
-                TK_CUDA(cudaMemcpyAsync(static_cast<char *>(h->d_in) + off,
-                                        static_cast<const char *>(h->host_in) + off, (size_t)nb * frame,
-                                        cudaMemcpyHostToDevice, h->copy_stream));
-            } else {
-                const size_t row = frame / (size_t)g.H;  // one detector row of one angle
-                TK_CUDA(cudaMemcpy2DAsync(static_cast<char *>(h->d_in) + off, (size_t)nb * row,
-                                          static_cast<const char *>(h->host_in) + (size_t)b0 * row,
-                                          (size_t)g.N * row, (size_t)nb * row, (size_t)g.H,
-                                          cudaMemcpyHostToDevice, h->copy_stream));
+        // The angle ranges of each chunk, in upload order: one contiguous range, or for the
+        // quarter-turn schedule the four ranges [c qL + k N/4, + qL), a set that a quarter turn maps
+        // onto itself.
+        struct Range {
+            int a, n;
+        };
+        std::vector<std::vector<Range>> chunks;
+        const int nq = g.N / 4;
+        if (qC > 0) {
+            for (int c = 0; c < qC; ++c) {
+                chunks.emplace_back();
+                for (int k = 0; k < 4; ++k) chunks.back().push_back({c * qL + k * nq, qL});
+            }
+        } else {
+            for (int b0 = 0; b0 < g.N; b0 += chunk) chunks.push_back({{b0, std::min(chunk, g.N - b0)}});
+        }
+        // chunks backprojected as they land (contiguous chunks), or together once the last of them is
+        // filtered (quarter-turn chunks)
+        const int early = !pipe ? 0 : (qC > 0 ? qE : major_end / chunk);
+        cudaStream_t fs = qC > 0 ? h->filt_stream : h->stream;  // the filters' stream
+        if (qC > 0) TK_CUDA(cudaStreamWaitEvent(fs, h->ev[8], 0));
+        auto bp_early = [&](int c, int nz, float zo, float *vol, int acc, cudaStream_t st) -> int {
+            if (qC > 0) return launch_backproject_quarter(g, d_q, d_scale, nz, zo, vol, 0, st, 0, qE * qL);
+            const Range r = chunks[c][0];
+            tk_geometry gc = g;
+            gc.N = r.n;
+            return launch_backproject(gc, d_q + (size_t)r.a * qframe, h->precision, d_scale, nz, zo, vol, acc, st,
+                                      r.a);
+        };
+        auto bp_rest = [&](int nz, float zo, float *vol, cudaStream_t st) -> int {
+            if (qC > 0)
+                return launch_backproject_quarter(g, d_q, d_scale, nz, zo, vol, 1, st, qE * qL, (qC - qE) * qL);
+            tk_geometry gr = g;
+            gr.N = g.N - major_end;
+            return launch_backproject(gr, d_q + (size_t)major_end * qframe, h->precision, d_scale, nz, zo, vol, 1,
+                                      st, major_end);
+        };
+        for (int c = 0; c < (int)chunks.size(); ++c) {
+            for (const Range &r : chunks[c]) {
+                const size_t off = (size_t)r.a * frame;
+                if (h->layout == TK_LAYOUT_PROJECTION) {
+                    TK_CUDA(cudaMemcpyAsync(static_cast<char *>(h->d_in) + off,
+                                            static_cast<const char *>(h->host_in) + off, (size_t)r.n * frame,
+                                            cudaMemcpyHostToDevice, h->copy_stream));
+                } else {
+                    const size_t row = frame / (size_t)g.H;  // one detector row of one angle
+                    TK_CUDA(cudaMemcpy2DAsync(static_cast<char *>(h->d_in) + off, (size_t)r.n * row,
+                                              static_cast<const char *>(h->host_in) + (size_t)r.a * row,
+                                              (size_t)g.N * row, (size_t)r.n * row, (size_t)g.H,
+                                              cudaMemcpyHostToDevice, h->copy_stream));
+                }
             }
             TK_CUDA(cudaEventRecord(h->ev[9], h->copy_stream));
-            TK_CUDA(cudaStreamWaitEvent(h->stream, h->ev[9], 0));
-            tk_geometry gc = g;
-            gc.N = nb;
-            if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + off, h->input_type, h->layout, &h->ff,
-                                       h->window, d_q + (size_t)b0 * qframe, h->precision, d_scale, h->stream))
-                return rc;
-            if (pipe && b0 + nb <= major_end && merged_slices > 0) {
-                if (int rc = launch_backproject(gc, d_q + (size_t)b0 * qframe, h->precision, d_scale, merged_slices,
-                                                zoff[0], h->d_vol_full, b0 > 0, h->stream, b0))
+            TK_CUDA(cudaStreamWaitEvent(fs, h->ev[9], 0));
+            for (const Range &r : chunks[c]) {
+                tk_geometry gc = g;
+                gc.N = r.n;
+                if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + (size_t)r.a * frame, h->input_type,
+                                           h->layout, &h->ff, h->window, d_q + (size_t)r.a * qframe, h->precision,
+                                           d_scale, fs))
                     return rc;
-            } else if (pipe && b0 + nb <= major_end) {
-                if (nblk > 1) {  // the odd blocks' stream waits for this chunk's filter
+            }
+            if (qC > 0 && c + 1 != qE) continue;  // the quarter-turn schedule's one early launch follows chunk qE - 1
+            if (qC > 0) {
+                TK_CUDA(cudaEventRecord(h->ev_filt, fs));
+                TK_CUDA(cudaStreamWaitEvent(h->stream, h->ev_filt, 0));
+            }
+            if (c < early && merged_slices > 0) {
+                if (int rc = bp_early(c, merged_slices, zoff[0], h->d_vol_full, c > 0, h->stream)) return rc;
+            } else if (c < early) {
+                if (nblk > 1) {  // the odd blocks' stream waits for this chunk's filters
                     TK_CUDA(cudaEventRecord(h->ev_filt, h->stream));
                     TK_CUDA(cudaStreamWaitEvent(h->aux_stream, h->ev_filt, 0));
                 }
                 for (int n = 0; n < nblk; ++n) {
                     int slices = h->zb;
                     if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;  // kernel.cu:838-840
-                    if (int rc = launch_backproject(gc, d_q + (size_t)b0 * qframe, h->precision, d_scale, slices,
-                                                    zoff[n], h->d_vol_full + (size_t)n * h->zb * slab, b0 > 0,
-                                                    (n & 1) ? h->aux_stream : h->stream, b0))
+                    if (int rc = bp_early(c, slices, zoff[n], h->d_vol_full + (size_t)n * h->zb * slab, c > 0,
+                                          (n & 1) ? h->aux_stream : h->stream))
                         return rc;
                 }
             }
         }
         h->pipe_split = 0;
         if (pipe) {
-            tk_geometry gr = g;
-            gr.N = g.N - major_end;
-            const void *qr = d_q + (size_t)major_end * qframe;
-            if (nblk > 1) {  // the odd blocks' stream waits for the last filter
-                TK_CUDA(cudaEventRecord(h->ev_filt, h->stream));
-                TK_CUDA(cudaStreamWaitEvent(h->aux_stream, h->ev_filt, 0));
-            }
+            TK_CUDA(cudaEventRecord(h->ev_filt, fs));
+            if (qC > 0) TK_CUDA(cudaStreamWaitEvent(h->stream, h->ev_filt, 0));
+            if (nblk > 1) TK_CUDA(cudaStreamWaitEvent(h->aux_stream, h->ev_filt, 0));  // the last filter
             for (int n = 0; n < nblk; ++n) {
                 int slices = h->zb;
                 if ((long long)(n + 1) * h->zb > g.Z) slices = g.Z - n * h->zb;
@@ -800,17 +877,12 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
                 if (split > 0) {
                     if (!h->ev_last_half)
                         TK_CUDA(cudaEventCreateWithFlags(&h->ev_last_half, cudaEventDisableTiming));
-                    if (int rc = launch_backproject(gr, qr, h->precision, d_scale, split, zoff[n], vb, 1, bs,
-                                                    major_end))
-                        return rc;
+                    if (int rc = bp_rest(split, zoff[n], vb, bs)) return rc;
                     TK_CUDA(cudaEventRecord(h->ev_last_half, bs));
-                    if (int rc = launch_backproject(gr, qr, h->precision, d_scale, slices - split,
-                                                    zoff[n] + (float)split, vb + (size_t)split * slab, 1, bs,
-                                                    major_end))
+                    if (int rc = bp_rest(slices - split, zoff[n] + (float)split, vb + (size_t)split * slab, bs))
                         return rc;
                     h->pipe_split = split;
-                } else if (int rc = launch_backproject(gr, qr, h->precision, d_scale, slices, zoff[n], vb, 1, bs,
-                                                       major_end)) {
+                } else if (int rc = bp_rest(slices, zoff[n], vb, bs)) {
                     return rc;
                 }
                 TK_CUDA(cudaEventRecord(h->ev_blocks[n], bs));
