@@ -187,12 +187,18 @@ def test_quarter_turn_kernel(orc, cuda, Z):
     4 runs the quarter-turn kernel (one geometry for four tiles and four
     projections); it meets the FP16 bound against FP64 and stays within FP16
     rounding of the general FP16 walk.  An x flip breaks the symmetry: the
-    general walk runs, bit for bit."""
+    general walk runs, bit for bit.  Every quarter-turn variant (stage
+    count, box capacity, row interpolation by HFMA2 on regrouped halves or by
+    FP16 FMAs on half-selected operands) gives the same bits, and so do the
+    two forms of the general FP16 walk (cimg_h2, cimg_h3)."""
     import torch
 
     L = _lib.load()
     names = [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
     h2 = next(i for i, n in enumerate(names) if n.startswith("cimg_h2<f16"))
+    quads = [i for i, n in enumerate(names) if n.startswith("quad<")]
+    h3 = next(i for i, n in enumerate(names) if n.startswith("cimg_h3<f16"))
+    assert len(quads) >= 2
     for flip in (0, 1):
         g = small_geometry(W=64, N=120, H=64, vol=(64, 64, Z), dirx=flip)
         G = orc.geom_from(g)
@@ -200,12 +206,15 @@ def test_quarter_turn_kernel(orc, cuda, Z):
         d_in = to_dev(sino, torch)
         vols = []
         try:
-            for sel in (-1, h2):
+            for sel in [-1, h2, h3] + quads:
                 _lib.check(L.tk_bp_select_variant(sel))
                 vols.append(device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy())
         finally:
             _lib.check(L.tk_bp_select_variant(-1))
         assert device.device_error_flags() == 0
+        np.testing.assert_array_equal(vols[2], vols[1])
+        for v in vols[3:]:
+            np.testing.assert_array_equal(v, vols[0])
         if flip:
             np.testing.assert_array_equal(vols[0], vols[1])
         else:

@@ -72,9 +72,9 @@ __device__ __forceinline__ int2 batch_footprint(const BatchItem &I, float2 cs, i
     return make_int2(bx, (int)floorf(vmin) - 1);
 }
 
-// WALK as in update_cimg: 2 is the FP16 half-math walk for TK_F16 and the
+// WALK as in update_cimg: 3 is the FP16 half-math walk for TK_F16 and the
 // packed FP32 walk for the other formats (the per-volume defaults).
-template <int PREC, int TX, int TY, int TZ, int STAGES, int MINB, int WALK = 2>
+template <int PREC, int TX, int TY, int TZ, int STAGES, int MINB, int WALK = 3>
 __global__ void __launch_bounds__(TX *TY, MINB)
     bp_batch_kernel(const BatchItem *__restrict__ items, int nitems, int nunits, int *counter, unsigned *err,
                     int maxN, int slot_elems)

@@ -488,10 +488,10 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // projection of the set once.  Step q stages four boxes at T's footprint
 // origin in projection q (projections (q + k N/4) mod N),
 // one TMA load each on one mbarrier, in slots of CAPB bytes (immediate load
-// offsets).  The walk is update_cimg's FP16 walk 2 with four loads and four
+// offsets).  The walk is update_cimg's FP16 walk 3 with four loads and four
 // accumulator sets per slice pair.  Used when the host has checked that the
 // tabulated angles (q + k N/4) mod N are within 1e-5 rad of beta_q + k pi/2.
-template <int CAPB, int STAGES, bool PARTIAL>
+template <int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE>
 __global__ void __launch_bounds__(256, 2)
     bp_quad_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
@@ -502,7 +502,8 @@ __global__ void __launch_bounds__(256, 2)
     int2 *boxo = reinterpret_cast<int2 *>(smem + (size_t)STAGES * 4 * CAPB);
     uint64_t *full = reinterpret_cast<uint64_t *>(boxo + steps);
     auto qof = [&](int t) { return P.qbase + t % P.qlen + (t / P.qlen) * NQ; };
-    volatile int &s_abort = *reinterpret_cast<int *>(full + STAGES);
+    volatile int &s_abort = *reinterpret_cast<volatile int *>(full + STAGES);
+    int *s_issued = reinterpret_cast<int *>(full + STAGES) + 1;  // steps issued so far
 
     const int tid = threadIdx.x;
     const int lx = tid % TX, ly = tid / TX;
@@ -533,16 +534,21 @@ __global__ void __launch_bounds__(256, 2)
     for (int t = tid; t < steps; t += NT) boxo[t] = footprint_origin_z<TX, TY, 2>(P, qof(t), x0, y0, z0, z0 + zlast);
     if (tid == 0) {
         s_abort = 0;
-        for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], 1);
+        *s_issued = min(steps, STAGES);
+        for (int s = 0; s < STAGES; ++s) mbar_init(&full[s], ISSUE == 0 ? 1 : 4);
         fence_mbar_init();
         prefetch_tensormap(&tmap);
     }
     __syncthreads();
     const uint32_t box_bytes = (uint32_t)(P.BW * P.BH * ES);
     const uint32_t smem0 = smem_u32(smem);
-    int qi = P.qbase, ri = 0;  // qof of the next step to issue (thread 0), kept by increments
-    auto issue = [&](int t, int s) {  // the four boxes of step t (projection qi) into stage s
-        mbar_arrive_expect_tx(&full[s], 4 * box_bytes);
+    // ISSUE 0: thread 0 issues a step's four boxes; ISSUE 1: lane 0 of warp k < 4 issues box k
+    // (one arrival with its bytes each, so the stage completes with the fourth), which spreads
+    // the refill's delay after each step's barrier over four warps.
+    const int wid = tid >> 5;
+    const bool issuer = ISSUE == 0 ? tid == 0 : ((tid & 31) == 0 && wid < 4);
+    int qi = P.qbase, ri = 0;  // the issuer's qof of the next step to issue, kept by increments
+    auto issue = [&](int t, int s) {  // the boxes of step t into stage s
         const int q = qi;
         if (++ri == P.qlen) {
             ri = 0;
@@ -550,13 +556,22 @@ __global__ void __launch_bounds__(256, 2)
         } else {
             ++qi;
         }
-        for (int k = 0; k < 4; ++k) {
-            int pk = q + k * NQ;
+        const int2 bo = boxo[t];
+        if (ISSUE == 0) {
+            mbar_arrive_expect_tx(&full[s], 4 * box_bytes);
+            for (int k = 0; k < 4; ++k) {
+                int pk = q + k * NQ;
+                if (pk >= P.N) pk -= P.N;
+                tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, bo.x * (ES / 4), bo.y, pk, &full[s]);
+            }
+        } else {
+            int pk = q + wid * NQ;
             if (pk >= P.N) pk -= P.N;
-            tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, boxo[t].x * (ES / 4), boxo[t].y, pk, &full[s]);
+            mbar_arrive_expect_tx(&full[s], box_bytes);
+            tma_load_3d(smem + (size_t)(s * 4 + wid) * CAPB, &tmap, bo.x * (ES / 4), bo.y, pk, &full[s]);
         }
     };
-    if (tid == 0)
+    if (issuer)
         for (int s = 0; s < STAGES && s < steps; ++s) issue(s, s);
 
     const float aZ0 = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
@@ -569,6 +584,8 @@ __global__ void __launch_bounds__(256, 2)
 
     const float cZ = P.cZ, Hm1 = P.Hm1;
     const uint32_t row_bytes = (uint32_t)P.BW * ES;
+    // A CTA barrier ends each step, then thread 0 refills the stage.  (Releasing stages per warp
+    // instead, with the last warp done refilling, measured 7 % slower.)
     int t = 0;
     int qt = P.qbase, rt = 0;  // qof(t), kept by increments: t mod qlen in rt
     for (; t < steps; ++t) {
@@ -579,7 +596,7 @@ __global__ void __launch_bounds__(256, 2)
             atomicOr(P.err, ERR_WAIT_TIMEOUT);
             s_abort = 1;
         }
-        if (active && got) {
+        if (got && active) {
             float U, u;
             column_geometry(aX, aY, P.trig[qt], P.D, P.cX, U, u);
             if (u >= 0.f && u <= P.Wm1) {  // column inside the detector (kernel.cu:127-128)
@@ -644,8 +661,17 @@ __global__ void __launch_bounds__(256, 2)
                                                        *reinterpret_cast<const __half2 *>(&e[bi][k][0]));
                             const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&e[bi][k][3]), fuh,
                                                        *reinterpret_cast<const __half2 *>(&e[bi][k][2]));
-                            const __half2 val = __hfma2(fvp[bi], __highs2half2(ha, hb), __lows2half2(ha, hb));
-                            acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), wp[bi], acc[k][z], acc[k][z + 1]);
+                            if (ROWI == 0) {
+                                const __half2 val =
+                                    __hfma2(fvp[bi], __highs2half2(ha, hb), __lows2half2(ha, hb));
+                                acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), wp[bi], acc[k][z],
+                                             acc[k][z + 1]);
+                            } else {
+                                row_acc_x2(*reinterpret_cast<const uint32_t *>(&ha),
+                                           *reinterpret_cast<const uint32_t *>(&hb),
+                                           *reinterpret_cast<const uint32_t *>(&fvp[bi]), wp[bi], acc[k][z],
+                                           acc[k][z + 1]);
+                            }
                         }
                     }
                 } else {
@@ -655,7 +681,10 @@ __global__ void __launch_bounds__(256, 2)
         }
         __syncthreads();  // every thread is done with stage s
         if (s_abort) break;
-        if (tid == 0 && t + STAGES < steps) issue(t + STAGES, s);
+        if (issuer && t + STAGES < steps) {
+            issue(t + STAGES, s);
+            if (tid == 0) *s_issued = t + STAGES + 1;
+        }
         if (++rt == P.qlen) {
             rt = 0;
             qt += NQ - P.qlen + 1;
@@ -664,12 +693,11 @@ __global__ void __launch_bounds__(256, 2)
         }
     }
 
-    if (s_abort) {
-        if (tid == 0) {
-            const int issued = min(steps, t + STAGES);
-            for (int k = t; k < issued; ++k)
+    if (s_abort) {  // (every thread left the loop at the same step, after the barrier)
+        const int issued = *s_issued;
+        if (tid == 0)  // the copies in flight land before the CTA's shared memory is released
+            for (int k = max(0, issued - STAGES); k < issued; ++k)
                 mbar_wait_bounded(&full[k % STAGES], (uint32_t)(k / STAGES) & 1u, 100000000ull);
-        }
         __syncthreads();
         return;
     }
@@ -970,10 +998,9 @@ struct BPVariant {
     int precision, TX, TY, TZ, STAGES;
     bool coef;  // coefficient image (bp_cimg_kernel) or raw FP32 samples (bp_tma_kernel)
     const char *name;
-    bool quad = false;  // bp_quad_kernel: needs the quarter-turn symmetry (quad_eligible)
+    int qcap = 0;  // > 0: bp_quad_kernel with staged boxes of up to qcap bytes (needs quad_eligible)
 };
 
-constexpr int kQuadCap = 8192;  // bytes per staged box of the quarter-turn kernel
 
 #define TK_BP_DIRECT(TX, TY, TZ, ST) \
     {reinterpret_cast<const void *>(&bp_tma_kernel<StoreF32, TX, TY, TZ, ST, 2>), nullptr, TK_F32, TX, TY, TZ, ST, \
@@ -990,24 +1017,24 @@ constexpr int kQuadCap = 8192;  // bytes per staged box of the quarter-turn kern
     {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB, 1>), \
      reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 1>), P, TX, TY, TZ, ST, true, \
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
-// quarter-turn FP16 kernel (same walk as WALK 2), for symmetric scans only
-#define TK_BP_QUAD(ST) \
-    {reinterpret_cast<const void *>(&bp_quad_kernel<kQuadCap, ST, false>), \
-     reinterpret_cast<const void *>(&bp_quad_kernel<kQuadCap, ST, true>), TK_F16, 16, 16, 16, ST, true, \
-     "quad<f16,16,16,16," #ST ",occ2>", true}
-// FP16 half-math walk (update_cimg WALK 2): not bit-identical to the FP32 walks
-#define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB) \
-    {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, 2>), \
-     reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, 2>), TK_F16, TX, TY, TZ, ST, \
-     true, "cimg_h2<f16," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
+// quarter-turn FP16 kernel (the walk of WALK 3, or of WALK 2 with ROWI 0), for symmetric scans only
+#define TK_BP_QUAD(CAP, ST, ROWI, ISSUE) \
+    {reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, false, ROWI, ISSUE>), \
+     reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, true, ROWI, ISSUE>), TK_F16, 16, 16, 16, ST, true, \
+     "quad<f16,16,16,16," #ST ",occ2,cap" #CAP ",row" #ROWI ",issue" #ISSUE ">", CAP}
+// FP16 half-math walks (update_cimg WALK 2 and 3, same bits): not bit-identical to the FP32 walks
+#define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB, WK) \
+    {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, WK>), \
+     reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, WK>), TK_F16, TX, TY, TZ, ST, \
+     true, "cimg_h" #WK "<f16," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
 // The first entry of each storage format is its default: the packed walks
 // (same bits as the scalar ones, fewer issued instructions), and for FP16
 // storage the half-math walk (FP16 row interpolation, FP32 accumulation).
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT_PK(16, 16, 32, 4),
-    TK_BP_QUAD(3),
-    TK_BP_CIMG_H2(16, 16, 64, 3, 2),
+    TK_BP_QUAD(8192, 3, 1, 1),
+    TK_BP_CIMG_H2(16, 16, 64, 3, 2, 3),
     TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
     TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
     TK_BP_DIRECT(16, 16, 32, 4),
@@ -1020,6 +1047,9 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
+    TK_BP_QUAD(8192, 3, 1, 0),
+    TK_BP_QUAD(8192, 3, 0, 0),
+    TK_BP_CIMG_H2(16, 16, 64, 3, 2, 2),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
@@ -1072,7 +1102,7 @@ int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ
 // launch with projection (q + k N/4) mod N at beta_q + k pi/2 (mod 2 pi) to within 1e-5 rad
 // (angles as build_trig forms them; 1e-5 rad is 0.01 pixel at 1000 pixels
 // from the axis), and a box that fits its slot.
-static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0)
+static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, int cap)
 {
     if (g.X != g.Y || g.X % 32 != 0 || g.dirx || g.diry) return false;
     if (g.cx != g.cy || g.cx != (float)(0.5 * (g.X - 1))) return false;
@@ -1086,7 +1116,7 @@ static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0)
         }
     int BW = 0, BH = 0;
     if (bp_box_dims(g, nz, zoff, 16, 16, 16, true, 2, &BW, &BH) != TK_OK) return false;
-    return BW * BH * 8 <= kQuadCap;
+    return BW * BH * 8 <= cap;
 }
 
 // qlen < 0: the variant the precision picks (the quarter-turn kernel over all
@@ -1105,27 +1135,29 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
     if (nz == 0) return TK_OK;
     const BPVariant *v = pick_variant(precision);
     TK_CHECK(v, TK_ERR_INVALID, "backproject: unknown precision %d", precision);
-    if (qlen > 0) {  // the quarter-turn kernel on a quarter-turn-closed angle subset
-        v = nullptr;
-        for (const auto &c : kVariants)
-            if (c.precision == precision && c.quad) {
-                v = &c;
-                break;
-            }
-        TK_CHECK(v && quad_eligible(g, nz, zoff, angle0), TK_ERR_UNSUPPORTED,
+    if (qlen > 0) {  // the quarter-turn kernel (the selected one, else the first) on a quarter-turn-closed subset
+        if (!v->qcap) {
+            v = nullptr;
+            for (const auto &c : kVariants)
+                if (c.precision == precision && c.qcap) {
+                    v = &c;
+                    break;
+                }
+        }
+        TK_CHECK(v && quad_eligible(g, nz, zoff, angle0, v->qcap), TK_ERR_UNSUPPORTED,
                  "backproject: no quarter-turn symmetry for this geometry");
         TK_CHECK(qbase >= 0 && qbase + qlen <= g.N / 4, TK_ERR_INVALID, "backproject: angle range outside a quarter");
-    } else if (v->quad && !quad_eligible(g, nz, zoff, angle0)) {  // the format's general walk instead
+    } else if (v->qcap && !quad_eligible(g, nz, zoff, angle0, v->qcap)) {  // the format's general walk instead
         const BPVariant *w = nullptr;
         for (const auto &c : kVariants)
-            if (c.precision == precision && !c.quad) {
+            if (c.precision == precision && !c.qcap) {
                 w = &c;
                 break;
             }
         v = w;
         TK_CHECK(v, TK_ERR_INVALID, "backproject: no general variant for precision %d", precision);
     }
-    const bool quad = v->quad;
+    const bool quad = v->qcap > 0;
     auto encode = get_encode_fn();
     TK_CHECK(encode, TK_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
 
@@ -1203,8 +1235,8 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
 
-        size_t smem = quad ? (size_t)v->STAGES * 4 * kQuadCap : (size_t)v->STAGES * P.stage_elems * ES;
-        // (the quarter-turn kernel keeps 4 qlen <= nb footprint origins)
+        size_t smem = quad ? (size_t)v->STAGES * 4 * v->qcap : (size_t)v->STAGES * P.stage_elems * ES;
+        // (the quarter-turn kernel keeps 4 qlen <= nb footprint origins, and full and empty barriers)
         smem += (size_t)nb * sizeof(int2) + (size_t)v->STAGES * sizeof(uint64_t) + 16;
         TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "backproject: %zu B of shared memory needed", smem);
         TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1229,7 +1261,7 @@ bool backproject_quarter_ok(const tk_geometry &g, int precision, int nz, float z
 {
     if (precision != TK_F16 || nz <= 0) return false;
     const BPVariant *v = pick_variant(precision);  // honours a selected variant
-    return v && v->quad && quad_eligible(g, nz, zoff, 0);
+    return v && v->qcap && quad_eligible(g, nz, zoff, 0, v->qcap);
 }
 
 int launch_backproject_quarter(const tk_geometry &g, const void *d_q, const float *d_q_scale, int nz, float zoff,

@@ -159,6 +159,27 @@ __device__ __forceinline__ void acc_mixed_x2(uint32_t val2, uint32_t w2, float &
         : "r"(val2), "r"(w2));
 }
 
+// The row interpolation and accumulation of two slices from their
+// column-interpolated entries ha = (value, row derivative) of slice a and hb of
+// slice b: acc0 += w.lo * (ha.lo + fv.lo * ha.hi), acc1 += w.hi * (hb.lo +
+// fv.hi * hb.hi), each interpolation one FP16 FMA on half-selected operands (the
+// same roundings as one HFMA2 on the regrouped halves, without regrouping them).
+__device__ __forceinline__ void row_acc_x2(uint32_t ha, uint32_t hb, uint32_t fv2, uint32_t w2, float &acc0,
+                                           float &acc1)
+{
+    asm("{\n\t.reg .b16 al, ah, bl, bh, fa, fb, wa, wb, va, vb;\n\t"
+        "mov.b32 {al, ah}, %2;\n\t"
+        "mov.b32 {bl, bh}, %3;\n\t"
+        "mov.b32 {fa, fb}, %4;\n\t"
+        "mov.b32 {wa, wb}, %5;\n\t"
+        "fma.rn.f16 va, fa, ah, al;\n\t"
+        "fma.rn.f16 vb, fb, bh, bl;\n\t"
+        "fma.rn.f32.f16 %0, wa, va, %0;\n\t"
+        "fma.rn.f32.f16 %1, wb, vb, %1;\n\t}"
+        : "+f"(acc0), "+f"(acc1)
+        : "r"(ha), "r"(hb), "r"(fv2), "r"(w2));
+}
+
 // Walks of a column (WALK):
 //   0  scalar FP32, one slice per step;
 //   1  packed FP32, two slices per step (floor/frac, the row interpolation and
@@ -169,18 +190,21 @@ __device__ __forceinline__ void acc_mixed_x2(uint32_t val2, uint32_t w2, float &
 //      fmaf(z, dv, v0), every 16 pairs (drift below 16 half-ulps of v between
 //      them); floor/frac in FP32 as above;
 //      the column interpolation of both entries by HFMA2, then the row
-//      interpolation of both slices by one HFMA2 with the fractions rounded
-//      to FP16, and the weight U^2 rounded to FP16 applied by fma.rn.f32.f16
-//      into the FP32 accumulators.  Fewer FP32-pipe operations, FP16
-//      rounding of fv, U^2 and the interpolated sample.  (One HFMA2 per slice on
-//      half-broadcast operands instead of the two permutes measured 0.6 %
-//      slower: it needs more registers and spills at 128.)
+//      interpolation of both slices by one HFMA2 on the regrouped halves
+//      (two permutes) with the fractions rounded to FP16, and the weight U^2
+//      rounded to FP16 applied by fma.rn.f32.f16 into the FP32 accumulators.
+//      Fewer FP32-pipe operations, FP16 rounding of fv, U^2 and the
+//      interpolated sample;
+//   3  walk 2 with each slice's row interpolation one FP16 FMA on
+//      half-selected operands (row_acc_x2) instead of the permutes and the
+//      HFMA2: the same roundings, so the same bits, and 4.5 % faster on the
+//      1024^2 x 64-slice slab (the default FP16 walk).
 template <int PREC, int TZ, bool ALL_IN, bool PARTIAL, int WALK = 0>
 __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu,
                                             float U2, float Hm1, int zlast, float (&acc)[TZ])
 {
     const float2 fu2 = pack_fu<PREC>(fu);
-    if constexpr (WALK == 2 && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
+    if constexpr ((WALK == 2 || WALK == 3) && PREC == TK_F16 && !PARTIAL && (TZ % 2 == 0)) {
         const __half2 fuh = *reinterpret_cast<const __half2 *>(&fu2.x);
         const __half2 U2h2 = __float2half2_rn(U2);
         const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
@@ -213,13 +237,19 @@ __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, 
                                        *reinterpret_cast<const __half2 *>(&loa));
             const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&hib), fuh,
                                        *reinterpret_cast<const __half2 *>(&lob));
-            const __half2 val = __hfma2(__floats2half2_rn(fva, fvb), __highs2half2(ha, hb), __lows2half2(ha, hb));
+            const __half2 fv2 = __floats2half2_rn(fva, fvb);
             uint32_t w2 = w_all;
             if constexpr (!ALL_IN) {  // kernel.cu:130-131
                 w2 = ((va >= 0.f && va <= Hm1) ? (w_all & 0xffffu) : 0u) |
                      ((vb >= 0.f && vb <= Hm1) ? (w_all & 0xffff0000u) : 0u);
             }
-            acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), w2, acc[z], acc[z + 1]);
+            if constexpr (WALK == 2) {
+                const __half2 val = __hfma2(fv2, __highs2half2(ha, hb), __lows2half2(ha, hb));
+                acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), w2, acc[z], acc[z + 1]);
+            } else {  // the same roundings on half-selected operands (row_acc_x2)
+                row_acc_x2(*reinterpret_cast<const uint32_t *>(&ha), *reinterpret_cast<const uint32_t *>(&hb),
+                           *reinterpret_cast<const uint32_t *>(&fv2), w2, acc[z], acc[z + 1]);
+            }
         }
     } else if constexpr (WALK >= 1 && !PARTIAL && (TZ % 2 == 0)) {
 #pragma unroll
