@@ -435,7 +435,9 @@ def run_ours(args):
     _lib.check(L.tk_measure_fp32_fma_rate(ctypes.byref(fma_peak)))
     fp32_peak = fma_peak.value
     traffic = None  # DRAM bytes per backprojection launch, from the committed ncu summary
-    tf = os.path.join(ROOT, "profiles", "bp_cimg_h2_f16_1024cube_dram.md")
+    kname = bp_kernel_name(args.variant)  # the traffic capture of the kernel that ran
+    tf = os.path.join(ROOT, "profiles", "bp_quad_f16_1024cube_dram.md" if kname.startswith("bp_quad")
+                      else "bp_cimg_h2_f16_1024cube_dram.md")
     try:
         for line in open(tf):
             if line.startswith("traffic_bytes_per_launch:"):

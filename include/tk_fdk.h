@@ -171,9 +171,14 @@ int tk_fdk_device(const tk_geometry *g, const void *d_in, int input_type, int la
  * pageable memory works but serialises them.  The reference splits the angles
  * into sub-allocations and sums partial volumes ("collecting",
  * kernel.cu:342-371, 849-876); here the volume stays whole in HBM and the
- * projections stream instead.  Returns once the work is enqueued: h_in must
- * stay valid and unchanged until `stream` has passed it.  Allocates nothing
- * on the device (the workspace holds two raw chunks and one filtered chunk). */
+ * projections stream instead.  With FP16 storage on a scan that has the
+ * quarter-turn symmetry (square volume centred on the axis, no flips, N
+ * divisible by 4), a chunk is instead the four ranges of chunk/4 projections
+ * a quarter turn apart, [k chunk/4 + q N/4, + chunk/4), q = 0..3, so that the
+ * quarter-turn backprojector runs on every chunk.  Returns once the work is
+ * enqueued: h_in must stay valid and unchanged until `stream` has passed it.
+ * Allocates nothing on the device (the workspace holds two raw chunks and one
+ * filtered chunk). */
 size_t tk_fdk_stream_workspace_bytes(const tk_geometry *g, int input_type, int precision, int chunk);
 int tk_fdk_stream(const tk_geometry *g, const void *h_in, int input_type, const tk_flatfield *ff, int window,
                   int precision, int chunk, void *d_workspace, size_t workspace_bytes, float *d_vol,

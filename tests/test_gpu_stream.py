@@ -78,3 +78,44 @@ def test_stream_pageable_equals_pinned(case):
     b = device.fdk_stream(g, np.ascontiguousarray(proj), _lib.TK_INPUT_F32, precision=_lib.TK_F16, chunk=30)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+
+
+@pytest.mark.parametrize("chunk", [8, 44, 200])
+def test_stream_quarter_turn_chunks(orc, cuda, chunk):
+    """FP16 storage on a square centred volume with N = 120: each chunk is the
+    four ranges of chunk/4 projections a quarter turn apart (2, 11 with a
+    ragged last chunk of 8, or all 30), backprojected by the quarter-turn
+    kernel from the chunk's compact image.  Raw counts with a scalar flat
+    field (a storage scale known before the data) make every chunk's FP16
+    entries those of the whole image: one chunk is bit-identical to the in-HBM
+    path, more chunks differ by FP32 accumulation order only.  The general FP16
+    walk gives other bits (another kernel ran)."""
+    import torch
+
+    g = small_geometry(W=64, N=120, H=64, vol=(64, 64, 40))
+    G = orc.geom_from(g)
+    proj = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=13), G, "proj")
+    raw = counts_u16(proj, I0, seed=14)
+    ff = device.flatfield(flat_value=I0, A=1.0, B=0.0, invert=True, floor_counts=0.5)
+    d_raw = torch.from_numpy(raw.view(np.int16)).cuda()
+    ref = device.fdk_device(g, d_raw, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff,
+                            window=_lib.TK_WINDOW_HANN, precision=_lib.TK_F16).cpu().numpy()
+    got = device.fdk_stream(g, pinned(raw.view(np.int16), torch), _lib.TK_INPUT_U16, ff=ff,
+                            window=_lib.TK_WINDOW_HANN, precision=_lib.TK_F16, chunk=chunk).cpu().numpy()
+    L = _lib.load()
+    names = [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
+    h3 = next(i for i, n in enumerate(names) if n.startswith("cimg_h3<f16"))
+    try:
+        _lib.check(L.tk_bp_select_variant(h3))
+        general = device.fdk_stream(g, pinned(raw.view(np.int16), torch), _lib.TK_INPUT_U16, ff=ff,
+                                    window=_lib.TK_WINDOW_HANN, precision=_lib.TK_F16,
+                                    chunk=chunk).cpu().numpy()
+    finally:
+        _lib.check(L.tk_bp_select_variant(-1))
+    if chunk >= g.N:
+        np.testing.assert_array_equal(got, ref)
+    else:
+        assert rel_rmse(got, ref) < 2e-6
+    assert not np.array_equal(got, general)
+    assert rel_rmse(got, general) < 2e-4
+    assert device.device_error_flags() == 0

@@ -55,6 +55,7 @@ struct BPParams {
     float fscale;               // dfi * (1/p)  (kernel.cu:113)
     const float *q_scale;       // device storage scale of the filtered projections, or null (= 1)
     int qbase, qlen;  // quarter-turn kernel: steps q = qbase + (t mod qlen) + (t / qlen) N/4, t < 4 qlen
+    int qf0, qfs;     // ... and the image frame of q + k N/4: qf0 + (q - qbase) mod N/4 + quarter * qfs
     float2 trig[kMaxParamProj]; // (cos, sin) per projection (kernel.cu:430-441)
 };
 
@@ -547,28 +548,27 @@ __global__ void __launch_bounds__(256, 2)
     // the refill's delay after each step's barrier over four warps.
     const int wid = tid >> 5;
     const bool issuer = ISSUE == 0 ? tid == 0 : ((tid & 31) == 0 && wid < 4);
-    int qi = P.qbase, ri = 0;  // the issuer's qof of the next step to issue, kept by increments
+    // step t = kk qlen + r is projection q = qbase + r + kk N/4; its k-th box comes from projection
+    // (q + k N/4) mod N, image frame qf0 + r + ((kk + k) mod 4) qfs (the whole image: qf0 = qbase,
+    // qfs = N/4; a compact image of the four ranges: qf0 = 0, qfs = qlen)
+    int ri = 0, kki = 0;  // the issuer's (r, kk) of the next step to issue, kept by increments
     auto issue = [&](int t, int s) {  // the boxes of step t into stage s
-        const int q = qi;
+        const int r = ri, kk = kki;
         if (++ri == P.qlen) {
             ri = 0;
-            qi += NQ - P.qlen + 1;
-        } else {
-            ++qi;
+            ++kki;
         }
         const int2 bo = boxo[t];
         if (ISSUE == 0) {
             mbar_arrive_expect_tx(&full[s], 4 * box_bytes);
             for (int k = 0; k < 4; ++k) {
-                int pk = q + k * NQ;
-                if (pk >= P.N) pk -= P.N;
-                tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, bo.x * (ES / 4), bo.y, pk, &full[s]);
+                const int f = P.qf0 + r + ((kk + k) & 3) * P.qfs;
+                tma_load_3d(smem + (size_t)(s * 4 + k) * CAPB, &tmap, bo.x * (ES / 4), bo.y, f, &full[s]);
             }
         } else {
-            int pk = q + wid * NQ;
-            if (pk >= P.N) pk -= P.N;
+            const int f = P.qf0 + r + ((kk + wid) & 3) * P.qfs;
             mbar_arrive_expect_tx(&full[s], box_bytes);
-            tma_load_3d(smem + (size_t)(s * 4 + wid) * CAPB, &tmap, bo.x * (ES / 4), bo.y, pk, &full[s]);
+            tma_load_3d(smem + (size_t)(s * 4 + wid) * CAPB, &tmap, bo.x * (ES / 4), bo.y, f, &full[s]);
         }
     };
     if (issuer)
@@ -1124,7 +1124,7 @@ static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, 
 // the quarter-turn images of angles [qbase, qbase + qlen) only.
 static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale, int nz,
                           float zoff, float *d_vol, int accumulate, cudaStream_t stream, int angle0, int qbase,
-                          int qlen)
+                          int qlen, bool compact = false)
 {
     if (int rc = validate_geometry(&g)) return rc;
     TK_CHECK(d_q && d_vol, TK_ERR_INVALID, "backproject: null device pointer");
@@ -1213,6 +1213,9 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
     P.q_scale = (precision == TK_F16 || precision == TK_BF16) ? d_q_scale : nullptr;
     P.qbase = qlen > 0 ? qbase : 0;
     P.qlen = qlen > 0 ? qlen : g.N / 4;
+    P.qf0 = compact ? 0 : P.qbase;
+    P.qfs = compact ? P.qlen : g.N / 4;
+    TK_CHECK(!compact || (quad && qlen > 0), TK_ERR_INVALID, "backproject: a compact image needs the quarter-turn kernel");
 
     const bool partial = v->coef && nz < v->TZ;
     const void *fn = partial ? v->fn_partial : v->fn;
@@ -1226,7 +1229,8 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
         const int fpe = v->coef ? ES / 4 : 1;
         CUtensorMap tmap;
         const char *base = static_cast<const char *>(d_q) + (size_t)b0 * g.H * pitch * ES;
-        cuuint64_t dims[3] = {(cuuint64_t)g.W * fpe, (cuuint64_t)g.H, (cuuint64_t)nb};
+        // (a compact quarter-turn image holds the four ranges' 4 qlen frames only)
+        cuuint64_t dims[3] = {(cuuint64_t)g.W * fpe, (cuuint64_t)g.H, (cuuint64_t)(compact ? 4 * P.qlen : nb)};
         cuuint64_t strides[2] = {(cuuint64_t)pitch * ES, (cuuint64_t)pitch * g.H * ES};
         cuuint32_t box[3] = {(cuuint32_t)(BW * fpe), (cuuint32_t)BH, 1};
         cuuint32_t estr[3] = {1, 1, 1};
@@ -1265,10 +1269,10 @@ bool backproject_quarter_ok(const tk_geometry &g, int precision, int nz, float z
 }
 
 int launch_backproject_quarter(const tk_geometry &g, const void *d_q, const float *d_q_scale, int nz, float zoff,
-                               float *d_vol, int accumulate, cudaStream_t stream, int qbase, int qlen)
+                               float *d_vol, int accumulate, cudaStream_t stream, int qbase, int qlen, bool compact)
 {
     TK_CHECK(qlen > 0, TK_ERR_INVALID, "backproject: empty angle range");
-    return launch_bp_impl(g, d_q, TK_F16, d_q_scale, nz, zoff, d_vol, accumulate, stream, 0, qbase, qlen);
+    return launch_bp_impl(g, d_q, TK_F16, d_q_scale, nz, zoff, d_vol, accumulate, stream, 0, qbase, qlen, compact);
 }
 
 int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, float zoff, float *d_qbar,

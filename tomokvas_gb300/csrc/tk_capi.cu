@@ -258,28 +258,51 @@ extern "C" int tk_fdk_stream(const tk_geometry *g, const void *h_in, int input_t
     // copies start only after the caller's earlier work on `stream` (which may use the workspace)
     TK_CUDA(cudaEventRecord(ss.start, st));
     TK_CUDA(cudaStreamWaitEvent(ss.copy, ss.start, 0));
+    const float zoff = tk_default_zoff(g);
+    // Quarter-turn chunks (FP16 storage, a scan with the quarter-turn symmetry): chunk k holds the
+    // four ranges [k L + q N/4, + len), q = 0..3, L = chunk/4, copied one after another, filtered
+    // as one image of 4 len projections and backprojected from that compact image by the
+    // quarter-turn kernel.  Otherwise chunk k is projections [k chunk, + chunk).
+    const int NQ = g->N / 4;
+    const bool quad =
+        precision == TK_F16 && g->N % 4 == 0 && C >= 4 && backproject_quarter_ok(*g, precision, g->Z, zoff);
+    const int L = quad ? C / 4 : 0;
+    const int nch = quad ? (NQ + L - 1) / L : nchunks;
+    auto qlen_of = [&](int k) { return std::min(L, NQ - k * L); };
     auto copy_chunk = [&](int k) -> int {
-        const int b0 = k * C, nb = std::min(C, g->N - b0);
-        TK_CUDA(cudaMemcpyAsync(raw[k & 1], host + (size_t)b0 * frame, (size_t)nb * frame, cudaMemcpyHostToDevice,
-                                ss.copy));
+        if (quad) {
+            const int len = qlen_of(k);
+            for (int q = 0; q < 4; ++q)
+                TK_CUDA(cudaMemcpyAsync(raw[k & 1] + (size_t)q * len * frame, host + (size_t)(k * L + q * NQ) * frame,
+                                        (size_t)len * frame, cudaMemcpyHostToDevice, ss.copy));
+        } else {
+            const int b0 = k * C, nb = std::min(C, g->N - b0);
+            TK_CUDA(cudaMemcpyAsync(raw[k & 1], host + (size_t)b0 * frame, (size_t)nb * frame,
+                                    cudaMemcpyHostToDevice, ss.copy));
+        }
         TK_CUDA(cudaEventRecord(ss.copied[k & 1], ss.copy));
         return TK_OK;
     };
     if (int rc = copy_chunk(0)) return rc;
-    if (nchunks > 1)
+    if (nch > 1)
         if (int rc = copy_chunk(1)) return rc;
-    const float zoff = tk_default_zoff(g);
-    for (int k = 0; k < nchunks; ++k) {
+    for (int k = 0; k < nch; ++k) {
         const int slot = k & 1, b0 = k * C;
         tk_geometry gc = *g;
-        gc.N = std::min(C, g->N - b0);
+        gc.N = quad ? 4 * qlen_of(k) : std::min(C, g->N - b0);
         TK_CUDA(cudaStreamWaitEvent(st, ss.copied[slot], 0));
         if (int rc = launch_filter(gc, raw[slot], input_type, TK_LAYOUT_PROJECTION, ff, window, d_q, precision,
                                    d_scale, st))
             return rc;
         TK_CUDA(cudaEventRecord(ss.consumed[slot], st));
-        if (int rc = launch_backproject(gc, d_q, precision, d_scale, g->Z, zoff, d_vol, k > 0, st, b0)) return rc;
-        if (k + 2 < nchunks) {
+        if (quad) {
+            if (int rc = launch_backproject_quarter(*g, d_q, d_scale, g->Z, zoff, d_vol, k > 0, st, k * L, qlen_of(k),
+                                                    true))
+                return rc;
+        } else if (int rc = launch_backproject(gc, d_q, precision, d_scale, g->Z, zoff, d_vol, k > 0, st, b0)) {
+            return rc;
+        }
+        if (k + 2 < nch) {
             TK_CUDA(cudaStreamWaitEvent(ss.copy, ss.consumed[slot], 0));  // raw[slot] is free again
             if (int rc = copy_chunk(k + 2)) return rc;
         }
