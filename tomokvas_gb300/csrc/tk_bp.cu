@@ -500,8 +500,9 @@ __global__ void __launch_bounds__(256, 2)
     extern __shared__ __align__(128) unsigned char smem[];
     const int NQ = P.N / 4;  // a quarter turn in projections
     const int steps = 4 * P.qlen;
-    int2 *boxo = reinterpret_cast<int2 *>(smem + (size_t)STAGES * 4 * CAPB);
-    uint64_t *full = reinterpret_cast<uint64_t *>(boxo + steps);
+    // footprint origins as 16-bit pairs (the host keeps W, H below 2^14): 4 qlen <= 3200 steps in 12.8 KB
+    short2 *boxo = reinterpret_cast<short2 *>(smem + (size_t)STAGES * 4 * CAPB);
+    uint64_t *full = reinterpret_cast<uint64_t *>(boxo + steps);  // steps = 4 qlen: 8-byte aligned
     auto qof = [&](int t) { return P.qbase + t % P.qlen + (t / P.qlen) * NQ; };
     volatile int &s_abort = *reinterpret_cast<volatile int *>(full + STAGES);
     int *s_issued = reinterpret_cast<int *>(full + STAGES) + 1;  // steps issued so far
@@ -532,7 +533,10 @@ __global__ void __launch_bounds__(256, 2)
         return;
     }
 
-    for (int t = tid; t < steps; t += NT) boxo[t] = footprint_origin_z<TX, TY, 2>(P, qof(t), x0, y0, z0, z0 + zlast);
+    for (int t = tid; t < steps; t += NT) {
+        const int2 o = footprint_origin_z<TX, TY, 2>(P, qof(t), x0, y0, z0, z0 + zlast);
+        boxo[t] = make_short2((short)o.x, (short)o.y);
+    }
     if (tid == 0) {
         s_abort = 0;
         *s_issued = min(steps, STAGES);
@@ -558,7 +562,7 @@ __global__ void __launch_bounds__(256, 2)
             ri = 0;
             ++kki;
         }
-        const int2 bo = boxo[t];
+        const short2 bo = boxo[t];
         if (ISSUE == 0) {
             mbar_arrive_expect_tx(&full[s], 4 * box_bytes);
             for (int k = 0; k < 4; ++k) {
@@ -1105,6 +1109,7 @@ int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ
 static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, int cap)
 {
     if (g.X != g.Y || g.X % 32 != 0 || g.dirx || g.diry) return false;
+    if (g.W >= (1 << 14) || g.H >= (1 << 14)) return false;  // footprint origins kept as 16-bit pairs
     if (g.cx != g.cy || g.cx != (float)(0.5 * (g.X - 1))) return false;
     if (g.N % 4 != 0 || g.N > kMaxParamProj) return false;
     const int nq = g.N / 4;
@@ -1240,8 +1245,8 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
 
         size_t smem = quad ? (size_t)v->STAGES * 4 * v->qcap : (size_t)v->STAGES * P.stage_elems * ES;
-        // (the quarter-turn kernel keeps 4 qlen <= nb footprint origins, and full and empty barriers)
-        smem += (size_t)nb * sizeof(int2) + (size_t)v->STAGES * sizeof(uint64_t) + 16;
+        // (the quarter-turn kernel keeps 4 qlen <= nb footprint origins as 16-bit pairs)
+        smem += (size_t)nb * (quad ? sizeof(short2) : sizeof(int2)) + (size_t)v->STAGES * sizeof(uint64_t) + 16;
         TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "backproject: %zu B of shared memory needed", smem);
         TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         // the quarter-turn kernel: one CTA per orbit of four tiles (a first-quadrant tile)
