@@ -617,19 +617,26 @@ def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, la
         assert rel_rmse(pip.volume, orc.fdk_f32(sino, G)) < (F16_RMSE if prec == "f16" else F32_RMSE)
 
 
-def test_setter_after_pipelined_initialize(orc, cuda):
+@pytest.mark.parametrize("vol_shape,prec,raw", [((40, 40, 40), "f32", False),
+                                               ((64, 64, 40), "f16", True)])  # quarter-turn chunks
+def test_setter_after_pipelined_initialize(orc, cuda, vol_shape, prec, raw):
     """A setter after Initialize (here the window) drops the pipelined volume
     and the filtered projections: the sinogram, stored on the device as
-    per-chunk [H][nb][W] blocks, is unpacked and filtered again, and the
+    per-chunk [H][nb][W] blocks (for the quarter-turn schedule, blocks of the
+    four ranges of each chunk), is unpacked and filtered again, and the
     volume equals a fresh regular run with that window."""
-    g = small_geometry(W=48, N=300, H=48, vol=(40, 40, 40), zb=16)
+    g = small_geometry(W=48, N=300, H=48, vol=vol_shape, zb=16)
     G = orc.geom_from(g)
     sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=7), G, "sino")
+    counts = counts_u16(sino, 60000.0, seed=8) if raw else None
+    data = None if raw else sino
     hann = lambda fbp: fbp.SetFilter("hann")  # noqa: E731
-    changed, launches = _handle_run(g, sino, "sinogram", "f32", True, 16, after_init=hann)
-    fresh, _ = _handle_run(g, sino, "sinogram", "f32", False, 16, window="hann")
-    nblk = len(orc.zblocks(G))
-    assert launches == pipelined_launches(g, nblk, 16) + 2 + nblk  # the pipelined pass, then a regular one
+    changed, launches = _handle_run(g, data, "sinogram", prec, True, 16, counts, after_init=hann)
+    fresh, _ = _handle_run(g, data, "sinogram", prec, False, 16, counts, window="hann")
+    zoff = orc.zblocks(G)
+    nblk = len(zoff)
+    # the pipelined pass, then a regular one
+    assert launches == pipelined_launches(g, nblk, g.Z - (nblk - 1) * 16, zoff, raw) + 2 + nblk
     # the fresh run filters in even 64-angle chunks, which pair FFT rows as one pass does
     assert rel_rmse(changed.volume, fresh.volume) < 1e-7
     assert max_abs(changed.volume, fresh.volume) <= 1e-6 * np.abs(fresh.volume).max()
