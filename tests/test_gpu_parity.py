@@ -223,6 +223,37 @@ def test_quarter_turn_kernel(orc, cuda, Z):
             assert rel_rmse(vols[0], vols[1]) < 2e-4
 
 
+@pytest.mark.parametrize("N,rot,Z", [(8, 0.3, 24),       # two projections per quarter, rotated scan
+                                      (360, 1.0, 40),     # a rotation of about a radian
+                                      (3200, 0.0, 8)])    # the most angles one launch carries
+def test_quarter_turn_kernel_angle_sets(orc, cuda, N, rot, Z):
+    """The quarter-turn kernel on small and large angle sets and with a
+    rotation offset (the angles stay in quarter-turn sets): it runs (other
+    bits than the general FP16 walk) and meets the FP16 bound against FP64."""
+    import torch
+
+    L = _lib.load()
+    names = [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
+    h3 = next(i for i, n in enumerate(names) if n.startswith("cimg_h3<f16"))
+    g = small_geometry(W=64, N=N, H=64, vol=(64, 64, Z), rot=rot)
+    G = orc.geom_from(g)
+    sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=21), G, "sino")
+    d_in = to_dev(sino, torch)
+    vols = []
+    try:
+        for sel in (-1, h3):
+            _lib.check(L.tk_bp_select_variant(sel))
+            vols.append(device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy())
+    finally:
+        _lib.check(L.tk_bp_select_variant(-1))
+    assert device.device_error_flags() == 0
+    assert not np.array_equal(vols[0], vols[1])
+    assert rel_rmse(vols[0], orc.fdk_f64(sino, G)) < F16_RMSE
+    # two FP16 forms: with 8 angles a voxel sums 8 rounded terms, so they differ by up to
+    # the FP16 bound itself (2.4e-4 at N = 8)
+    assert rel_rmse(vols[0], vols[1]) < F16_RMSE
+
+
 def test_packed_variants_equal_scalar(orc, cuda, case):
     """The *_x2 variants walk two slices per step with packed FP32 but do the
     same IEEE operations per voxel as the scalar walk: identical bits."""
