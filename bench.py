@@ -847,7 +847,7 @@ def run_reference_gpu(args):
         emit({"reference_gpu": "unavailable: oracle/_ref/tk_ref_kernels.fatbin missing"})
         return 0
     out = {}
-    for name, seed in (("c1", 1), ("c2", 2)):
+    for name, seed in (("c1", 1), ("c2", 2), ("c4", 4)):
         g = config(name).replace(zb=30)
         from tomokvas_gb300.phantom import random_ellipsoids
 

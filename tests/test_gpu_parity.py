@@ -254,6 +254,36 @@ def test_quarter_turn_kernel_angle_sets(orc, cuda, N, rot, Z):
     assert rel_rmse(vols[0], vols[1]) < F16_RMSE
 
 
+def test_quarter_turn_wide_boxes(orc, cuda):
+    """At scale 1.5 a 16x16x16 tile's footprint (46 x 32 entries, 11.8 KB)
+    exceeds the default quarter-turn kernel's 8 KB slots: with no variant
+    selected the two-stage 13.5 KB form runs (the same bits as selecting it),
+    while selecting the 8 KB form falls back to the general FP16 walk."""
+    import torch
+
+    L = _lib.load()
+    names = [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
+    h3 = next(i for i, n in enumerate(names) if n.startswith("cimg_h3<f16"))
+    narrow = next(i for i, n in enumerate(names) if n.startswith("quad<") and "cap8192" in n)
+    wide = next(i for i, n in enumerate(names) if n.startswith("quad<") and "cap13824" in n)
+    g = small_geometry(W=96, N=120, H=96, vol=(64, 64, 40), voxel_mm=1.2)
+    G = orc.geom_from(g)
+    sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=23), G, "sino")
+    d_in = to_dev(sino, torch)
+    vols = {}
+    try:
+        for sel in (-1, wide, narrow, h3):
+            _lib.check(L.tk_bp_select_variant(sel))
+            vols[sel] = device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy()
+    finally:
+        _lib.check(L.tk_bp_select_variant(-1))
+    assert device.device_error_flags() == 0
+    np.testing.assert_array_equal(vols[-1], vols[wide])
+    np.testing.assert_array_equal(vols[narrow], vols[h3])
+    assert not np.array_equal(vols[-1], vols[h3])
+    assert rel_rmse(vols[-1], orc.fdk_f64(sino, G)) < F16_RMSE
+
+
 def test_packed_variants_equal_scalar(orc, cuda, case):
     """The *_x2 variants walk two slices per step with packed FP32 but do the
     same IEEE operations per voxel as the scalar walk: identical bits."""

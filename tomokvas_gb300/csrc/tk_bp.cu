@@ -1003,6 +1003,7 @@ struct BPVariant {
     bool coef;  // coefficient image (bp_cimg_kernel) or raw FP32 samples (bp_tma_kernel)
     const char *name;
     int qcap = 0;  // > 0: bp_quad_kernel with staged boxes of up to qcap bytes (needs quad_eligible)
+    bool qauto = false;  // a quarter-turn variant the default selection tries, in table order
 };
 
 
@@ -1022,10 +1023,10 @@ struct BPVariant {
      reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 1>), P, TX, TY, TZ, ST, true, \
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 // quarter-turn FP16 kernel (the walk of WALK 3, or of WALK 2 with ROWI 0), for symmetric scans only
-#define TK_BP_QUAD(CAP, ST, ROWI, ISSUE) \
+#define TK_BP_QUAD(CAP, ST, ROWI, ISSUE, AUTO) \
     {reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, false, ROWI, ISSUE>), \
      reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, true, ROWI, ISSUE>), TK_F16, 16, 16, 16, ST, true, \
-     "quad<f16,16,16,16," #ST ",occ2,cap" #CAP ",row" #ROWI ",issue" #ISSUE ">", CAP}
+     "quad<f16,16,16,16," #ST ",occ2,cap" #CAP ",row" #ROWI ",issue" #ISSUE ">", CAP, AUTO}
 // FP16 half-math walks (update_cimg WALK 2 and 3, same bits): not bit-identical to the FP32 walks
 #define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB, WK) \
     {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, WK>), \
@@ -1037,7 +1038,7 @@ struct BPVariant {
 // storage the half-math walk (FP16 row interpolation, FP32 accumulation).
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT_PK(16, 16, 32, 4),
-    TK_BP_QUAD(8192, 3, 1, 1),
+    TK_BP_QUAD(8192, 3, 1, 1, true),
     TK_BP_CIMG_H2(16, 16, 64, 3, 2, 3),
     TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
     TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
@@ -1051,8 +1052,9 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
-    TK_BP_QUAD(8192, 3, 1, 0),
-    TK_BP_QUAD(8192, 3, 0, 0),
+    TK_BP_QUAD(8192, 3, 1, 0, false),
+    TK_BP_QUAD(8192, 3, 0, 0, false),
+    TK_BP_QUAD(13824, 2, 1, 1, true),  // footprints of up to 13.5 KB (scales near 1.5), two stages
     TK_BP_CIMG_H2(16, 16, 64, 3, 2, 2),
 };
 
@@ -1124,6 +1126,20 @@ static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, 
     return BW * BH * 8 <= cap;
 }
 
+// The quarter-turn variant for this launch: the selected variant if it is one
+// (and fits), else, with no selection, the first automatic one whose box
+// capacity holds the tile footprint; nullptr when none applies.
+static const BPVariant *pick_quad(const tk_geometry &g, int precision, int nz, float zoff, int angle0)
+{
+    if (g_variant_override >= 0 && kVariants[g_variant_override].precision == precision) {
+        const BPVariant *v = &kVariants[g_variant_override];
+        return v->qcap && quad_eligible(g, nz, zoff, angle0, v->qcap) ? v : nullptr;
+    }
+    for (const auto &c : kVariants)
+        if (c.precision == precision && c.qcap && c.qauto && quad_eligible(g, nz, zoff, angle0, c.qcap)) return &c;
+    return nullptr;
+}
+
 // qlen < 0: the variant the precision picks (the quarter-turn kernel over all
 // angles when the geometry allows it); qlen > 0: the quarter-turn kernel over
 // the quarter-turn images of angles [qbase, qbase + qlen) only.
@@ -1140,25 +1156,18 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
     if (nz == 0) return TK_OK;
     const BPVariant *v = pick_variant(precision);
     TK_CHECK(v, TK_ERR_INVALID, "backproject: unknown precision %d", precision);
-    if (qlen > 0) {  // the quarter-turn kernel (the selected one, else the first) on a quarter-turn-closed subset
-        if (!v->qcap) {
-            v = nullptr;
+    if (qlen > 0) {  // the quarter-turn kernel on a quarter-turn-closed subset
+        v = pick_quad(g, precision, nz, zoff, angle0);
+        TK_CHECK(v, TK_ERR_UNSUPPORTED, "backproject: no quarter-turn symmetry for this geometry");
+        TK_CHECK(qbase >= 0 && qbase + qlen <= g.N / 4, TK_ERR_INVALID, "backproject: angle range outside a quarter");
+    } else if (v->qcap) {  // a quarter-turn variant that applies, else the format's general walk
+        const BPVariant *w = pick_quad(g, precision, nz, zoff, angle0);
+        if (!w)
             for (const auto &c : kVariants)
-                if (c.precision == precision && c.qcap) {
-                    v = &c;
+                if (c.precision == precision && !c.qcap) {
+                    w = &c;
                     break;
                 }
-        }
-        TK_CHECK(v && quad_eligible(g, nz, zoff, angle0, v->qcap), TK_ERR_UNSUPPORTED,
-                 "backproject: no quarter-turn symmetry for this geometry");
-        TK_CHECK(qbase >= 0 && qbase + qlen <= g.N / 4, TK_ERR_INVALID, "backproject: angle range outside a quarter");
-    } else if (v->qcap && !quad_eligible(g, nz, zoff, angle0, v->qcap)) {  // the format's general walk instead
-        const BPVariant *w = nullptr;
-        for (const auto &c : kVariants)
-            if (c.precision == precision && !c.qcap) {
-                w = &c;
-                break;
-            }
         v = w;
         TK_CHECK(v, TK_ERR_INVALID, "backproject: no general variant for precision %d", precision);
     }
@@ -1270,7 +1279,7 @@ bool backproject_quarter_ok(const tk_geometry &g, int precision, int nz, float z
 {
     if (precision != TK_F16 || nz <= 0) return false;
     const BPVariant *v = pick_variant(precision);  // honours a selected variant
-    return v && v->qcap && quad_eligible(g, nz, zoff, 0, v->qcap);
+    return v && v->qcap && pick_quad(g, precision, nz, zoff, 0) != nullptr;
 }
 
 int launch_backproject_quarter(const tk_geometry &g, const void *d_q, const float *d_q_scale, int nz, float zoff,
