@@ -350,7 +350,11 @@ int tk_fdk_set_stream(tk_fdk *h, void *stream);
  * the angles into a whole-volume device buffer (Z block by Z block, the
  * reference's block offsets) as they land; it then queues one accumulating
  * launch per Z block over the rest (the last block's in two parts) and
- * returns once the host buffer has been read.
+ * returns once the host buffer has been read.  With FP16 storage on a scan
+ * with the quarter-turn symmetry (square volume centred on the axis, no flips,
+ * N divisible by 4) the chunks are sets of four angle ranges a quarter turn
+ * apart, filtered on their own stream, and one launch backprojects the first
+ * quarter to third of the angles once they are filtered.
  * tk_fdk_calculate_reconstruction only delivers the blocks, each copy starting
  * once its block's launch has run, overlapping the next block's launch.  It applies to
  * non-collecting runs with N >= 128 whose storage scale is known up front
