@@ -603,7 +603,7 @@ def _handle_run(g, data, layout, prec, pipeline, zb, counts=None, after_init=Non
     return out, launches
 
 
-def pipelined_launches(g, nblk, last_slices, zoff=None, quad=False):
+def pipelined_launches(g, nblk, last_slices, zoff=None, quad=False, layout="projection"):
     """Launches of a pipelined Initialize (tk_fdk_initialize).  Chunks of
     max(32, ceil(N/8)) angles, each a storage-scale and a filter launch; the
     chunks ending by the first quarter of the angles backprojected block by
@@ -612,8 +612,9 @@ def pipelined_launches(g, nblk, last_slices, zoff=None, quad=False):
     start on 64-slice boundaries; one launch per block over the rest, the
     last block in two when it holds at least 128 slices.  With the
     quarter-turn kernel (quad): C chunks (the first of 8, 6, 5, 4, 3 that
-    divides N/4) of four N/(4C)-angle ranges a quarter turn apart, each range
-    a storage-scale and a filter launch; the first (C + 2) // 4 chunks
+    divides N/4) of four N/(4C)-angle ranges a quarter turn apart, each chunk
+    (detector frames) or each range (sinograms) a storage-scale and a filter
+    launch; the first (C + 2) // 4 chunks
     backprojected together once filtered (one launch, or one per block when
     not merged), the rest per block as above."""
     split = 1 if (last_slices // 2) // 64 * 64 > 0 else 0
@@ -624,7 +625,7 @@ def pipelined_launches(g, nblk, last_slices, zoff=None, quad=False):
                      for n in range(nblk) for z in range(min(g.zb, g.Z - n * g.zb)))
     if quad:
         C = next(c for c in (8, 6, 5, 4, 3) if (g.N // 4) % c == 0)
-        return 8 * C + (1 if merged else nblk) + nblk + split
+        return (2 if layout == "projection" else 8) * C + (1 if merged else nblk) + nblk + split
     chunk = max(32, -(-g.N // 8))
     nch = -(-g.N // chunk)
     major_end = min(g.N - chunk, chunk * max(1, (nch + 2) // 4))
@@ -667,7 +668,7 @@ def test_pipelined_handle_equals_regular(orc, cuda, vol_shape, zb, prec, raw, la
     nblk = len(zoff)
     last = g.Z - (nblk - 1) * zb if nblk * zb > g.Z else zb
     quad = prec == "f16" and vol_shape[0] == vol_shape[1] == 64
-    assert launches == pipelined_launches(g, nblk, last, zoff, quad)
+    assert launches == pipelined_launches(g, nblk, last, zoff, quad, layout)
     assert pip.blocks_requested == reg.blocks_requested
     assert rel_rmse(pip.volume, reg.volume) < 1e-6
     assert max_abs(pip.volume, reg.volume) < 1e-5 * np.abs(reg.volume).max()
@@ -697,7 +698,7 @@ def test_setter_after_pipelined_initialize(orc, cuda, vol_shape, prec, raw):
     zoff = orc.zblocks(G)
     nblk = len(zoff)
     # the pipelined pass, then a regular one
-    assert launches == pipelined_launches(g, nblk, g.Z - (nblk - 1) * 16, zoff, raw) + 2 + nblk
+    assert launches == pipelined_launches(g, nblk, g.Z - (nblk - 1) * 16, zoff, raw, "sinogram") + 2 + nblk
     # the fresh run filters in even 64-angle chunks, which pair FFT rows as one pass does
     assert rel_rmse(changed.volume, fresh.volume) < 1e-7
     assert max_abs(changed.volume, fresh.volume) <= 1e-6 * np.abs(fresh.volume).max()

@@ -732,7 +732,8 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
     }
     // Quarter-turn schedule (the FP16 quarter-turn kernel applies to every launch it needs): chunk c
     // holds the four ranges [c qL + k N/4, + qL), qC chunks of N/4 (the first of 8, 6, 5, 4, 3 that
-    // divides N/4), filtered on their own stream as they land; once the first qE = (qC + 2) / 4
+    // divides N/4), filtered on their own stream as they land (detector frames: one launch over
+    // the chunk's four ranges as frame groups); once the first qE = (qC + 2) / 4
     // chunks (a quarter to a third of the angles) are filtered, one launch backprojects them while
     // the other chunks land and filter beside it; then one launch per block over the rest.
     int qC = 0, qL = 0, qE = 0;
@@ -857,13 +858,22 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
             }
             TK_CUDA(cudaEventRecord(h->ev[9], h->copy_stream));
             TK_CUDA(cudaStreamWaitEvent(fs, h->ev[9], 0));
-            for (const Range &r : chunks[c]) {
+            if (qC > 0 && h->layout == TK_LAYOUT_PROJECTION) {  // the chunk's four ranges in one launch
                 tk_geometry gc = g;
-                gc.N = r.n;
-                if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + (size_t)r.a * frame, h->input_type,
-                                           h->layout, &h->ff, h->window, d_q + (size_t)r.a * qframe, h->precision,
-                                           d_scale, fs))
+                gc.N = 4 * qL;
+                const size_t a = (size_t)c * qL;
+                if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + a * frame, h->input_type, h->layout,
+                                           &h->ff, h->window, d_q + a * qframe, h->precision, d_scale, fs, qL, nq))
                     return rc;
+            } else {
+                for (const Range &r : chunks[c]) {
+                    tk_geometry gc = g;
+                    gc.N = r.n;
+                    if (int rc = launch_filter(gc, static_cast<char *>(h->d_in) + (size_t)r.a * frame,
+                                               h->input_type, h->layout, &h->ff, h->window,
+                                               d_q + (size_t)r.a * qframe, h->precision, d_scale, fs))
+                        return rc;
+                }
             }
             if (qC > 0 && c + 1 != qE) continue;  // the quarter-turn schedule's one early launch follows chunk qE - 1
             if (qC > 0) {

@@ -89,6 +89,7 @@ struct FiltParams {
     int Wp, p, lg, precision;
     int rc, nchunks;        // coefficient image: rows per work unit, units per projection
     long long nunits;
+    int fgrp, fstride;      // coefficient image, frames in groups (> 0): frame f is f/fgrp*fstride + f%fgrp
     int out_layout;         // raw output: TK_LAYOUT_PROJECTION [N][H][Wp] or TK_LAYOUT_SINOGRAM [H][N][Wp]
     int weight_out;         // multiply the output by the cosine weight (the filter's transpose)
     FFTPlan plan;           // passes of the length-p transform (fft_plan(lg))
@@ -597,6 +598,8 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
         const bool valid = unit < P.nunits;
         const long long b = valid ? unit / P.nchunks : 0;
         const int r0 = valid ? (int)(unit - b * P.nchunks) * RC : 0;
+        // the frame of the input and of the output (frame groups: fgrp frames every fstride)
+        const long long bf = P.fgrp > 0 ? b / P.fgrp * P.fstride + b % P.fgrp : b;
         const int r1 = min(r0 + RC, H);         // coefficient rows [r0, r1)
         const int rend = min(r0 + RC, H - 1);   // last filtered row (includes the next unit's first)
         const int npair = valid ? (rend - r0 + 2) / 2 : 0;
@@ -614,8 +617,8 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
             const int qa = r0 + 2 * kk, qb = qa + 1;
             const bool hb = lv && qb <= rend;
             int rr;
-            const long long oa = lv ? in_row_offset(P.L, b * H + qa, rr) : 0;
-            const long long ob = hb ? in_row_offset(P.L, b * H + qb, rr) : 0;
+            const long long oa = lv ? in_row_offset(P.L, bf * H + qa, rr) : 0;
+            const long long ob = hb ? in_row_offset(P.L, bf * H + qb, rr) : 0;
             load_run<NV>(P.L, oa, x0, lv, raw_a);
             load_run<NV>(P.L, ob, x0, hb, raw_b);
         };
@@ -656,7 +659,7 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
             __syncthreads();
             const float2 *Q = fft_forward_c<LG>(R, Sb, twp, t);
             if (live) {
-                const size_t base = (size_t)b * H;
+                const size_t base = (size_t)bf * H;
                 const float zero[3] = {0.f, 0.f, 0.f};
 #pragma unroll
                 for (int i = 0; i < NPR; ++i) {
@@ -870,9 +873,11 @@ static int launch_filter_typed(const FiltParams &P, int p, cudaStream_t stream, 
 }
 
 int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int layout, const tk_flatfield *ff,
-                  int window, void *d_q, int precision, float *d_q_scale, cudaStream_t stream)
+                  int window, void *d_q, int precision, float *d_q_scale, cudaStream_t stream, int fgrp, int fstride)
 {
     if (int rc = validate_geometry(&g)) return rc;
+    TK_CHECK(fgrp <= 0 || (is_coef(precision) && layout == TK_LAYOUT_PROJECTION && fstride >= fgrp), TK_ERR_INVALID,
+             "filter: frame groups need a coefficient image from detector frames");
     TK_CHECK(d_in && d_q, TK_ERR_INVALID, "filter: null device pointer");
     TK_CHECK(input_type == TK_INPUT_F32 || input_type == TK_INPUT_U16, TK_ERR_INVALID, "filter: bad input type");
     TK_CHECK(layout == TK_LAYOUT_SINOGRAM || layout == TK_LAYOUT_PROJECTION, TK_ERR_INVALID, "filter: bad layout");
@@ -880,6 +885,8 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     TK_CHECK(valid_precision(precision), TK_ERR_INVALID, "filter: bad precision");
     const bool sixteen = precision == TK_F16 || precision == TK_BF16;
     TK_CHECK(!sixteen || d_q_scale, TK_ERR_INVALID, "filter: 16-bit storage needs d_q_scale");
+    TK_CHECK(fgrp <= 0 || !sixteen || (input_type == TK_INPUT_U16 && ff && !ff->dark && !ff->flat), TK_ERR_INVALID,
+             "filter: frame groups need a storage scale known without a scan of the data");
     TK_CHECK(input_type == TK_INPUT_F32 || ff, TK_ERR_INVALID, "filter: raw input needs flat-field parameters");
     const int p = reference_pad_length(g.W);
     TK_CHECK(p <= 2 * (kMaxHf - 1), TK_ERR_UNSUPPORTED, "filter: W = %d exceeds the supported 4096", g.W);
@@ -930,6 +937,8 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
     P.rc = 64;
     P.nchunks = (g.H + P.rc - 1) / P.rc;
     P.nunits = (long long)g.N * P.nchunks;
+    P.fgrp = fgrp > 0 ? fgrp : 0;
+    P.fstride = fgrp > 0 ? fstride : 0;
     std::memcpy(P.Hf, sp.Hf.data(), sizeof(float) * sp.Hf.size());
 
     if (!sixteen) {

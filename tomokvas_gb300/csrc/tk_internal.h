@@ -40,9 +40,11 @@ int reference_pad_length(int W);
 void build_trig(const tk_geometry &g, float *cos_out, float *sin_out, int angle0 = 0);
 
 // Launchers (asynchronous on `stream`).
+// fgrp > 0 (coefficient images from detector frames only): the g.N frames
+// come in groups of fgrp, group k at frame k * fstride of d_in and of d_q.
 int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int layout,
                   const tk_flatfield *ff, int window, void *d_q, int precision, float *d_q_scale,
-                  cudaStream_t stream);
+                  cudaStream_t stream, int fgrp = 0, int fstride = 0);
 // d_q holds g.N projections whose angle indices start at angle0 (a chunk of
 // a longer scan when angle0 > 0).
 int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale,
