@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // offsets).  The walk is update_cimg's FP16 walk 3 with four loads and four
 // accumulator sets per slice pair.  Used when the host has checked that the
 // tabulated angles (q + k N/4) mod N are within 1e-5 rad of beta_q + k pi/2.
-template <int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE>
+template <int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE, int GEO = 0>
 __global__ void __launch_bounds__(256, 2)
     bp_quad_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
@@ -588,21 +588,24 @@ __global__ void __launch_bounds__(256, 2)
 
     const float cZ = P.cZ, Hm1 = P.Hm1;
     const uint32_t row_bytes = (uint32_t)P.BW * ES;
-    // A CTA barrier ends each step, then thread 0 refills the stage.  (Releasing stages per warp
-    // instead, with the last warp done refilling, measured 7 % slower.)
+    // A CTA barrier ends each step, then the issuing warps refill the stage.  (Releasing stages
+    // per warp instead, with the last warp done refilling, measured 7 % slower.)  GEO 1: the
+    // step's column geometry (a divide and the trig load) is formed before the stage's wait.
     int t = 0;
     int qt = P.qbase, rt = 0;  // qof(t), kept by increments: t mod qlen in rt
     for (; t < steps; ++t) {
         const int s = t % STAGES;
         const uint32_t parity = (uint32_t)(t / STAGES) & 1u;
+        float Ue = 0.f, ue = 0.f;
+        if constexpr (GEO == 1) column_geometry(aX, aY, P.trig[qt], P.D, P.cX, Ue, ue);  // before the wait
         const bool got = mbar_wait_bounded(&full[s], parity, kWaitLimitNs);
         if (!got) {
             atomicOr(P.err, ERR_WAIT_TIMEOUT);
             s_abort = 1;
         }
         if (got && active) {
-            float U, u;
-            column_geometry(aX, aY, P.trig[qt], P.D, P.cX, U, u);
+            float U = Ue, u = ue;
+            if constexpr (GEO == 0) column_geometry(aX, aY, P.trig[qt], P.D, P.cX, U, u);
             if (u >= 0.f && u <= P.Wm1) {  // column inside the detector (kernel.cu:127-128)
                 const int bx0 = boxo[t].x, by0 = boxo[t].y;
                 const float fla = __fadd_rd(u, kMagic);
@@ -1023,10 +1026,10 @@ struct BPVariant {
      reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 1>), P, TX, TY, TZ, ST, true, \
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 // quarter-turn FP16 kernel (the walk of WALK 3, or of WALK 2 with ROWI 0), for symmetric scans only
-#define TK_BP_QUAD(CAP, ST, ROWI, ISSUE, AUTO) \
-    {reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, false, ROWI, ISSUE>), \
-     reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, true, ROWI, ISSUE>), TK_F16, 16, 16, 16, ST, true, \
-     "quad<f16,16,16,16," #ST ",occ2,cap" #CAP ",row" #ROWI ",issue" #ISSUE ">", CAP, AUTO}
+#define TK_BP_QUAD(CAP, ST, ROWI, ISSUE, AUTO, GEO) \
+    {reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, false, ROWI, ISSUE, GEO>), \
+     reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, true, ROWI, ISSUE, GEO>), TK_F16, 16, 16, 16, ST, true, \
+     "quad<f16,16,16,16," #ST ",occ2,cap" #CAP ",row" #ROWI ",issue" #ISSUE ",geo" #GEO ">", CAP, AUTO}
 // FP16 half-math walks (update_cimg WALK 2 and 3, same bits): not bit-identical to the FP32 walks
 #define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB, WK) \
     {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, WK>), \
@@ -1038,7 +1041,7 @@ struct BPVariant {
 // storage the half-math walk (FP16 row interpolation, FP32 accumulation).
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT_PK(16, 16, 32, 4),
-    TK_BP_QUAD(8192, 3, 1, 1, true),
+    TK_BP_QUAD(8192, 2, 1, 1, true, 1),
     TK_BP_CIMG_H2(16, 16, 64, 3, 2, 3),
     TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
     TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
@@ -1052,9 +1055,11 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
-    TK_BP_QUAD(8192, 3, 1, 0, false),
-    TK_BP_QUAD(8192, 3, 0, 0, false),
-    TK_BP_QUAD(13824, 2, 1, 1, true),  // footprints of up to 13.5 KB (scales near 1.5), two stages
+    TK_BP_QUAD(8192, 3, 1, 0, false, 0),
+    TK_BP_QUAD(8192, 3, 0, 0, false, 0),
+    TK_BP_QUAD(13824, 2, 1, 1, true, 1),  // footprints of up to 13.5 KB (scales near 1.5), two stages
+    TK_BP_QUAD(8192, 3, 1, 1, false, 0),
+    TK_BP_QUAD(8192, 3, 1, 1, false, 1),
     TK_BP_CIMG_H2(16, 16, 64, 3, 2, 2),
 };
 
