@@ -492,11 +492,13 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // offsets).  The walk is update_cimg's FP16 walk 3 with four loads and four
 // accumulator sets per slice pair.  Used when the host has checked that the
 // tabulated angles (q + k N/4) mod N are within 1e-5 rad of beta_q + k pi/2.
-template <int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE, int GEO = 0>
-__global__ void __launch_bounds__(256, 2)
+template <int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE, int GEO = 0, int TYQ = 16>
+__global__ void __launch_bounds__(16 * TYQ, 32 / TYQ)
     bp_quad_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
-    constexpr int TX = 16, TY = 16, TZ = 16, NT = TX * TY, ES = 8;
+    // tiles of 16 x TYQ columns (TYQ 16: 2 CTAs of 8 warps per SM; TYQ 8: 4 CTAs of 4 warps)
+    constexpr int TX = 16, TY = TYQ, TZ = 16, NT = TX * TY, ES = 8;
+    static_assert(ISSUE == 0 || NT / 32 >= 4, "four issuing warps");
     extern __shared__ __align__(128) unsigned char smem[];
     const int NQ = P.N / 4;  // a quarter turn in projections
     const int steps = 4 * P.qlen;
@@ -509,8 +511,7 @@ __global__ void __launch_bounds__(256, 2)
 
     const int tid = threadIdx.x;
     const int lx = tid % TX, ly = tid / TX;
-    const int half = P.tilesX / 2;  // tiles per side of a quadrant
-    const int2 tile = tile_of(blockIdx.x, half, half);
+    const int2 tile = tile_of(blockIdx.x, P.tilesX / 2, P.tilesY / 2);  // a tile of the first quadrant
     const int x0 = tile.x * TX, y0 = tile.y * TY;
     const int zc = blockIdx.y * TZ;
     const int z0 = PARTIAL ? zc : min(zc, P.nz - TZ);
@@ -1026,10 +1027,11 @@ struct BPVariant {
      reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 1>), P, TX, TY, TZ, ST, true, \
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 // quarter-turn FP16 kernel (the walk of WALK 3, or of WALK 2 with ROWI 0), for symmetric scans only
-#define TK_BP_QUAD(CAP, ST, ROWI, ISSUE, AUTO, GEO) \
-    {reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, false, ROWI, ISSUE, GEO>), \
-     reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, true, ROWI, ISSUE, GEO>), TK_F16, 16, 16, 16, ST, true, \
-     "quad<f16,16,16,16," #ST ",occ2,cap" #CAP ",row" #ROWI ",issue" #ISSUE ",geo" #GEO ">", CAP, AUTO}
+#define TK_BP_QUAD_T(CAP, ST, ROWI, ISSUE, AUTO, GEO, TY) \
+    {reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, false, ROWI, ISSUE, GEO, TY>), \
+     reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, true, ROWI, ISSUE, GEO, TY>), TK_F16, 16, TY, 16, ST, true, \
+     "quad<f16,16," #TY ",16," #ST ",cap" #CAP ",row" #ROWI ",issue" #ISSUE ",geo" #GEO ">", CAP, AUTO}
+#define TK_BP_QUAD(CAP, ST, ROWI, ISSUE, AUTO, GEO) TK_BP_QUAD_T(CAP, ST, ROWI, ISSUE, AUTO, GEO, 16)
 // FP16 half-math walks (update_cimg WALK 2 and 3, same bits): not bit-identical to the FP32 walks
 #define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB, WK) \
     {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, WK>), \
@@ -1041,7 +1043,7 @@ struct BPVariant {
 // storage the half-math walk (FP16 row interpolation, FP32 accumulation).
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT_PK(16, 16, 32, 4),
-    TK_BP_QUAD(8192, 2, 1, 1, true, 1),
+    TK_BP_QUAD_T(6144, 2, 1, 1, true, 1, 8),
     TK_BP_CIMG_H2(16, 16, 64, 3, 2, 3),
     TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
     TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
@@ -1057,6 +1059,7 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
     TK_BP_QUAD(8192, 3, 1, 0, false, 0),
     TK_BP_QUAD(8192, 3, 0, 0, false, 0),
+    TK_BP_QUAD(8192, 2, 1, 1, true, 1),    // 16 x 16 tiles when a 16 x 8 tile's footprint exceeds 6 KB
     TK_BP_QUAD(13824, 2, 1, 1, true, 1),  // footprints of up to 13.5 KB (scales near 1.5), two stages
     TK_BP_QUAD(8192, 3, 1, 1, false, 0),
     TK_BP_QUAD(8192, 3, 1, 1, false, 1),
@@ -1113,7 +1116,7 @@ int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ
 // launch with projection (q + k N/4) mod N at beta_q + k pi/2 (mod 2 pi) to within 1e-5 rad
 // (angles as build_trig forms them; 1e-5 rad is 0.01 pixel at 1000 pixels
 // from the axis), and a box that fits its slot.
-static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, int cap)
+static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, int cap, int TY = 16)
 {
     if (g.X != g.Y || g.X % 32 != 0 || g.dirx || g.diry) return false;
     if (g.W >= (1 << 14) || g.H >= (1 << 14)) return false;  // footprint origins kept as 16-bit pairs
@@ -1127,7 +1130,7 @@ static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, 
             if (std::fabs(d) > 1e-5) return false;
         }
     int BW = 0, BH = 0;
-    if (bp_box_dims(g, nz, zoff, 16, 16, 16, true, 2, &BW, &BH) != TK_OK) return false;
+    if (bp_box_dims(g, nz, zoff, 16, TY, 16, true, 2, &BW, &BH) != TK_OK) return false;
     return BW * BH * 8 <= cap;
 }
 
@@ -1138,10 +1141,10 @@ static const BPVariant *pick_quad(const tk_geometry &g, int precision, int nz, f
 {
     if (g_variant_override >= 0 && kVariants[g_variant_override].precision == precision) {
         const BPVariant *v = &kVariants[g_variant_override];
-        return v->qcap && quad_eligible(g, nz, zoff, angle0, v->qcap) ? v : nullptr;
+        return v->qcap && quad_eligible(g, nz, zoff, angle0, v->qcap, v->TY) ? v : nullptr;
     }
     for (const auto &c : kVariants)
-        if (c.precision == precision && c.qcap && c.qauto && quad_eligible(g, nz, zoff, angle0, c.qcap)) return &c;
+        if (c.precision == precision && c.qcap && c.qauto && quad_eligible(g, nz, zoff, angle0, c.qcap, c.TY)) return &c;
     return nullptr;
 }
 
