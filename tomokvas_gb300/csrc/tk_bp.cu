@@ -1040,7 +1040,10 @@ struct BPVariant {
 
 // The first entry of each storage format is its default: the packed walks
 // (same bits as the scalar ones, fewer issued instructions), and for FP16
-// storage the half-math walk (FP16 row interpolation, FP32 accumulation).
+// storage the quarter-turn kernel (16 x 8 tiles), whose automatic alternatives
+// (qauto, in table order) take larger footprints, and otherwise the first
+// general entry, the half-math walk 3 (FP16 row interpolation, FP32
+// accumulation).
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT_PK(16, 16, 32, 4),
     TK_BP_QUAD_T(6144, 2, 1, 1, true, 1, 8),
