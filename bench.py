@@ -40,14 +40,47 @@ CPU_SAMPLE_SLICES = (508, 509, 510, 511, 512, 513, 514, 515)
 RMSE_SLICES = ((480, 512, 544), (1010,))
 
 
-def bp_kernel_name(variant):
-    """Name of the FP16 backprojection variant the chosen form runs (the selected one, else the default)."""
+def bp_kernel_name(variant, precision=None):
+    """Name of the backprojection variant a storage format runs at 1024^3 (the selected one, else the
+    format's default, a quarter-turn kernel for this symmetric scan)."""
     from tomokvas_gb300 import _lib
 
     L = _lib.load()
-    if variant < 0:
-        variant = next(i for i in range(L.tk_bp_variant_count()) if L.tk_bp_variant_precision(i) == _lib.TK_F16)
+    precision = _lib.TK_F16 if precision is None else precision
+    if variant < 0 or L.tk_bp_variant_precision(variant) != precision:
+        variant = next(i for i in range(L.tk_bp_variant_count()) if L.tk_bp_variant_precision(i) == precision)
     return "bp_" + L.tk_bp_variant_name(variant).decode()
+
+
+def half_math_variant():
+    """Index of the selectable FP16 half-math quarter-turn kernel (16 x 8 tiles; FP16 interpolation
+    arithmetic), reported beside the headline, never as it."""
+    from tomokvas_gb300 import _lib
+
+    L = _lib.load()
+    return next(i for i in range(L.tk_bp_variant_count())
+                if L.tk_bp_variant_name(i).decode().startswith("quad<f16,16,8,") and ",h16row1," in
+                L.tk_bp_variant_name(i).decode())
+
+
+# DRAM traffic of the default FP16 backprojection kernel: dram__bytes_read.sum + dram__bytes_write.sum
+# of one launch on the 64-slice, 180-projection slab case (bench.py --profile-bp f16, one ncu pass),
+# scaled to the 1024^3 / 720-projection launch by the ratio of voxel-projection updates (64: 16x the
+# z chunks, each streaming 4x the projections).  source_sha1 is the sha1 of tk_bp.cu + tk_bp_core.cuh
+# at capture: a later source reports the traffic as stale (null) instead of a frozen number.
+BP_TRAFFIC = {"kernel": None, "slab_bytes": None, "scale": 64, "source_sha1": None,
+              "capture": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none "
+                         "-k regex:bp_quad -c 1 python bench.py --profile-bp f16"}
+
+
+def bp_source_sha1():
+    import hashlib
+
+    h = hashlib.sha1()
+    for f in ("tk_bp.cu", "tk_bp_core.cuh"):
+        with open(os.path.join(ROOT, "tomokvas_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()
 
 
 def parse():
@@ -329,16 +362,32 @@ def run_ours(args):
         return total_ms / steps, statistics.mean(filt), statistics.mean(bp), clocks
 
     K, W = args.steps, args.warmup
+
+    def slices():
+        return {tuple(zs): vol[torch.tensor(zs, device="cuda")].cpu().numpy() for zs in RMSE_SLICES}
+
+    # chosen form: FP16 storage, FP32 interpolation (the default FP16 kernel)
     ms16, f16_filter, f16_bp, clocks = timed(_lib.TK_F16, K, W, sample_clocks=(rank == 0))
-    vol16 = {tuple(zs): vol[torch.tensor(zs, device="cuda")].cpu().numpy() for zs in RMSE_SLICES}
+    vol16 = slices()
     # plain form: the faster of the two FP32 storage formats (samples / coefficients)
     plain_runs = {}
     for pname, pcode in (("f32", _lib.TK_F32), ("f32c", _lib.TK_F32_COEF)):
         r = timed(pcode, K, W)
-        plain_runs[pname] = (r, {tuple(zs): vol[torch.tensor(zs, device="cuda")].cpu().numpy() for zs in RMSE_SLICES})
+        plain_runs[pname] = (r, slices())
     plain_name = min(plain_runs, key=lambda k: plain_runs[k][0][0])
     (ms32, f32_filter, f32_bp, _), vol32 = plain_runs[plain_name]
-    plain_alt = {k: {"ms_per_step": v[0][0], "bp_ms": v[0][2], "filter_ms": v[0][1]} for k, v in plain_runs.items()}
+    plain_code = _lib.TK_F32 if plain_name == "f32" else _lib.TK_F32_COEF
+    plain_alt = {k: {"ms_per_step": v[0][0], "bp_ms": v[0][2], "filter_ms": v[0][1],
+                     "kernel": bp_kernel_name(-1, _lib.TK_F32 if k == "f32" else _lib.TK_F32_COEF)}
+                 for k, v in plain_runs.items()}
+    # the selectable FP16 half-math form (FP16 interpolation arithmetic): reported beside, not the headline
+    hm = half_math_variant()
+    _lib.check(L.tk_bp_select_variant(hm))
+    try:
+        ms_hm, hm_filter, hm_bp, _ = timed(_lib.TK_F16, K, W)
+        vol_hm = slices()
+    finally:
+        _lib.check(L.tk_bp_select_variant(args.variant))
     value = replica_gups(upd, world, ms16 * 1e-3)
     plain = replica_gups(upd, world, ms32 * 1e-3)
     flags = device.device_error_flags()
@@ -417,14 +466,16 @@ def run_ours(args):
         G = orc.geom_from(g)
         raw_np = raw.cpu().numpy().view(np.uint16)
         sino = orc.log_u16(raw_np, np.float32(I0))
-        num16 = num32 = den = 0.0
+        num16 = num32 = numhm = den = 0.0
         for zs in RMSE_SLICES:
             ref = orc.fdk_f64(sino, G, "hann", np.array(zs, dtype=np.int32))
             num16 += float(np.sum((vol16[tuple(zs)] - ref) ** 2))
             num32 += float(np.sum((vol32[tuple(zs)] - ref) ** 2))
+            numhm += float(np.sum((vol_hm[tuple(zs)] - ref) ** 2))
             den += float(np.sum(ref ** 2))
         del sino
         rmse = {"chosen_f16_vs_fp64": (num16 / den) ** 0.5, "plain_f32_vs_fp64": (num32 / den) ** 0.5,
+                "half_math_f16_vs_fp64": (numhm / den) ** 0.5,
                 "slices": [z for zs in RMSE_SLICES for z in zs], "metric": "relative RMSE"}
 
     cores = os.cpu_count() or 1
@@ -434,16 +485,15 @@ def run_ours(args):
     fma_peak = ctypes.c_double(0.0)
     _lib.check(L.tk_measure_fp32_fma_rate(ctypes.byref(fma_peak)))
     fp32_peak = fma_peak.value
-    traffic = None  # DRAM bytes per backprojection launch, from the committed ncu summary
-    kname = bp_kernel_name(args.variant)  # the traffic capture of the kernel that ran
-    tf = os.path.join(ROOT, "profiles", "bp_quad_f16_1024cube_dram.md" if kname.startswith("bp_quad")
-                      else "bp_cimg_h2_f16_1024cube_dram.md")
-    try:
-        for line in open(tf):
-            if line.startswith("traffic_bytes_per_launch:"):
-                traffic = int(line.split(":", 1)[1])
-    except (OSError, ValueError):
-        traffic = None
+    kname = bp_kernel_name(args.variant)
+    traffic, traffic_note = None, "no capture recorded for this kernel"
+    if BP_TRAFFIC["kernel"] == kname and BP_TRAFFIC["slab_bytes"]:
+        if BP_TRAFFIC["source_sha1"] == bp_source_sha1():
+            traffic = int(BP_TRAFFIC["slab_bytes"] * BP_TRAFFIC["scale"])
+            traffic_note = (f"ncu capture of the 64-slice / 180-projection slab case scaled x{BP_TRAFFIC['scale']} "
+                            f"by updates; {BP_TRAFFIC['capture']}")
+        else:
+            traffic_note = "stale: the backprojection source changed after the capture"
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -454,13 +504,24 @@ def run_ours(args):
     out = {
         "metric": "GUPS", "value": value, "unit": "GUPS", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": ms16, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f16-stored filtered projections, f16 row interpolation, f32 geometry and accumulation", "data": "synthetic: seeded 40-ellipsoid phantom, "
+        "dtype": "f16-stored filtered projections (bilinear coefficient image, 8 B/entry); f32 geometry, "
+                 "f32 bilinear interpolation (16-bit values converted exactly to f32), f32 U^2 weighting and "
+                 "accumulation", "data": "synthetic: seeded 40-ellipsoid phantom, "
         "Poisson counts I0=60000 (no dataset)", "config": CONFIG,
         "s_per_volume": ms16 * 1e-3,
+        "kernel": kname,
         "plain": {"value": plain, "unit": "GUPS", "ms_per_step": ms32, "s_per_volume": ms32 * 1e-3,
                   "dtype": "f32 math, f32-stored filtered projections", "storage": plain_name,
+                  "kernel": plain_alt[plain_name]["kernel"],
                   "filter_ms": f32_filter, "bp_ms": f32_bp, "formats": plain_alt},
         "chosen_vs_plain": plain and value / plain,
+        "chosen_vs_plain_kernels": [kname, plain_alt[plain_name]["kernel"]],
+        "half_math": {"value": replica_gups(upd, world, ms_hm * 1e-3), "unit": "GUPS", "ms_per_step": ms_hm,
+                      "bp_ms": hm_bp, "filter_ms": hm_filter, "kernel": bp_kernel_name(hm),
+                      "dtype": "f16 storage with f16 interpolation arithmetic (HFMA2 column and FP16 row "
+                               "interpolation, U^2 rounded to f16, f32 accumulation): a selectable form, not "
+                               "the headline",
+                      "rmse_vs_fp64": rmse and rmse["half_math_f16_vs_fp64"]},
         "stages_ms": {"filter": f16_filter, "backprojection": f16_bp},
         "rmse": rmse,
         "e2e": e2e,
@@ -468,7 +529,7 @@ def run_ours(args):
         "device_error_flags": flags,
         "roofline": {"bound": "fp32", "kernel": bp_kernel_name(args.variant),
                      "achieved": bp_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": bp_tflops / fp32_peak, "traffic": traffic,
+                     "frac": bp_tflops / fp32_peak, "traffic": traffic, "traffic_note": traffic_note,
                      "flops_per_update": FLOPS_PER_UPDATE, "peak_nominal": PEAK_FP32_NOMINAL,
                      "frac_of_nominal": bp_tflops / PEAK_FP32_NOMINAL,
                      "peak_source": "measured live on this GPU: FP32 FMA throughput kernel "

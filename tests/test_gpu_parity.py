@@ -181,24 +181,35 @@ def test_every_bp_variant_matches_oracle(orc, cuda, case):
         check(L.tk_bp_select_variant(-1))
 
 
+def _names(L):
+    return [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
+
+
+def _general(names, pn):
+    """Index of the general (non-quarter-turn) default walk of a storage format."""
+    if pn == "f32c":
+        return next(i for i, n in enumerate(names) if n.startswith("cimg_x2<f32c"))
+    return next(i for i, n in enumerate(names) if n.startswith(f"cimg_f32i<{pn},"))
+
+
 @pytest.mark.parametrize("Z", [40, 10])  # a moved-down last z chunk; a chunk shorter than 16 slices
-def test_quarter_turn_kernel(orc, cuda, Z):
-    """FP16 storage on a square, centred, unflipped volume with N divisible by
-    4 runs the quarter-turn kernel (one geometry for four tiles and four
-    projections); it meets the FP16 bound against FP64 and stays within FP16
-    rounding of the general FP16 walk.  An x flip breaks the symmetry: the
-    general walk runs, bit for bit.  Every quarter-turn variant (stage
-    count, box capacity, row interpolation by HFMA2 on regrouped halves or by
-    FP16 FMAs on half-selected operands) gives the same bits, and so do the
-    two forms of the general FP16 walk (cimg_h2, cimg_h3)."""
+@pytest.mark.parametrize("pn,prec,tol", [("f16", _lib.TK_F16, F16_RMSE), ("bf16", _lib.TK_BF16, BF16_RMSE),
+                                         ("f32c", _lib.TK_F32_COEF, F32_RMSE)])
+def test_quarter_turn_kernel(orc, cuda, Z, pn, prec, tol):
+    """A square, centred, unflipped volume with N divisible by 4 runs the
+    quarter-turn kernel of the storage format (one geometry for four tiles and
+    four projections, FP32 interpolation); it meets the format's bound against
+    FP64 and stays within rounding of the general FP32-interpolation walk.  An
+    x flip breaks the symmetry: the general walk runs, bit for bit.  Every
+    FP32-interpolation quarter-turn variant of the format (tile height, stage
+    count, box capacity) gives the same bits."""
     import torch
 
     L = _lib.load()
-    names = [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
-    h2 = next(i for i, n in enumerate(names) if n.startswith("cimg_h2<f16"))
-    quads = [i for i, n in enumerate(names) if n.startswith("quad<")]
-    h3 = next(i for i, n in enumerate(names) if n.startswith("cimg_h3<f16"))
-    assert len(quads) >= 2
+    names = _names(L)
+    gen = _general(names, pn)
+    quads = [i for i, n in enumerate(names) if n.startswith(f"quad<{pn},") and ",f32i," in n]
+    assert quads
     for flip in (0, 1):
         g = small_geometry(W=64, N=120, H=64, vol=(64, 64, Z), dirx=flip)
         G = orc.geom_from(g)
@@ -206,21 +217,60 @@ def test_quarter_turn_kernel(orc, cuda, Z):
         d_in = to_dev(sino, torch)
         vols = []
         try:
-            for sel in [-1, h2, h3] + quads:
+            for sel in [-1, gen] + quads:
                 _lib.check(L.tk_bp_select_variant(sel))
-                vols.append(device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy())
+                vols.append(device.fdk_device(g, d_in, precision=prec).cpu().numpy())
         finally:
             _lib.check(L.tk_bp_select_variant(-1))
         assert device.device_error_flags() == 0
-        np.testing.assert_array_equal(vols[2], vols[1])
-        for v in vols[3:]:
+        for v in vols[2:]:
             np.testing.assert_array_equal(v, vols[0])
         if flip:
             np.testing.assert_array_equal(vols[0], vols[1])
         else:
             assert not np.array_equal(vols[0], vols[1])  # a different kernel ran
-            assert rel_rmse(vols[0], orc.fdk_f64(sino, G)) < F16_RMSE
-            assert rel_rmse(vols[0], vols[1]) < 2e-4
+            ref = orc.fdk_f64(sino, G) if prec != _lib.TK_F32_COEF else orc.fdk_f32(sino, G)
+            assert rel_rmse(vols[0], ref) < tol
+            # the same arithmetic on the same stored values, geometry of the turned columns taken
+            # from the base column (angles a quarter turn apart agree to 1e-5 rad)
+            assert rel_rmse(vols[0], vols[1]) < 2e-6
+
+
+@pytest.mark.parametrize("Z", [40, 10])
+def test_quarter_turn_half_math_forms(orc, cuda, Z):
+    """The selectable FP16 half-math forms (FP16 interpolation arithmetic):
+    every quarter-turn half-math variant (row interpolation by HFMA2 on
+    regrouped halves or by FP16 FMAs on half-selected operands) gives the same
+    bits, and so do the two general half-math walks (cimg_h2, cimg_h3); both
+    meet the FP16 bound.  The default FP32-interpolation form is at least as
+    close to FP64 on this case."""
+    import torch
+
+    L = _lib.load()
+    names = _names(L)
+    h2 = next(i for i, n in enumerate(names) if n.startswith("cimg_h2<f16"))
+    h3 = next(i for i, n in enumerate(names) if n.startswith("cimg_h3<f16"))
+    hq = [i for i, n in enumerate(names) if n.startswith("quad<f16,") and ",h16row" in n]
+    assert len(hq) >= 2
+    g = small_geometry(W=64, N=120, H=64, vol=(64, 64, Z))
+    G = orc.geom_from(g)
+    sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=11), G, "sino")
+    d_in = to_dev(sino, torch)
+    vols = []
+    try:
+        for sel in [-1, h2, h3] + hq:
+            _lib.check(L.tk_bp_select_variant(sel))
+            vols.append(device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy())
+    finally:
+        _lib.check(L.tk_bp_select_variant(-1))
+    assert device.device_error_flags() == 0
+    np.testing.assert_array_equal(vols[2], vols[1])
+    for v in vols[4:]:
+        np.testing.assert_array_equal(v, vols[3])
+    ref = orc.fdk_f64(sino, G)
+    assert rel_rmse(vols[3], ref) < F16_RMSE and rel_rmse(vols[1], ref) < F16_RMSE
+    assert rel_rmse(vols[3], vols[1]) < 2e-4
+    assert rel_rmse(vols[0], ref) <= rel_rmse(vols[3], ref) * 1.05
 
 
 @pytest.mark.parametrize("N,rot,Z", [(8, 0.3, 24),       # two projections per quarter, rotated scan
@@ -229,19 +279,19 @@ def test_quarter_turn_kernel(orc, cuda, Z):
 def test_quarter_turn_kernel_angle_sets(orc, cuda, N, rot, Z):
     """The quarter-turn kernel on small and large angle sets and with a
     rotation offset (the angles stay in quarter-turn sets): it runs (other
-    bits than the general FP16 walk) and meets the FP16 bound against FP64."""
+    bits than the general FP32-interpolation walk) and meets the FP16 bound
+    against FP64."""
     import torch
 
     L = _lib.load()
-    names = [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
-    h3 = next(i for i, n in enumerate(names) if n.startswith("cimg_h3<f16"))
+    gen = _general(_names(L), "f16")
     g = small_geometry(W=64, N=N, H=64, vol=(64, 64, Z), rot=rot)
     G = orc.geom_from(g)
     sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=21), G, "sino")
     d_in = to_dev(sino, torch)
     vols = []
     try:
-        for sel in (-1, h3):
+        for sel in (-1, gen):
             _lib.check(L.tk_bp_select_variant(sel))
             vols.append(device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy())
     finally:
@@ -249,38 +299,38 @@ def test_quarter_turn_kernel_angle_sets(orc, cuda, N, rot, Z):
     assert device.device_error_flags() == 0
     assert not np.array_equal(vols[0], vols[1])
     assert rel_rmse(vols[0], orc.fdk_f64(sino, G)) < F16_RMSE
-    # two FP16 forms: with 8 angles a voxel sums 8 rounded terms, so they differ by up to
-    # the FP16 bound itself (2.4e-4 at N = 8)
-    assert rel_rmse(vols[0], vols[1]) < F16_RMSE
+    assert rel_rmse(vols[0], vols[1]) < 1e-5
 
 
 def test_quarter_turn_wide_boxes(orc, cuda):
     """At scale 1.5 a 16x16x16 tile's footprint (46 x 32 entries, 11.8 KB)
-    exceeds the default quarter-turn kernel's 8 KB slots: with no variant
-    selected the two-stage 13.5 KB form runs (the same bits as selecting it),
-    while selecting the 8 KB form falls back to the general FP16 walk."""
+    exceeds the 6 KB slots of the default FP16 quarter-turn kernel (16x8
+    tiles) and the 8 KB slots of its 16x16 form: with no variant selected the
+    two-stage 13.5 KB form runs (the same bits as selecting it), while
+    selecting the 8 KB form falls back to the general FP32-interpolation
+    walk."""
     import torch
 
     L = _lib.load()
-    names = [L.tk_bp_variant_name(i).decode() for i in range(L.tk_bp_variant_count())]
-    h3 = next(i for i, n in enumerate(names) if n.startswith("cimg_h3<f16"))
-    narrow = next(i for i, n in enumerate(names) if n.startswith("quad<") and "cap8192" in n)
-    wide = next(i for i, n in enumerate(names) if n.startswith("quad<") and "cap13824" in n)
+    names = _names(L)
+    gen = _general(names, "f16")
+    narrow = next(i for i, n in enumerate(names) if n.startswith("quad<f16,") and "cap8192" in n and ",f32i," in n)
+    wide = next(i for i, n in enumerate(names) if n.startswith("quad<f16,") and "cap13824" in n and ",f32i," in n)
     g = small_geometry(W=96, N=120, H=96, vol=(64, 64, 40), voxel_mm=1.2)
     G = orc.geom_from(g)
     sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=23), G, "sino")
     d_in = to_dev(sino, torch)
     vols = {}
     try:
-        for sel in (-1, wide, narrow, h3):
+        for sel in (-1, wide, narrow, gen):
             _lib.check(L.tk_bp_select_variant(sel))
             vols[sel] = device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy()
     finally:
         _lib.check(L.tk_bp_select_variant(-1))
     assert device.device_error_flags() == 0
     np.testing.assert_array_equal(vols[-1], vols[wide])
-    np.testing.assert_array_equal(vols[narrow], vols[h3])
-    assert not np.array_equal(vols[-1], vols[h3])
+    np.testing.assert_array_equal(vols[narrow], vols[gen])
+    assert not np.array_equal(vols[-1], vols[gen])
     assert rel_rmse(vols[-1], orc.fdk_f64(sino, G)) < F16_RMSE
 
 

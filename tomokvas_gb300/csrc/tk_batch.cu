@@ -72,9 +72,10 @@ __device__ __forceinline__ int2 batch_footprint(const BatchItem &I, float2 cs, i
     return make_int2(bx, (int)floorf(vmin) - 1);
 }
 
-// WALK as in update_cimg: 3 is the FP16 half-math walk for TK_F16 and the
-// packed FP32 walk for the other formats (the per-volume defaults).
-template <int PREC, int TX, int TY, int TZ, int STAGES, int MINB, int WALK = 3>
+// WALK as in update_cimg: 4 (FP32 interpolation of 16-bit storage) for TK_F16
+// and TK_BF16 and 1 (packed FP32) for TK_F32_COEF are the per-volume
+// defaults; 3 is the selectable FP16 half-math walk.
+template <int PREC, int TX, int TY, int TZ, int STAGES, int MINB, int WALK = 4>
 __global__ void __launch_bounds__(TX *TY, MINB)
     bp_batch_kernel(const BatchItem *__restrict__ items, int nitems, int nunits, int *counter, unsigned *err,
                     int maxN, int slot_elems)
@@ -187,9 +188,11 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                         const bool all_in = vlo >= 0.f && vhi <= Hm1;
                         if (partial) {
                             if (all_in)
-                                update_cimg<PREC, TZ, true, true>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                                update_cimg<PREC, TZ, true, true, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
+                                                                        acc);
                             else
-                                update_cimg<PREC, TZ, false, true>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                                update_cimg<PREC, TZ, false, true, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
+                                                                         acc);
                         } else {
                             if (all_in)
                                 update_cimg<PREC, TZ, true, false, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
@@ -237,11 +240,13 @@ struct BatchVariant {
     const void *fn;
     int precision, TX, TY, TZ, STAGES;
     const char *name;
+    int walk;  // update_cimg walk; the autotuner tries the FP32-interpolation walks only
 };
 
-#define TK_BATCH(P, PN, TX, TY, TZ, ST, MB) \
-    {reinterpret_cast<const void *>(&bp_batch_kernel<P, TX, TY, TZ, ST, MB>), P, TX, TY, TZ, ST, \
-     "batch<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
+#define TK_BATCH_W(P, PN, TX, TY, TZ, ST, MB, WK, WN) \
+    {reinterpret_cast<const void *>(&bp_batch_kernel<P, TX, TY, TZ, ST, MB, WK>), P, TX, TY, TZ, ST, \
+     "batch<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB WN ">", WK}
+#define TK_BATCH(P, PN, TX, TY, TZ, ST, MB) TK_BATCH_W(P, PN, TX, TY, TZ, ST, MB, 4, "")
 
 // The first entry of each storage format is its default, with the tile
 // shape of the per-volume default (tk_bp.cu) so that both give the same bits:
@@ -254,6 +259,7 @@ static const BatchVariant kBatchVariants[] = {
     TK_BATCH(TK_F16, "f16", 16, 16, 48, 3, 2),
     TK_BATCH(TK_F16, "f16", 16, 16, 64, 2, 2),
     TK_BATCH(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
+    TK_BATCH_W(TK_F16, "f16", 16, 16, 64, 3, 2, 3, ",h16"),  // the FP16 half-math walk
 };
 constexpr int kNumBatchVariants = (int)(sizeof(kBatchVariants) / sizeof(kBatchVariants[0]));
 
@@ -638,7 +644,7 @@ extern "C" int tk_batch_autotune(tk_batch *b, void *stream, int *variant_out, fl
     float best_ms = 3.0e38f;
     int rc = TK_OK;
     for (int vi = 0; vi < kNumBatchVariants && rc == TK_OK; ++vi) {
-        if (kBatchVariants[vi].precision != b->precision) continue;
+        if (kBatchVariants[vi].precision != b->precision || kBatchVariants[vi].walk == 3) continue;
         drop_graph(b);
         b->planned = false;
         if (build_tables(b, vi, st) != TK_OK) continue;  // shape does not fit this batch

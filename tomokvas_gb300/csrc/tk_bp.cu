@@ -474,7 +474,128 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 }
 
 // ---------------------------------------------------------------------------
-// Quarter-turn backprojector (FP16 coefficient images): a circular scan of a
+// The quarter-turn kernel's walk of one step: a column's 16 slices at four
+// projections a quarter turn apart, whose entries sit at the same offsets in
+// the step's four boxes (sbase + k CAPB).  fu, U^2 and the row coordinates
+// v_z = fma(z, dv, v0) are shared by the four.  Past the chunk's last slice
+// (a partial chunk ending on an even slice) the pair's second slice repeats
+// the first, whose rows are inside the box, at weight 0.
+template <int PREC, int INTERP, int CAPB, bool PARTIAL, int ROWI>
+__device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu, float U2,
+                                          float Hm1, bool all_in, int zlast, float (&acc)[4][16])
+{
+    constexpr int TZ = 16;
+    if constexpr (PREC == TK_F32_COEF) {
+        // shared-memory bound (a 16-byte load per voxel): no software pipeline
+#pragma unroll
+        for (int z = 0; z < TZ; z += 2) {
+            if (PARTIAL && z > zlast) break;
+            const bool bin = !PARTIAL || z + 1 <= zlast;
+            const float va = fmaf((float)z, dv, v0);
+            const float vb = bin ? fmaf((float)(z + 1), dv, v0) : va;
+            float fla, flb, fva, fvb;
+            floor_frac_x2(va, vb, fla, flb, fva, fvb);
+            const uint32_t ra = (uint32_t)__float_as_int(fla) * row_bytes + sbase;
+            const uint32_t rb = (uint32_t)__float_as_int(flb) * row_bytes + sbase;
+            float wa = U2, wb = bin ? U2 : 0.f;
+            if (!all_in) {  // kernel.cu:130-131
+                wa = (va >= 0.f && va <= Hm1) ? wa : 0.f;
+                wb = (vb >= 0.f && vb <= Hm1) ? wb : 0.f;
+            }
+            float e[4][8];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                             : "=f"(e[k][0]), "=f"(e[k][1]), "=f"(e[k][2]), "=f"(e[k][3])
+                             : "r"(ra + (uint32_t)(k * CAPB)));
+                asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                             : "=f"(e[k][4]), "=f"(e[k][5]), "=f"(e[k][6]), "=f"(e[k][7])
+                             : "r"(rb + (uint32_t)(k * CAPB)));
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {  // entry (Q, dU, dV, dUV)
+                const float Aa = fmaf(fu, e[k][1], e[k][0]), Ba = fmaf(fu, e[k][3], e[k][2]);
+                const float Ab = fmaf(fu, e[k][5], e[k][4]), Bb = fmaf(fu, e[k][7], e[k][6]);
+                acc[k][z] = fmaf(wa, fmaf(fva, Ba, Aa), acc[k][z]);
+                if (!PARTIAL || z + 1 < TZ) acc[k][z + 1] = fmaf(wb, fmaf(fvb, Bb, Ab), acc[k][z + 1]);
+            }
+        }
+    } else {
+        // 8-byte entries {(Q, dV), (dU, dUV)}, software-pipelined: pair p+1's coordinates,
+        // fractions and eight loads are issued before pair p's arithmetic
+        uint32_t e[2][4][4];  // [buffer][k][lo a, hi a, lo b, hi b]
+        float fvp[2][2], wp[2][2];
+        uint32_t fvh[2], wh[2];
+        const __half2 U2h2 = __float2half2_rn(U2);
+        const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
+        auto fetch = [&](int z, int bi) {
+            const bool bin = !PARTIAL || z + 1 <= zlast;
+            const float va = fmaf((float)z, dv, v0);
+            const float vb = bin ? fmaf((float)(z + 1), dv, v0) : va;
+            float fla, flb, fva, fvb;
+            floor_frac_x2(va, vb, fla, flb, fva, fvb);
+            const uint32_t ra = (uint32_t)__float_as_int(fla) * row_bytes + sbase;
+            const uint32_t rb = (uint32_t)__float_as_int(flb) * row_bytes + sbase;
+            const bool ina = all_in || (va >= 0.f && va <= Hm1);  // kernel.cu:130-131
+            const bool inb = bin && (all_in || (vb >= 0.f && vb <= Hm1));
+            if constexpr (INTERP == 1) {
+                fvp[bi][0] = fva;
+                fvp[bi][1] = fvb;
+                wp[bi][0] = ina ? U2 : 0.f;
+                wp[bi][1] = inb ? U2 : 0.f;
+            } else {
+                const __half2 f2 = __floats2half2_rn(fva, fvb);
+                fvh[bi] = *reinterpret_cast<const uint32_t *>(&f2);
+                wh[bi] = (ina ? (w_all & 0xffffu) : 0u) | (inb ? (w_all & 0xffff0000u) : 0u);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                             : "=r"(e[bi][k][0]), "=r"(e[bi][k][1])
+                             : "r"(ra + (uint32_t)(k * CAPB)));
+                asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                             : "=r"(e[bi][k][2]), "=r"(e[bi][k][3])
+                             : "r"(rb + (uint32_t)(k * CAPB)));
+            }
+        };
+        const __half2 fuh = __float2half2_rn(fu);
+        fetch(0, 0);
+#pragma unroll
+        for (int z = 0; z < TZ; z += 2) {
+            if (PARTIAL && z > zlast) break;
+            const int bi = (z / 2) & 1;
+            if (z + 2 < TZ && (!PARTIAL || z + 2 <= zlast)) fetch(z + 2, bi ^ 1);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if constexpr (INTERP == 1) {
+                    float qa, dva, dua, duva, qb, dvb, dub, duvb;
+                    unpack_pair<PREC>(e[bi][k][0], qa, dva);
+                    unpack_pair<PREC>(e[bi][k][1], dua, duva);
+                    unpack_pair<PREC>(e[bi][k][2], qb, dvb);
+                    unpack_pair<PREC>(e[bi][k][3], dub, duvb);
+                    interp4_acc_x2(qa, qb, dua, dub, dva, dvb, duva, duvb, fu, fvp[bi][0], fvp[bi][1], wp[bi][0],
+                                   wp[bi][1], acc[k][z], acc[k][z + 1]);
+                } else {
+                    const __half2 ha = __hfma2(*reinterpret_cast<const __half2 *>(&e[bi][k][1]), fuh,
+                                               *reinterpret_cast<const __half2 *>(&e[bi][k][0]));
+                    const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&e[bi][k][3]), fuh,
+                                               *reinterpret_cast<const __half2 *>(&e[bi][k][2]));
+                    if (ROWI == 0) {
+                        const __half2 val = __hfma2(*reinterpret_cast<const __half2 *>(&fvh[bi]),
+                                                    __highs2half2(ha, hb), __lows2half2(ha, hb));
+                        acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), wh[bi], acc[k][z], acc[k][z + 1]);
+                    } else {
+                        row_acc_x2(*reinterpret_cast<const uint32_t *>(&ha), *reinterpret_cast<const uint32_t *>(&hb),
+                                   fvh[bi], wh[bi], acc[k][z], acc[k][z + 1]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Quarter-turn backprojector (coefficient images): a circular scan of a
 // square, centred, unflipped volume maps onto itself under a quarter turn.
 // Voxel column (x, y) at angle beta and the column R(x, y) = (X-1-y, x) at
 // beta + 90 degrees have the same S, T, U and u (S' = -aY (-sin) + aX cos = S,
@@ -482,23 +603,36 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // and one floor / fraction / address per slice pair serve four
 // (column, projection) pairs: column c of tile T at projection q and its
 // turns R^k(c) at projection (q + k N/4) mod N.  A CTA owns one orbit
-// {T, R(T), R^2(T), R^3(T)} of 16x16-column tiles (T in the first quadrant)
-// and 16 slices, and steps through the projections q of an angle set closed
-// under quarter turns (all N, or the quarter-turn images of one range
-// [qbase, qbase + qlen)); over the steps each of the four columns sees every
-// projection of the set once.  Step q stages four boxes at T's footprint
-// origin in projection q (projections (q + k N/4) mod N),
-// one TMA load each on one mbarrier, in slots of CAPB bytes (immediate load
-// offsets).  The walk is update_cimg's FP16 walk 3 with four loads and four
-// accumulator sets per slice pair.  Used when the host has checked that the
-// tabulated angles (q + k N/4) mod N are within 1e-5 rad of beta_q + k pi/2.
-template <int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE, int GEO = 0, int TYQ = 16>
-__global__ void __launch_bounds__(16 * TYQ, 32 / TYQ)
+// {T, R(T), R^2(T), R^3(T)} of 16 x TYQ-column tiles (T in the first
+// quadrant) and 16 slices, and steps through the projections q of an angle
+// set closed under quarter turns (all N, or the quarter-turn images of one
+// range [qbase, qbase + qlen)); over the steps each of the four columns sees
+// every projection of the set once.  Step q stages four boxes at T's
+// footprint origin in projection q (projections (q + k N/4) mod N), one TMA
+// load each on one mbarrier, in slots of CAPB bytes (immediate load offsets).
+// Used when the host has checked that the tabulated angles (q + k N/4) mod N
+// are within 1e-5 rad of beta_q + k pi/2.
+//
+// Storage and arithmetic (PREC, INTERP):
+//   TK_F16 / TK_BF16, INTERP 1 (the default): per slice pair and turn k, two
+//     LDS.64 (the pair's entries), the eight 16-bit values converted exactly
+//     to FP32, then FP32 interpolation and accumulation as four fma.rn.f32x2
+//     (interp4_acc_x2): per voxel the operations of update_cimg's walk 4;
+//   TK_F16, INTERP 0 (selectable half-math form): update_cimg's walk 3 --
+//     column interpolation by HFMA2, row interpolation by one FP16 FMA, U^2
+//     rounded to FP16 and applied by fma.rn.f32.f16;
+//   TK_F32_COEF, INTERP 1: one LDS.128 per voxel and the same FP32
+//     operations as scalar FMAs.
+// The 8-byte forms are software-pipelined: pair p+1's coordinates, fractions
+// and eight loads are issued before pair p's arithmetic.
+template <int PREC, int INTERP, int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE, int GEO = 0, int TYQ = 16>
+__global__ void __launch_bounds__(16 * TYQ, (PREC == TK_F32_COEF ? 2 : 32 / TYQ))
     bp_quad_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
     // tiles of 16 x TYQ columns (TYQ 16: 2 CTAs of 8 warps per SM; TYQ 8: 4 CTAs of 4 warps)
-    constexpr int TX = 16, TY = TYQ, TZ = 16, NT = TX * TY, ES = 8;
+    constexpr int TX = 16, TY = TYQ, TZ = 16, NT = TX * TY, ES = Cimg<PREC>::kBytes;
     static_assert(ISSUE == 0 || NT / 32 >= 4, "four issuing warps");
+    static_assert(INTERP == 1 || PREC == TK_F16, "the half-math walk is FP16 only");
     extern __shared__ __align__(128) unsigned char smem[];
     const int NQ = P.N / 4;  // a quarter turn in projections
     const int steps = 4 * P.qlen;
@@ -535,7 +669,7 @@ __global__ void __launch_bounds__(16 * TYQ, 32 / TYQ)
     }
 
     for (int t = tid; t < steps; t += NT) {
-        const int2 o = footprint_origin_z<TX, TY, 2>(P, qof(t), x0, y0, z0, z0 + zlast);
+        const int2 o = footprint_origin_z<TX, TY, Cimg<PREC>::kAlign>(P, qof(t), x0, y0, z0, z0 + zlast);
         boxo[t] = make_short2((short)o.x, (short)o.y);
     }
     if (tid == 0) {
@@ -621,67 +755,9 @@ __global__ void __launch_bounds__(16 * TYQ, 32 / TYQ)
                     const uint32_t sbase = smem0 + (uint32_t)(s * 4) * CAPB + (uint32_t)col * ES -
                                            (uint32_t)(kMagicBits + by0) * row_bytes;
                     const float U2 = __fmul_rn(U, U);
-                    const __half2 fuh = __float2half2_rn(fu);
-                    const __half2 U2h2 = __float2half2_rn(U2);
-                    const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
                     const bool all_in = vlo >= 0.f && vhi <= Hm1;
-                    // software-pipelined: pair p+1's coordinates, fractions and eight loads are issued
-                    // before pair p's arithmetic, so the loads' latency overlaps it
-                    uint32_t e[2][4][4];  // [buffer][k][lo a, hi a, lo b, hi b]
-                    __half2 fvp[2];
-                    uint32_t wp[2];
-                    auto fetch = [&](int z, int bi) {
-                        // past the chunk's last slice (a partial chunk ending on an even slice) the
-                        // pair's second slice repeats the first, whose rows are inside the box, at weight 0
-                        const bool bin = !PARTIAL || z + 1 <= zlast;
-                        const float va = fmaf((float)z, dv, v0);
-                        const float vb = bin ? fmaf((float)(z + 1), dv, v0) : va;
-                        float fla2, flb2, fva, fvb;
-                        floor_frac_x2(va, vb, fla2, flb2, fva, fvb);
-                        const uint32_t ra = (uint32_t)__float_as_int(fla2) * row_bytes + sbase;
-                        const uint32_t rb = (uint32_t)__float_as_int(flb2) * row_bytes + sbase;
-                        fvp[bi] = __floats2half2_rn(fva, fvb);
-                        uint32_t w2 = w_all;
-                        if (!all_in)  // kernel.cu:130-131
-                            w2 = ((va >= 0.f && va <= Hm1) ? (w_all & 0xffffu) : 0u) |
-                                 ((vb >= 0.f && vb <= Hm1) ? (w_all & 0xffff0000u) : 0u);
-                        if (!bin) w2 &= 0xffffu;
-                        wp[bi] = w2;
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
-                                         : "=r"(e[bi][k][0]), "=r"(e[bi][k][1])
-                                         : "r"(ra + (uint32_t)(k * CAPB)));
-                            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
-                                         : "=r"(e[bi][k][2]), "=r"(e[bi][k][3])
-                                         : "r"(rb + (uint32_t)(k * CAPB)));
-                        }
-                    };
-                    fetch(0, 0);
-#pragma unroll
-                    for (int z = 0; z < TZ; z += 2) {
-                        if (PARTIAL && z > zlast) break;
-                        const int bi = (z / 2) & 1;
-                        if (z + 2 < TZ && (!PARTIAL || z + 2 <= zlast)) fetch(z + 2, bi ^ 1);
-#pragma unroll
-                        for (int k = 0; k < 4; ++k) {
-                            const __half2 ha = __hfma2(*reinterpret_cast<const __half2 *>(&e[bi][k][1]), fuh,
-                                                       *reinterpret_cast<const __half2 *>(&e[bi][k][0]));
-                            const __half2 hb = __hfma2(*reinterpret_cast<const __half2 *>(&e[bi][k][3]), fuh,
-                                                       *reinterpret_cast<const __half2 *>(&e[bi][k][2]));
-                            if (ROWI == 0) {
-                                const __half2 val =
-                                    __hfma2(fvp[bi], __highs2half2(ha, hb), __lows2half2(ha, hb));
-                                acc_mixed_x2(*reinterpret_cast<const uint32_t *>(&val), wp[bi], acc[k][z],
-                                             acc[k][z + 1]);
-                            } else {
-                                row_acc_x2(*reinterpret_cast<const uint32_t *>(&ha),
-                                           *reinterpret_cast<const uint32_t *>(&hb),
-                                           *reinterpret_cast<const uint32_t *>(&fvp[bi]), wp[bi], acc[k][z],
-                                           acc[k][z + 1]);
-                            }
-                        }
-                    }
+                    quad_walk<PREC, INTERP, CAPB, PARTIAL, ROWI>(sbase, row_bytes, v0, dv, fu, U2, Hm1, all_in,
+                                                                zlast, acc);
                 } else {
                     atomicOr(P.err, ERR_BOX_OVERFLOW);
                 }
@@ -1026,31 +1102,56 @@ struct BPVariant {
     {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB, 1>), \
      reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 1>), P, TX, TY, TZ, ST, true, \
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
-// quarter-turn FP16 kernel (the walk of WALK 3, or of WALK 2 with ROWI 0), for symmetric scans only
-#define TK_BP_QUAD_T(CAP, ST, ROWI, ISSUE, AUTO, GEO, TY) \
-    {reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, false, ROWI, ISSUE, GEO, TY>), \
-     reinterpret_cast<const void *>(&bp_quad_kernel<CAP, ST, true, ROWI, ISSUE, GEO, TY>), TK_F16, 16, TY, 16, ST, true, \
-     "quad<f16,16," #TY ",16," #ST ",cap" #CAP ",row" #ROWI ",issue" #ISSUE ",geo" #GEO ">", CAP, AUTO}
-#define TK_BP_QUAD(CAP, ST, ROWI, ISSUE, AUTO, GEO) TK_BP_QUAD_T(CAP, ST, ROWI, ISSUE, AUTO, GEO, 16)
+// quarter-turn kernels, for symmetric scans only: PREC storage, INTERP 1 FP32 interpolation
+// (update_cimg walk 4's operations), INTERP 0 the FP16 half-math walk 3 (ROWI 1) or 2 (ROWI 0)
+#define TK_BP_QUAD_T(P, PN, IN, INAME, CAP, ST, ROWI, ISSUE, AUTO, GEO, TY) \
+    {reinterpret_cast<const void *>(&bp_quad_kernel<P, IN, CAP, ST, false, ROWI, ISSUE, GEO, TY>), \
+     reinterpret_cast<const void *>(&bp_quad_kernel<P, IN, CAP, ST, true, ROWI, ISSUE, GEO, TY>), P, 16, TY, 16, ST, \
+     true, "quad<" PN ",16," #TY ",16," #ST ",cap" #CAP "," INAME ",issue" #ISSUE ",geo" #GEO ">", CAP, AUTO}
+#define TK_BP_QUADF(P, PN, CAP, ST, AUTO, TY) TK_BP_QUAD_T(P, PN, 1, "f32i", CAP, ST, 1, 1, AUTO, 1, TY)
+#define TK_BP_QUADH(CAP, ST, ROWI, ISSUE, AUTO, GEO, TY) \
+    TK_BP_QUAD_T(TK_F16, "f16", 0, "h16row" #ROWI, CAP, ST, ROWI, ISSUE, AUTO, GEO, TY)
 // FP16 half-math walks (update_cimg WALK 2 and 3, same bits): not bit-identical to the FP32 walks
 #define TK_BP_CIMG_H2(TX, TY, TZ, ST, MB, WK) \
     {reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, false, MB, WK>), \
      reinterpret_cast<const void *>(&bp_cimg_kernel<TK_F16, TX, TY, TZ, ST, true, MB, WK>), TK_F16, TX, TY, TZ, ST, \
      true, "cimg_h" #WK "<f16," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
+// 16-bit storage with FP32 interpolation (update_cimg WALK 4)
+#define TK_BP_CIMG_F(P, PN, TX, TY, TZ, ST, MB) \
+    {reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, false, MB, 4>), \
+     reinterpret_cast<const void *>(&bp_cimg_kernel<P, TX, TY, TZ, ST, true, MB, 4>), P, TX, TY, TZ, ST, true, \
+     "cimg_f32i<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 
-// The first entry of each storage format is its default: the packed walks
-// (same bits as the scalar ones, fewer issued instructions), and for FP16
-// storage the quarter-turn kernel (16 x 8 tiles), whose automatic alternatives
-// (qauto, in table order) take larger footprints, and otherwise the first
-// general entry, the half-math walk 3 (FP16 row interpolation, FP32
-// accumulation).
+// The first entry of each storage format is its default.  Every default
+// interpolates in FP32 (FP32 geometry, interpolation weights, interpolation and
+// accumulation; 16-bit storage converted exactly to FP32).  Where a format has
+// quarter-turn variants its first entry is one; the automatic quarter-turn
+// alternatives (qauto, in table order) take larger footprints, and a scan
+// without the symmetry runs the format's first general entry.  FP16 storage:
+// the quarter-turn kernel with 16 x 8 tiles, else walk 4.  The half-math
+// walks (FP16 interpolation arithmetic) are selectable only.
 static const BPVariant kVariants[] = {
     TK_BP_DIRECT_PK(16, 16, 32, 4),
-    TK_BP_QUAD_T(6144, 2, 1, 1, true, 1, 8),
-    TK_BP_CIMG_H2(16, 16, 64, 3, 2, 3),
-    TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
+    TK_BP_QUADF(TK_F16, "f16", 6144, 2, true, 8),
+    TK_BP_CIMG_F(TK_F16, "f16", 16, 16, 64, 3, 2),
+    TK_BP_QUADF(TK_BF16, "bf16", 6144, 2, true, 8),
+    TK_BP_CIMG_F(TK_BF16, "bf16", 16, 16, 64, 3, 2),
+    TK_BP_QUADF(TK_F32_COEF, "f32c", 13312, 2, true, 16),
     TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
     TK_BP_DIRECT(16, 16, 32, 4),
+    TK_BP_QUADF(TK_F16, "f16", 8192, 2, true, 16),   // 16 x 16 tiles when a 16 x 8 tile's footprint exceeds 6 KB
+    TK_BP_QUADF(TK_F16, "f16", 13824, 2, true, 16),  // footprints of up to 13.5 KB (scales near 1.5)
+    TK_BP_QUADF(TK_BF16, "bf16", 8192, 2, true, 16),
+    TK_BP_QUADF(TK_BF16, "bf16", 13824, 2, true, 16),
+    TK_BP_QUADH(6144, 2, 1, 1, false, 1, 8),  // the FP16 half-math forms
+    TK_BP_QUADH(8192, 2, 1, 1, false, 1, 16),
+    TK_BP_QUADH(13824, 2, 1, 1, false, 1, 16),
+    TK_BP_QUADH(8192, 3, 1, 0, false, 0, 16),
+    TK_BP_QUADH(8192, 3, 0, 0, false, 0, 16),
+    TK_BP_CIMG_H2(16, 16, 64, 3, 2, 3),
+    TK_BP_CIMG_H2(16, 16, 64, 3, 2, 2),
+    TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
+    TK_BP_CIMG_PK(TK_BF16, "bf16", 16, 16, 64, 3, 2),
     TK_BP_CIMG(TK_F16, "f16", 16, 16, 64, 3, 2),
     TK_BP_CIMG(TK_BF16, "bf16", 16, 16, 64, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
@@ -1059,14 +1160,6 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 48, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
-    TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 64, 3, 2),
-    TK_BP_QUAD(8192, 3, 1, 0, false, 0),
-    TK_BP_QUAD(8192, 3, 0, 0, false, 0),
-    TK_BP_QUAD(8192, 2, 1, 1, true, 1),    // 16 x 16 tiles when a 16 x 8 tile's footprint exceeds 6 KB
-    TK_BP_QUAD(13824, 2, 1, 1, true, 1),  // footprints of up to 13.5 KB (scales near 1.5), two stages
-    TK_BP_QUAD(8192, 3, 1, 1, false, 0),
-    TK_BP_QUAD(8192, 3, 1, 1, false, 1),
-    TK_BP_CIMG_H2(16, 16, 64, 3, 2, 2),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
@@ -1119,7 +1212,7 @@ int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ
 // launch with projection (q + k N/4) mod N at beta_q + k pi/2 (mod 2 pi) to within 1e-5 rad
 // (angles as build_trig forms them; 1e-5 rad is 0.01 pixel at 1000 pixels
 // from the axis), and a box that fits its slot.
-static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, int cap, int TY = 16)
+static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, int cap, int TY, int precision)
 {
     if (g.X != g.Y || g.X % 32 != 0 || g.dirx || g.diry) return false;
     if (g.W >= (1 << 14) || g.H >= (1 << 14)) return false;  // footprint origins kept as 16-bit pairs
@@ -1132,9 +1225,10 @@ static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, 
             const double d = std::remainder(beta((q + k * nq) % g.N) - beta(q) - k * (M_PI / 2), 2 * M_PI);
             if (std::fabs(d) > 1e-5) return false;
         }
+    const int ES = (int)entry_size(precision);
     int BW = 0, BH = 0;
-    if (bp_box_dims(g, nz, zoff, 16, TY, 16, true, 2, &BW, &BH) != TK_OK) return false;
-    return BW * BH * 8 <= cap;
+    if (bp_box_dims(g, nz, zoff, 16, TY, 16, true, 16 / ES, &BW, &BH) != TK_OK) return false;
+    return BW * BH * ES <= cap;
 }
 
 // The quarter-turn variant for this launch: the selected variant if it is one
@@ -1144,10 +1238,11 @@ static const BPVariant *pick_quad(const tk_geometry &g, int precision, int nz, f
 {
     if (g_variant_override >= 0 && kVariants[g_variant_override].precision == precision) {
         const BPVariant *v = &kVariants[g_variant_override];
-        return v->qcap && quad_eligible(g, nz, zoff, angle0, v->qcap, v->TY) ? v : nullptr;
+        return v->qcap && quad_eligible(g, nz, zoff, angle0, v->qcap, v->TY, precision) ? v : nullptr;
     }
     for (const auto &c : kVariants)
-        if (c.precision == precision && c.qcap && c.qauto && quad_eligible(g, nz, zoff, angle0, c.qcap, c.TY)) return &c;
+        if (c.precision == precision && c.qcap && c.qauto && quad_eligible(g, nz, zoff, angle0, c.qcap, c.TY, precision))
+            return &c;
     return nullptr;
 }
 
@@ -1288,16 +1383,18 @@ int launch_backproject(const tk_geometry &g, const void *d_q, int precision, con
 
 bool backproject_quarter_ok(const tk_geometry &g, int precision, int nz, float zoff)
 {
-    if (precision != TK_F16 || nz <= 0) return false;
+    if (precision == TK_F32 || nz <= 0) return false;
     const BPVariant *v = pick_variant(precision);  // honours a selected variant
     return v && v->qcap && pick_quad(g, precision, nz, zoff, 0) != nullptr;
 }
 
-int launch_backproject_quarter(const tk_geometry &g, const void *d_q, const float *d_q_scale, int nz, float zoff,
-                               float *d_vol, int accumulate, cudaStream_t stream, int qbase, int qlen, bool compact)
+int launch_backproject_quarter(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale, int nz,
+                               float zoff, float *d_vol, int accumulate, cudaStream_t stream, int qbase, int qlen,
+                               bool compact)
 {
     TK_CHECK(qlen > 0, TK_ERR_INVALID, "backproject: empty angle range");
-    return launch_bp_impl(g, d_q, TK_F16, d_q_scale, nz, zoff, d_vol, accumulate, stream, 0, qbase, qlen, compact);
+    return launch_bp_impl(g, d_q, precision, d_q_scale, nz, zoff, d_vol, accumulate, stream, 0, qbase, qlen,
+                          compact);
 }
 
 int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, float zoff, float *d_qbar,

@@ -48,7 +48,9 @@ __device__ __forceinline__ float slice_v(float aZ, float U, float cZ) { return f
 // detector cell [r, r+1] x [c, c+1], so an update is one shared load of one
 // entry and
 //   A = Q + fu dU,  B = dV + fu dUV,  acc += U^2 (A + fv B)
-// (FP16/BF16: A and B come from one packed HFMA2).  Loads use 32-bit shared
+// (16-bit storage: the four values converted to FP32 first, eval_f32; the
+// selectable half-math forms take A and B from one packed HFMA2, eval).
+// Loads use 32-bit shared
 // addresses (inline PTX) so the address of an update is one IMAD.
 template <int PREC> struct Cimg;
 template <> struct Cimg<TK_F32_COEF> {
@@ -59,7 +61,39 @@ template <> struct Cimg<TK_F32_COEF> {
         asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(q), "=f"(du), "=f"(dv), "=f"(duv) : "r"(addr));
         return make_float2(fmaf(fu, du, q), fmaf(fu, duv, dv));
     }
+    static __device__ __forceinline__ float2 eval_f32(uint32_t addr, float fu) { return eval(addr, fu, float2{}); }
 };
+// The two halves of a 16-bit pair word as FP32 (exact conversions): lo is
+// the half in bits 0-15.
+template <int PREC> __device__ __forceinline__ void unpack_pair(uint32_t w, float &lo, float &hi)
+{
+    if constexpr (PREC == TK_BF16) {
+        // a bfloat16 is the upper half of its FP32 value: two byte permutes (integer pipe)
+        uint32_t l, h;
+        asm("prmt.b32 %0, %2, 0, 0x1044;\n\t"
+            "prmt.b32 %1, %2, 0, 0x3244;"
+            : "=r"(l), "=r"(h)
+            : "r"(w));
+        lo = __uint_as_float(l);
+        hi = __uint_as_float(h);
+    } else {
+        const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w));
+        lo = f.x;
+        hi = f.y;
+    }
+}
+// FP32 interpolation of a 16-bit entry {(Q, dV), (dU, dUV)}: the four values
+// converted exactly to FP32, then A = fma(fu, dU, Q), B = fma(fu, dUV, dV) --
+// the operations of the FP32 coefficient format on the stored values.
+template <int PREC> __device__ __forceinline__ float2 eval16_f32(uint32_t addr, float fu)
+{
+    uint32_t lo, hi;
+    asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(lo), "=r"(hi) : "r"(addr));
+    float q, dv, du, duv;
+    unpack_pair<PREC>(lo, q, dv);
+    unpack_pair<PREC>(hi, du, duv);
+    return make_float2(fmaf(fu, du, q), fmaf(fu, duv, dv));
+}
 template <> struct Cimg<TK_F16> {
     static constexpr int kBytes = 8, kAlign = 2;
     static __device__ __forceinline__ float2 eval(uint32_t addr, float, float2 fu2raw)
@@ -71,6 +105,7 @@ template <> struct Cimg<TK_F16> {
                                   *reinterpret_cast<const __half2 *>(&lo));
         return __half22float2(h);
     }
+    static __device__ __forceinline__ float2 eval_f32(uint32_t addr, float fu) { return eval16_f32<TK_F16>(addr, fu); }
 };
 template <> struct Cimg<TK_BF16> {
     static constexpr int kBytes = 8, kAlign = 2;
@@ -83,6 +118,7 @@ template <> struct Cimg<TK_BF16> {
                                          *reinterpret_cast<const __nv_bfloat162 *>(&lo));
         return __bfloat1622float2(h);
     }
+    static __device__ __forceinline__ float2 eval_f32(uint32_t addr, float fu) { return eval16_f32<TK_BF16>(addr, fu); }
 };
 
 // fu packed for the 16-bit HFMA2 (carried in the bits of a float2.x).
@@ -146,6 +182,33 @@ __device__ __forceinline__ void interp_acc_x2(float aa, float ab, float ba, floa
         : "f"(aa), "f"(ab), "f"(ba), "f"(bb), "f"(fva), "f"(fvb), "f"(wa), "f"(wb));
 }
 
+// FP32 bilinear interpolation and accumulation of two slices a, b from their
+// entries' four values (Q, dU, dV, dUV) as four fma.rn.f32x2; per lane
+//   A = fma(fu, dU, Q), B = fma(fu, dUV, dV), acc = fma(w, fma(fv, B, A), acc),
+// the operations of Cimg<TK_F32_COEF>::eval followed by interp_acc_x2.
+__device__ __forceinline__ void interp4_acc_x2(float qa, float qb, float dua, float dub, float dva, float dvb,
+                                               float duva, float duvb, float fu, float fva, float fvb, float wa,
+                                               float wb, float &acc0, float &acc1)
+{
+    asm("{\n\t.reg .b64 Q, DU, DV, DUV, FU, FV, W, C;\n\t"
+        "mov.b64 Q, {%2, %3};\n\t"
+        "mov.b64 DU, {%4, %5};\n\t"
+        "mov.b64 DV, {%6, %7};\n\t"
+        "mov.b64 DUV, {%8, %9};\n\t"
+        "mov.b64 FU, {%10, %10};\n\t"
+        "mov.b64 FV, {%11, %12};\n\t"
+        "mov.b64 W, {%13, %14};\n\t"
+        "mov.b64 C, {%0, %1};\n\t"
+        "fma.rn.f32x2 Q, FU, DU, Q;\n\t"
+        "fma.rn.f32x2 DV, FU, DUV, DV;\n\t"
+        "fma.rn.f32x2 Q, FV, DV, Q;\n\t"
+        "fma.rn.f32x2 C, W, Q, C;\n\t"
+        "mov.b64 {%0, %1}, C;\n\t}"
+        : "+f"(acc0), "+f"(acc1)
+        : "f"(qa), "f"(qb), "f"(dua), "f"(dub), "f"(dva), "f"(dvb), "f"(duva), "f"(duvb), "f"(fu), "f"(fva),
+          "f"(fvb), "f"(wa), "f"(wb));
+}
+
 // acc0 += w.lo * val.lo and acc1 += w.hi * val.hi: FP16 products (exact in
 // FP32) added to FP32 accumulators with one rounding (fma.rn.f32.f16).
 __device__ __forceinline__ void acc_mixed_x2(uint32_t val2, uint32_t w2, float &acc0, float &acc1)
@@ -198,7 +261,12 @@ __device__ __forceinline__ void row_acc_x2(uint32_t ha, uint32_t hb, uint32_t fv
 //   3  walk 2 with each slice's row interpolation one FP16 FMA on
 //      half-selected operands (row_acc_x2) instead of the permutes and the
 //      HFMA2: the same roundings, so the same bits, and 4.5 % faster on the
-//      1024^2 x 64-slice slab (the default FP16 walk).
+//      1024^2 x 64-slice slab (the FP16 half-math walk, selectable);
+//   4  16-bit storage with FP32 interpolation (the TK_F16 and TK_BF16
+//      default): walk 1 with each entry's four values converted exactly to
+//      FP32 and interpolated by interp4_acc_x2, so per voxel the operations of
+//      the FP32 coefficient format on the stored values; PARTIAL chunks take
+//      the scalar form of the same operations (Cimg::eval_f32).
 template <int PREC, int TZ, bool ALL_IN, bool PARTIAL, int WALK = 0>
 __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu,
                                             float U2, float Hm1, int zlast, float (&acc)[TZ])
@@ -251,6 +319,31 @@ __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, 
                            *reinterpret_cast<const uint32_t *>(&fv2), w2, acc[z], acc[z + 1]);
             }
         }
+    } else if constexpr (WALK == 4 && PREC != TK_F32_COEF && !PARTIAL && (TZ % 2 == 0)) {
+#pragma unroll
+        for (int z = 0; z < TZ; z += 2) {
+            const float va = fmaf((float)z, dv, v0), vb = fmaf((float)(z + 1), dv, v0);
+            float fla, flb, fva, fvb;
+            floor_frac_x2(va, vb, fla, flb, fva, fvb);
+            uint32_t loa, hia, lob, hib;
+            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                         : "=r"(loa), "=r"(hia)
+                         : "r"((uint32_t)__float_as_int(fla) * row_bytes + sbase));
+            asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                         : "=r"(lob), "=r"(hib)
+                         : "r"((uint32_t)__float_as_int(flb) * row_bytes + sbase));
+            float qa, dva, dua, duva, qb, dvb, dub, duvb;
+            unpack_pair<PREC>(loa, qa, dva);
+            unpack_pair<PREC>(hia, dua, duva);
+            unpack_pair<PREC>(lob, qb, dvb);
+            unpack_pair<PREC>(hib, dub, duvb);
+            float wa = U2, wb = U2;
+            if constexpr (!ALL_IN) {
+                wa = (va >= 0.f && va <= Hm1) ? U2 : 0.f;  // kernel.cu:130-131
+                wb = (vb >= 0.f && vb <= Hm1) ? U2 : 0.f;
+            }
+            interp4_acc_x2(qa, qb, dua, dub, dva, dvb, duva, duvb, fu, fva, fvb, wa, wb, acc[z], acc[z + 1]);
+        }
     } else if constexpr (WALK >= 1 && !PARTIAL && (TZ % 2 == 0)) {
 #pragma unroll
         for (int z = 0; z < TZ; z += 2) {
@@ -274,7 +367,7 @@ __device__ __forceinline__ void update_cimg(uint32_t sbase, uint32_t row_bytes, 
             const float fl = __fadd_rd(v, kMagic);
             const float fv = v - (fl - kMagic);
             const uint32_t addr = (uint32_t)__float_as_int(fl) * row_bytes + sbase;
-            const float2 ab = Cimg<PREC>::eval(addr, fu, fu2);
+            const float2 ab = WALK == 4 ? Cimg<PREC>::eval_f32(addr, fu) : Cimg<PREC>::eval(addr, fu, fu2);
             const float val = fmaf(fv, ab.y, ab.x);
             if constexpr (ALL_IN) {
                 acc[z] = fmaf(U2, val, acc[z]);

@@ -265,7 +265,7 @@ extern "C" int tk_fdk_stream(const tk_geometry *g, const void *h_in, int input_t
     // quarter-turn kernel.  Otherwise chunk k is projections [k chunk, + chunk).
     const int NQ = g->N / 4;
     const bool quad =
-        precision == TK_F16 && g->N % 4 == 0 && C >= 4 && backproject_quarter_ok(*g, precision, g->Z, zoff);
+        g->N % 4 == 0 && C >= 4 && backproject_quarter_ok(*g, precision, g->Z, zoff);
     const int L = quad ? C / 4 : 0;
     const int nch = quad ? (NQ + L - 1) / L : nchunks;
     auto qlen_of = [&](int k) { return std::min(L, NQ - k * L); };
@@ -296,8 +296,8 @@ extern "C" int tk_fdk_stream(const tk_geometry *g, const void *h_in, int input_t
             return rc;
         TK_CUDA(cudaEventRecord(ss.consumed[slot], st));
         if (quad) {
-            if (int rc = launch_backproject_quarter(*g, d_q, d_scale, g->Z, zoff, d_vol, k > 0, st, k * L, qlen_of(k),
-                                                    true))
+            if (int rc = launch_backproject_quarter(*g, d_q, precision, d_scale, g->Z, zoff, d_vol, k > 0, st, k * L,
+                                                    qlen_of(k), true))
                 return rc;
         } else if (int rc = launch_backproject(gc, d_q, precision, d_scale, g->Z, zoff, d_vol, k > 0, st, b0)) {
             return rc;
@@ -826,7 +826,7 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
         cudaStream_t fs = qC > 0 ? h->filt_stream : h->stream;  // the filters' stream
         if (qC > 0) TK_CUDA(cudaStreamWaitEvent(fs, h->ev[8], 0));
         auto bp_early = [&](int c, int nz, float zo, float *vol, int acc, cudaStream_t st) -> int {
-            if (qC > 0) return launch_backproject_quarter(g, d_q, d_scale, nz, zo, vol, 0, st, 0, qE * qL);
+            if (qC > 0) return launch_backproject_quarter(g, d_q, h->precision, d_scale, nz, zo, vol, 0, st, 0, qE * qL);
             const Range r = chunks[c][0];
             tk_geometry gc = g;
             gc.N = r.n;
@@ -835,7 +835,8 @@ extern "C" int tk_fdk_initialize(tk_fdk *h)
         };
         auto bp_rest = [&](int nz, float zo, float *vol, cudaStream_t st) -> int {
             if (qC > 0)
-                return launch_backproject_quarter(g, d_q, d_scale, nz, zo, vol, 1, st, qE * qL, (qC - qE) * qL);
+                return launch_backproject_quarter(g, d_q, h->precision, d_scale, nz, zo, vol, 1, st, qE * qL,
+                                                  (qC - qE) * qL);
             tk_geometry gr = g;
             gr.N = g.N - major_end;
             return launch_backproject(gr, d_q + (size_t)major_end * qframe, h->precision, d_scale, nz, zo, vol, 1,

@@ -49,14 +49,15 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
 // a longer scan when angle0 > 0).
 int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale,
                        int nz, float zoff, float *d_vol, int accumulate, cudaStream_t stream, int angle0 = 0);
-// The quarter-turn FP16 kernel (square centred unflipped volume, N divisible
-// by 4, the default variant selection): whether it applies, and a launch over
+// The quarter-turn kernel of a coefficient-image format (square centred
+// unflipped volume, N divisible by 4, the format's default or selected
+// quarter-turn variant): whether it applies, and a launch over
 // the quarter-turn images of angles [qbase, qbase + qlen), qbase + qlen <= N/4,
 // with d_q holding all N filtered projections, or (compact) only the four
 // ranges [qbase + k N/4, + qlen), k = 0..3, one after another.
 bool backproject_quarter_ok(const tk_geometry &g, int precision, int nz, float zoff);
-int launch_backproject_quarter(const tk_geometry &g, const void *d_q, const float *d_q_scale, int nz, float zoff,
-                               float *d_vol, int accumulate, cudaStream_t stream, int qbase, int qlen,
+int launch_backproject_quarter(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale, int nz,
+                               float zoff, float *d_vol, int accumulate, cudaStream_t stream, int qbase, int qlen,
                                bool compact = false);
 int launch_filter_transpose(const tk_geometry &g, const float *d_qbar, int window, float *d_pbar, int layout,
                             cudaStream_t stream);
