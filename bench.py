@@ -369,6 +369,9 @@ def run_ours(args):
     # chosen form: FP16 storage, FP32 interpolation (the default FP16 kernel)
     ms16, f16_filter, f16_bp, clocks = timed(_lib.TK_F16, K, W, sample_clocks=(rank == 0))
     vol16 = slices()
+    # the same form with bfloat16 storage (widening on the integer pipe)
+    ms_bf, bf_filter, bf_bp, _ = timed(_lib.TK_BF16, K, W)
+    vol_bf = slices()
     # plain form: the faster of the two FP32 storage formats (samples / coefficients)
     plain_runs = {}
     for pname, pcode in (("f32", _lib.TK_F32), ("f32c", _lib.TK_F32_COEF)):
@@ -466,16 +469,17 @@ def run_ours(args):
         G = orc.geom_from(g)
         raw_np = raw.cpu().numpy().view(np.uint16)
         sino = orc.log_u16(raw_np, np.float32(I0))
-        num16 = num32 = numhm = den = 0.0
+        num16 = num32 = numhm = numbf = den = 0.0
         for zs in RMSE_SLICES:
             ref = orc.fdk_f64(sino, G, "hann", np.array(zs, dtype=np.int32))
             num16 += float(np.sum((vol16[tuple(zs)] - ref) ** 2))
+            numbf += float(np.sum((vol_bf[tuple(zs)] - ref) ** 2))
             num32 += float(np.sum((vol32[tuple(zs)] - ref) ** 2))
             numhm += float(np.sum((vol_hm[tuple(zs)] - ref) ** 2))
             den += float(np.sum(ref ** 2))
         del sino
         rmse = {"chosen_f16_vs_fp64": (num16 / den) ** 0.5, "plain_f32_vs_fp64": (num32 / den) ** 0.5,
-                "half_math_f16_vs_fp64": (numhm / den) ** 0.5,
+                "half_math_f16_vs_fp64": (numhm / den) ** 0.5, "bf16_vs_fp64": (numbf / den) ** 0.5,
                 "slices": [z for zs in RMSE_SLICES for z in zs], "metric": "relative RMSE"}
 
     cores = os.cpu_count() or 1
@@ -516,6 +520,11 @@ def run_ours(args):
                   "filter_ms": f32_filter, "bp_ms": f32_bp, "formats": plain_alt},
         "chosen_vs_plain": plain and value / plain,
         "chosen_vs_plain_kernels": [kname, plain_alt[plain_name]["kernel"]],
+        "bf16": {"value": replica_gups(upd, world, ms_bf * 1e-3), "unit": "GUPS", "ms_per_step": ms_bf,
+                 "bp_ms": bf_bp, "filter_ms": bf_filter, "kernel": bp_kernel_name(-1, _lib.TK_BF16),
+                 "dtype": "bf16-stored filtered projections, f32 bilinear interpolation and accumulation",
+                 "rmse_vs_fp64": rmse and rmse["bf16_vs_fp64"],
+                 "vs_plain": plain and replica_gups(upd, world, ms_bf * 1e-3) / plain},
         "half_math": {"value": replica_gups(upd, world, ms_hm * 1e-3), "unit": "GUPS", "ms_per_step": ms_hm,
                       "bp_ms": hm_bp, "filter_ms": hm_filter, "kernel": bp_kernel_name(hm),
                       "dtype": "f16 storage with f16 interpolation arithmetic (HFMA2 column and FP16 row "

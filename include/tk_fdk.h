@@ -226,6 +226,28 @@ int tk_fdk_backward(const tk_geometry *g, const float *d_vol_grad, int layout, i
 int tk_fdk_device_noalloc(const tk_geometry *g, const void *d_in, int input_type, int layout,
                           const tk_flatfield *ff, int window, int precision, float *d_vol, void *stream);
 
+/* Ramp-filter form.  The filter is the convolution of each detector row with
+ * the even kernel K = C2R_p(tau |R2C_p(h)|), a symmetric Toeplitz matrix
+ * (fConvolution, kernel.cu:557-781):
+ *   TK_FILTER_FFT       shared-memory Stockham FFT of the padded row (any W);
+ *   TK_FILTER_TOEPLITZ  the W x W Toeplitz product on the tcgen05 tensor
+ *                       cores with split-BF16 compensated products and FP32
+ *                       accumulation (8 <= W <= 512; other widths take the FFT);
+ *   TK_FILTER_AUTO      (default) the Toeplitz product for 16-bit storage
+ *                       up to W = 512, where it is the faster form; the FFT
+ *                       for wider rows and for FP32 storage (the split-BF16
+ *                       product carries about 2e-5 relative error, below
+ *                       16-bit rounding but above the FP32 forms' bound).
+ * The selection is process-wide; tk_filter_form_for reports the form a width and
+ * storage format would run.  No counterpart in the reference (cuFFT only). */
+typedef enum tk_filter_form {
+    TK_FILTER_AUTO = 0,
+    TK_FILTER_FFT = 1,
+    TK_FILTER_TOEPLITZ = 2
+} tk_filter_form;
+int tk_filter_select_form(int form);
+int tk_filter_form_for(int W, int precision);
+
 /* Backprojection kernel variants (tile shape, pipeline), for benchmarking
  * and the autotuner; no counterpart in the reference, whose launch shape is
  * fixed (kernel.cu:825-827).  tk_bp_select_variant(-1) restores the default
@@ -272,7 +294,8 @@ int tk_half_to_parallel(const float *d_in, int W, int N, int rows, int axis_move
  * into a CUDA graph on first use and replays it afterwards (inputs are read
  * from the submitted pointers at every run).  tk_batch_autotune times every
  * compiled tile shape of the batch's storage format on the planned batch and
- * keeps the fastest.  Storage is a coefficient image (TK_F16 by default, or
+ * keeps the fastest, after choosing each item's filter form (FFT or tensor-core
+ * Toeplitz product) by timing both.  Storage is a coefficient image (TK_F16 by default, or
  * TK_BF16 / TK_F32_COEF); W <= 2048.  Results equal tk_fdk_device's for the
  * same tile shape.  No counterpart in the reference (one volume per process).
  * A batch is not thread-safe; submitted buffers must outlive its runs. */
@@ -298,6 +321,11 @@ const char *tk_batch_variant_name(int i);
 int tk_batch_variant(const tk_batch *b);
 /* Forces a tile shape (-1: default); takes effect at the next plan. */
 int tk_batch_select_variant(tk_batch *b, int i);
+/* The filter form item i runs (tk_filter_form): TK_FILTER_AUTO until
+ * tk_batch_autotune, which times both forms on each item and keeps the faster
+ * (the tensor-core Toeplitz product only where it supports the width); -1 for
+ * a bad index. */
+int tk_batch_item_filter_form(const tk_batch *b, int i);
 
 /* ------------------------------------------------------------ diagnostics
  * tk_kernel_launches: kernels this library has launched in this process (a

@@ -10,8 +10,9 @@ Checks:
     rotation offset, scale != 1, a volume thinner than one z chunk and one
     whose depth is not a multiple of it;
   * a graph replay equals the eager run, and replays read the inputs anew;
-  * after the autotuner picks a tile shape, every item stays within the FP16
-    bound (5e-4 relative RMSE) of the FP64 oracle.
+  * after the autotuner picks each item's filter form (FFT or tensor-core
+    Toeplitz product, by timing) and a tile shape, every item stays within
+    the FP16 bound (5e-4 relative RMSE) of the FP64 oracle.
 """
 import numpy as np
 import pytest
@@ -122,6 +123,12 @@ def test_autotuned_batch_vs_fp64(orc, items):
     name, ms = b.autotune()
     assert name in [n for _, n in variants(_lib.TK_F16)] and ms > 0
     assert b.variant == name
+    # each item's filter form was chosen by timing: the FFT or (W <= 512) the tensor-core product
+    forms = b.filter_forms()
+    assert len(forms) == len(items)
+    for it, f in zip(items, forms):
+        assert f in (_lib.TK_FILTER_FFT, _lib.TK_FILTER_TOEPLITZ)
+        assert f == _lib.TK_FILTER_FFT or it["g"].W <= 512
     for v in vols:
         v.fill_(float("nan"))
     b.run(graph=True)

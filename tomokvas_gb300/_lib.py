@@ -16,6 +16,7 @@ TK_WINDOW_RAMLAK, TK_WINDOW_SHEPP_LOGAN, TK_WINDOW_HANN = 0, 1, 2
 TK_F32, TK_F16, TK_BF16, TK_F32_COEF = 0, 1, 2, 3
 TK_LAYOUT_SINOGRAM, TK_LAYOUT_PROJECTION = 0, 1
 TK_INPUT_F32, TK_INPUT_U16 = 0, 1
+TK_FILTER_AUTO, TK_FILTER_FFT, TK_FILTER_TOEPLITZ = 0, 1, 2
 
 WINDOWS = {"ramlak": TK_WINDOW_RAMLAK, "shepp_logan": TK_WINDOW_SHEPP_LOGAN, "hann": TK_WINDOW_HANN}
 PRECISIONS = {"f32": TK_F32, "f16": TK_F16, "bf16": TK_BF16, "f32c": TK_F32_COEF}
@@ -39,6 +40,7 @@ EXPORTS = [
     "tk_batch_workspace_bytes", "tk_batch_plan", "tk_batch_run", "tk_batch_autotune", "tk_batch_variant_count",
     "tk_batch_variant_name", "tk_batch_variant", "tk_batch_select_variant",
     "tk_half_to_full_fan", "tk_half_to_parallel", "tk_kernel_launches", "tk_measure_fp32_fma_rate",
+    "tk_filter_select_form", "tk_filter_form_for", "tk_batch_item_filter_form",
 ]
 
 
@@ -126,6 +128,9 @@ def _declare(L):
     L.tk_bp_variant_precision.argtypes = [ip]
     L.tk_bp_select_variant.argtypes = [ip]
     L.tk_fp_select_variant.argtypes = [ip]
+    L.tk_filter_select_form.argtypes = [ip]
+    L.tk_filter_form_for.argtypes = [ip, ip]
+    L.tk_batch_item_filter_form.argtypes = [vp, ip]
     L.tk_batch_create.argtypes = [ctypes.POINTER(vp)]
     L.tk_batch_destroy.argtypes = [vp]
     L.tk_batch_destroy.restype = None

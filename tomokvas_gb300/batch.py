@@ -55,6 +55,10 @@ class Batch:
         check(self._L.tk_batch_autotune(self._h, _stream_ptr(stream), ctypes.byref(v), ctypes.byref(ms)))
         return self._L.tk_batch_variant_name(v.value).decode(), float(ms.value)
 
+    def filter_forms(self) -> list:
+        """Filter form of every item (TK_FILTER_*): what tk_batch_autotune chose by timing."""
+        return [int(self._L.tk_batch_item_filter_form(self._h, i)) for i in range(self._L.tk_batch_size(self._h))]
+
     def select_variant(self, i: int):
         check(self._L.tk_batch_select_variant(self._h, int(i)))
 

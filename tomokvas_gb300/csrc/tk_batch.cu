@@ -277,6 +277,7 @@ struct tk_batch {
         tk_flatfield ff;
         bool has_ff;
         float *d_vol;
+        int filter_form = TK_FILTER_AUTO;  // chosen per item by tk_batch_autotune
     };
     std::vector<Input> in;
     int precision = TK_F16;
@@ -474,7 +475,8 @@ int enqueue(tk_batch *b, cudaStream_t st)
     for (int i = 0; i < n; ++i) {
         const auto &it = b->in[i];
         if (int rc = launch_filter(it.g, it.d_in, it.input_type, it.layout, it.has_ff ? &it.ff : nullptr, it.window,
-                                   b->ws + b->off_q[i], b->precision, scales + i, b->fstreams[i % K]))
+                                   b->ws + b->off_q[i], b->precision, scales + i, b->fstreams[i % K], 0, 0,
+                                   it.filter_form))
             return rc;
     }
     for (int k = 0; k < K; ++k) {
@@ -640,9 +642,43 @@ extern "C" int tk_batch_autotune(tk_batch *b, void *stream, int *variant_out, fl
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     TK_CUDA(cudaEventCreate(&e0));
     TK_CUDA(cudaEventCreate(&e1));
+    int rc = TK_OK;
+    // the filter form of each item: the FFT or the tensor-core Toeplitz product, whichever runs its
+    // filter faster (one warm-up and three timed runs each; items of one width get the same answer
+    // up to timing noise)
+    {
+        float *scales = reinterpret_cast<float *>(b->ws + b->off_scale);
+        for (size_t i = 0; i < b->in.size() && rc == TK_OK; ++i) {
+            auto &it = b->in[i];
+            float best_f = 3.0e38f;
+            int best_form = TK_FILTER_FFT;
+            for (int form : {TK_FILTER_FFT, TK_FILTER_TOEPLITZ}) {
+                if (form == TK_FILTER_TOEPLITZ && !toeplitz_supported(it.g.W, b->precision, TK_LAYOUT_PROJECTION))
+                    continue;
+                auto run = [&]() {
+                    return launch_filter(it.g, it.d_in, it.input_type, it.layout, it.has_ff ? &it.ff : nullptr,
+                                         it.window, b->ws + b->off_q[i], b->precision, scales + i, st, 0, 0, form);
+                };
+                if ((rc = run()) != TK_OK) break;
+                if (cudaEventRecord(e0, st) != cudaSuccess) { rc = TK_ERR_CUDA; break; }
+                for (int k = 0; k < 3 && rc == TK_OK; ++k) rc = run();
+                if (rc) break;
+                if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+                    rc = cuda_fail(cudaGetLastError(), "batch filter autotune timing");
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best_f) {
+                    best_f = ms;
+                    best_form = form;
+                }
+            }
+            it.filter_form = best_form;
+        }
+    }
     int best = -1;
     float best_ms = 3.0e38f;
-    int rc = TK_OK;
     for (int vi = 0; vi < kNumBatchVariants && rc == TK_OK; ++vi) {
         if (kBatchVariants[vi].precision != b->precision || kBatchVariants[vi].walk == 3) continue;
         drop_graph(b);
@@ -677,4 +713,10 @@ extern "C" int tk_batch_autotune(tk_batch *b, void *stream, int *variant_out, fl
     if (variant_out) *variant_out = best;
     if (ms_out) *ms_out = best_ms;
     return TK_OK;
+}
+
+extern "C" int tk_batch_item_filter_form(const tk_batch *b, int i)
+{
+    if (!b || i < 0 || i >= (int)b->in.size()) return -1;
+    return b->in[(size_t)i].filter_form;
 }

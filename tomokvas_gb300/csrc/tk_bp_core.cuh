@@ -13,8 +13,6 @@ __device__ __forceinline__ float flip(float v, unsigned mask)
     return __uint_as_float(__float_as_uint(v) ^ mask);
 }
 
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: a TMA stage never takes this long
-
 // Tile of CTA index i: tiles are visited in column groups kTileGroup tiles
 // wide (row by row inside a group), so the CTAs resident at one time cover a
 // compact patch of the slice whose footprints overlap in L2, rather than a

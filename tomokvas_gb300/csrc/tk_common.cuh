@@ -87,6 +87,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: no TMA stage or MMA batch takes this long
+
 // Wait for phase `parity` of `bar`, giving up after `limit_ns` nanoseconds
 // (and after a fixed number of polls).  Returns false on timeout.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint64_t limit_ns)

@@ -42,9 +42,12 @@ void build_trig(const tk_geometry &g, float *cos_out, float *sin_out, int angle0
 // Launchers (asynchronous on `stream`).
 // fgrp > 0 (coefficient images from detector frames only): the g.N frames
 // come in groups of fgrp, group k at frame k * fstride of d_in and of d_q.
+// form: TK_FILTER_FFT or TK_FILTER_TOEPLITZ forces a form (the FFT where the
+// Toeplitz product does not support the width); TK_FILTER_AUTO or -1 follows
+// filter_form_for.
 int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int layout,
                   const tk_flatfield *ff, int window, void *d_q, int precision, float *d_q_scale,
-                  cudaStream_t stream, int fgrp = 0, int fstride = 0);
+                  cudaStream_t stream, int fgrp = 0, int fstride = 0, int form = -1);
 // d_q holds g.N projections whose angle indices start at angle0 (a chunk of
 // a longer scan when angle0 > 0).
 int launch_backproject(const tk_geometry &g, const void *d_q, int precision, const float *d_q_scale,
@@ -61,6 +64,18 @@ int launch_backproject_quarter(const tk_geometry &g, const void *d_q, int precis
                                bool compact = false);
 int launch_filter_transpose(const tk_geometry &g, const float *d_qbar, int window, float *d_pbar, int layout,
                             cudaStream_t stream);
+// The ramp filter as a Toeplitz product on the tensor cores (tk_toeplitz.cu):
+// whether a width / storage format / output layout is supported, and the
+// launch (after launch_filter has set up the storage scale).  Hf is the float
+// spectrum of pad length p the FFT form multiplies by.
+struct LoadParams;
+bool toeplitz_supported(int W, int precision, int out_layout);
+int launch_filter_toeplitz(const LoadParams &L, const float *Hf, int p, void *d_q, int precision,
+                           const float *d_q_scale, long long nrows, int pitch, int fgrp, int fstride,
+                           cudaStream_t stream);
+// The filter form launch_filter runs for a width and storage format under the
+// current selection (tk_filter_select_form): TK_FILTER_FFT or TK_FILTER_TOEPLITZ.
+int filter_form_for(int W, int precision);
 int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, float zoff, float *d_qbar,
                            int accumulate, cudaStream_t stream);
 int launch_phantom(const tk_geometry &g, const double *ell, int nell, int layout, float *d_out,
