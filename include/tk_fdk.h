@@ -209,6 +209,37 @@ int tk_fdk_forward(const tk_geometry *g, const float *d_proj, int layout, int wi
 int tk_fdk_backward(const tk_geometry *g, const float *d_vol_grad, int layout, int window, void *d_workspace,
                     size_t workspace_bytes, float *d_proj_grad, void *stream);
 
+/* --------------------------------- volume data-consistency refinement
+ * Refines a volume x (the FDK volume x0 = B q to start) by gradient steps on
+ * the data-consistency loss L(x) = ||B^T x - q||^2,
+ *   x <- x - alpha B (B^T x - q),
+ * where B is the FP32 backprojection (tk_backproject with TK_F32 samples,
+ * FBPConeKernel + fQ3D of kernel.cu:68-177) and B^T its exact transpose
+ * (tk_forward_project), and q = F W p the filtered projections of the
+ * measured line integrals.  q is the only data a step needs besides x: it is
+ * checkpointed once after the filter (tk_refine_checkpoint) as FP32 samples,
+ * or as FP16 samples where HBM is short (half the bytes; the residual is
+ * formed in FP32).  A step is B^T x, one residual pass (r = -alpha (B^T x - q)
+ * and the loss), and B r accumulated into x.  alpha < 2 / lambda_max(B B^T)
+ * decreases L at every step; tk_refine_step_size returns 1 / lambda_max from a
+ * power iteration.  The workspace (tk_refine_workspace_bytes, 256-byte
+ * aligned) holds the FP32 residual.  No counterpart in the reference, which
+ * stops at the FDK volume. */
+size_t tk_refine_checkpoint_bytes(const tk_geometry *g, int precision); /* TK_F32 or TK_F16 samples [N][H][Wp] */
+size_t tk_refine_workspace_bytes(const tk_geometry *g);
+/* q = F W p (the FFT filter of the FP32 FDK) into d_ckpt [N][H][Wp]. */
+int tk_refine_checkpoint(const tk_geometry *g, const void *d_in, int input_type, int layout,
+                         const tk_flatfield *ff, int window, void *d_ckpt, int precision,
+                         void *d_workspace, size_t workspace_bytes, void *stream);
+/* `steps` gradient steps on d_vol[Z][Y][X] in place; d_loss (device, may be
+ * NULL) receives L(x_k) before step k for k < steps. */
+int tk_refine_volume(const tk_geometry *g, const void *d_ckpt, int precision, float alpha, int steps,
+                     float *d_vol, double *d_loss, void *d_workspace, size_t workspace_bytes, void *stream);
+/* 1 / lambda_max(B B^T) by `iters` power iterations from a fixed
+ * pseudo-random volume (d_vol_tmp, overwritten).  Synchronous. */
+int tk_refine_step_size(const tk_geometry *g, int iters, float *d_vol_tmp, void *d_workspace,
+                        size_t workspace_bytes, float *alpha_out, void *stream);
+
 /* Whole FDK on device buffers for callers that cannot allocate device memory:
  * a service that reserves a fixed device-memory budget at start-up and may
  * not grow it, or code inside a callback or timing-critical loop where

@@ -90,6 +90,8 @@ def _declare(L):
     L.orc_fdk_f64.argtypes = [f32p, gp, ctypes.c_int, i32p, ctypes.c_int, f64p, ctypes.c_int]
     L.orc_rows_needed.argtypes = [gp, i32p, ctypes.c_int, i32p, i32p]
     L.orc_fdk_adjoint_f64.argtypes = [f32p, gp, ctypes.c_int, f64p, ctypes.c_int]
+    L.orc_b_f64.argtypes = [f64p, gp, f64p, ctypes.c_int]
+    L.orc_bt_f64.argtypes = [f64p, gp, f64p, ctypes.c_int]
     d = ctypes.c_double
     L.orc_fdk_u16_f32_sampled.argtypes = [P(ctypes.c_uint16), d, d, d, d, ctypes.c_int, d, gp, ctypes.c_int,
                                           i32p, ctypes.c_int, f32p, ctypes.c_int]
@@ -236,6 +238,26 @@ def fdk_adjoint_f64(vol: np.ndarray, g: Geom, window="ramlak", nthreads=0) -> np
     if lib().orc_fdk_adjoint_f64(_ptr(v, ctypes.c_float), ctypes.byref(g), win, _ptr(out, ctypes.c_double),
                                  _threads(nthreads)):
         raise MemoryError("oracle adjoint failed")
+    return out
+
+
+def b_f64(q: np.ndarray, g: Geom, nthreads=0) -> np.ndarray:
+    """FP64 plain backprojection B of q [N][H][W] (scale dfi/p), volume [Z][Y][X]."""
+    x = np.ascontiguousarray(q, dtype=np.float64)
+    assert x.shape == (g.N, g.H, g.W), x.shape
+    out = np.empty((g.Z, g.Y, g.X), dtype=np.float64)
+    if lib().orc_b_f64(_ptr(x, ctypes.c_double), ctypes.byref(g), _ptr(out, ctypes.c_double), _threads(nthreads)):
+        raise MemoryError("oracle backprojection failed")
+    return out
+
+
+def bt_f64(vol: np.ndarray, g: Geom, nthreads=0) -> np.ndarray:
+    """FP64 transpose B^T of the plain backprojection: volume [Z][Y][X] -> q [N][H][W]."""
+    v = np.ascontiguousarray(vol, dtype=np.float64)
+    assert v.shape == (g.Z, g.Y, g.X), v.shape
+    out = np.empty((g.N, g.H, g.W), dtype=np.float64)
+    if lib().orc_bt_f64(_ptr(v, ctypes.c_double), ctypes.byref(g), _ptr(out, ctypes.c_double), _threads(nthreads)):
+        raise MemoryError("oracle forward projection failed")
     return out
 
 

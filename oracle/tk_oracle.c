@@ -934,6 +934,136 @@ int orc_fdk_adjoint_f64(const float *vol, const orc_geom *g, int window, double 
 }
 
 /* ------------------------------------------------------------------------ */
+/* The plain backprojection pair of the volume data-consistency refinement
+ * (tk_refine_volume), in double:
+ *   B:   vol[z][y][x] = (dfi/p) sum_b U^2 Q_b(u, v), the bilinear backprojection
+ *        of FBPConeKernel + fQ3D (kernel.cu:68-177) with the reference's final
+ *        scale delta_f * (1/p) (kernel.cu:113, 575), zero outside the detector
+ *        and outside the FOV cylinder;
+ *   B^T: its exact transpose, q[b][r][c] += (dfi/p) U^2 w_rc vol for the four
+ *        bilinear weights w_rc of every voxel.
+ * q is [N][H][W]; slice z sits at aZ = s (z - (Z-1)/2 - cz). */
+typedef struct {
+    const orc_geom *g;
+    const double *sn, *cs;
+    double fs;
+    const double *vin;
+    double *qout;
+    const double *qin;
+    double *vout;
+} orc_pair_ctx;
+
+static int orc_pair_coords(const orc_geom *g, int x, int y, int z, double *aX, double *aY, double *aZ)
+{
+    double s = g->scale;
+    *aX = s * ((double)x - g->cx);
+    *aY = s * ((double)y - g->cy);
+    *aZ = s * ((double)z - (g->Z - 1) / 2.0 - g->cz);
+    if (g->dirx) *aX = -*aX;
+    if (g->diry) *aY = -*aY;
+    if (g->dirz) *aZ = -*aZ;
+    return sqrt(*aX * *aX + *aY * *aY) < g->W / 2.0;
+}
+
+static void orc_bt_proj(void *vctx, long b)
+{
+    orc_pair_ctx *c = (orc_pair_ctx *)vctx;
+    const orc_geom *g = c->g;
+    double *q = c->qout + (size_t)b * g->H * g->W;
+    for (int z = 0; z < g->Z; ++z)
+        for (int y = 0; y < g->Y; ++y)
+            for (int x = 0; x < g->X; ++x) {
+                double aX, aY, aZ;
+                if (!orc_pair_coords(g, x, y, z, &aX, &aY, &aZ)) continue;
+                double val = c->vin[((size_t)z * g->Y + y) * g->X + x];
+                if (val == 0) continue;
+                double S = aX * c->cs[b] + aY * c->sn[b], T = aY * c->cs[b] - aX * c->sn[b];
+                double U = g->D / (g->D - S), u = T * U + g->cX, v = aZ * U + g->cZ;
+                if (u < 0 || u > g->W - 1 || v < 0 || v > g->H - 1) continue;
+                int a = (int)floor(u), r = (int)floor(v);
+                double fu = u - a, fv = v - r, w = c->fs * U * U * val;
+                q[(size_t)r * g->W + a] += w * (1 - fu) * (1 - fv);
+                if (a + 1 < g->W) q[(size_t)r * g->W + a + 1] += w * fu * (1 - fv);
+                if (r + 1 < g->H) {
+                    q[(size_t)(r + 1) * g->W + a] += w * (1 - fu) * fv;
+                    if (a + 1 < g->W) q[(size_t)(r + 1) * g->W + a + 1] += w * fu * fv;
+                }
+            }
+}
+
+static double orc_q_at(const orc_geom *g, const double *qb, int r, int c)
+{
+    return (r < g->H && c < g->W) ? qb[(size_t)r * g->W + c] : 0.0;
+}
+
+static void orc_b_row(void *vctx, long idx)
+{
+    orc_pair_ctx *c = (orc_pair_ctx *)vctx;
+    const orc_geom *g = c->g;
+    int z = (int)(idx / g->Y), y = (int)(idx % g->Y);
+    double *out = c->vout + ((size_t)z * g->Y + y) * g->X;
+    for (int x = 0; x < g->X; ++x) {
+        double aX, aY, aZ, acc = 0;
+        if (orc_pair_coords(g, x, y, z, &aX, &aY, &aZ)) {
+            for (int b = 0; b < g->N; ++b) {
+                double S = aX * c->cs[b] + aY * c->sn[b], T = aY * c->cs[b] - aX * c->sn[b];
+                double U = g->D / (g->D - S), u = T * U + g->cX, v = aZ * U + g->cZ;
+                if (u < 0 || u > g->W - 1 || v < 0 || v > g->H - 1) continue;
+                int a = (int)floor(u), r = (int)floor(v);
+                double fu = u - a, fv = v - r;
+                const double *qb = c->qin + (size_t)b * g->H * g->W;
+                double top = orc_q_at(g, qb, r, a) * (1 - fu) + orc_q_at(g, qb, r, a + 1) * fu;
+                double bot = orc_q_at(g, qb, r + 1, a) * (1 - fu) + orc_q_at(g, qb, r + 1, a + 1) * fu;
+                acc += U * U * (top * (1 - fv) + bot * fv);
+            }
+        }
+        out[x] = c->fs * acc;
+    }
+}
+
+static void orc_pair_setup(const orc_geom *g, orc_pair_ctx *c, double *trig)
+{
+    c->g = g;
+    c->sn = trig;
+    c->cs = trig + g->N;
+    for (int b = 0; b < g->N; ++b) {
+        double a = orc_angle(g, b);
+        trig[b] = sin(a);
+        trig[g->N + b] = cos(a);
+    }
+    c->fs = (double)g->dfi / (double)orc_pad_length(g->W);
+}
+
+int orc_bt_f64(const double *vol, const orc_geom *g, double *q, int nthreads)
+{
+    double *trig = (double *)malloc(sizeof(double) * 2 * (size_t)g->N);
+    if (!trig) return -1;
+    orc_pair_ctx c;
+    memset(&c, 0, sizeof(c));
+    orc_pair_setup(g, &c, trig);
+    memset(q, 0, sizeof(double) * (size_t)g->N * g->H * g->W);
+    c.vin = vol;
+    c.qout = q;
+    orc_parallel_for(g->N, nthreads, orc_bt_proj, &c);
+    free(trig);
+    return 0;
+}
+
+int orc_b_f64(const double *q, const orc_geom *g, double *vol, int nthreads)
+{
+    double *trig = (double *)malloc(sizeof(double) * 2 * (size_t)g->N);
+    if (!trig) return -1;
+    orc_pair_ctx c;
+    memset(&c, 0, sizeof(c));
+    orc_pair_setup(g, &c, trig);
+    c.qin = q;
+    c.vout = vol;
+    orc_parallel_for((long)g->Z * g->Y, nthreads, orc_b_row, &c);
+    free(trig);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* raw uint16 -> line integral (rsq::FlatFieldCorrection, rsq_load.cpp:299-325) */
 
 typedef struct {

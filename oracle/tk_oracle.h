@@ -113,6 +113,11 @@ void orc_half2para_f64(const double *in, int W, int N, int rows, int am, double 
  * backprojection (same masks and weights) and F the symmetric ramp filter.
  * vol [Z][Y][X], out [H][N][W] (double). */
 int orc_fdk_adjoint_f64(const float *vol, const orc_geom *g, int window, double *out, int nthreads);
+/* The plain backprojection B (FBPConeKernel + fQ3D, kernel.cu:68-177, scale
+ * dfi/p of kernel.cu:113, 575) and its exact transpose B^T in double, q as
+ * [N][H][W]: the pair of the volume data-consistency refinement. */
+int orc_b_f64(const double *q, const orc_geom *g, double *vol, int nthreads);
+int orc_bt_f64(const double *vol, const orc_geom *g, double *q, int nthreads);
 /* Detector rows [lo, hi] that slices zlist can touch (for sampled oracles). */
 void orc_rows_needed(const orc_geom *g, const int *zlist, int nz, int *lo, int *hi);
 

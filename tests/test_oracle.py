@@ -178,3 +178,15 @@ def test_fp64_adjoint_is_exact_transpose(orc):
         lhs = float(np.sum(orc.fdk_f64(x, G, window) * y))
         rhs = float(np.sum(x.astype(np.float64) * orc.fdk_adjoint_f64(y, G, window)))
         assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_oracle_backprojection_pair_is_a_transpose(orc):
+    """<B q, x> = <q, B^T x> in FP64 for the refinement's pair (orc_b_f64, orc_bt_f64), with a flip and a rotation."""
+    g = small_geometry(W=24, N=10, H=20, vol=(16, 14, 12), dirx=1, rot=0.4)
+    G = orc.geom_from(g)
+    rng = np.random.default_rng(2)
+    q = rng.normal(size=(g.N, g.H, g.W))
+    x = rng.normal(size=(g.Z, g.Y, g.X))
+    lhs = float(np.sum(orc.b_f64(q, G) * x))
+    rhs = float(np.sum(q * orc.bt_f64(x, G)))
+    assert abs(lhs - rhs) < 1e-12 * max(abs(lhs), 1.0)

@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB_DIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIB_DIR, "libtk_fdk.so")
-SOURCES = ["tk_capi.cu", "tk_filter.cu", "tk_bp.cu", "tk_batch.cu", "tk_phantom.cu", "tk_noalloc.cu", "tk_rebin.cu", "tk_diag.cu", "tk_toeplitz.cu"]
+SOURCES = ["tk_capi.cu", "tk_filter.cu", "tk_bp.cu", "tk_batch.cu", "tk_phantom.cu", "tk_noalloc.cu", "tk_rebin.cu", "tk_diag.cu", "tk_toeplitz.cu", "tk_refine.cu"]
 HEADERS = ["tk_common.cuh", "tk_internal.h", "tk_bp_core.cuh", "tk_filter_core.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CLI_SRC = os.path.join(PKG, "cli", "tk_para_tc.cpp")

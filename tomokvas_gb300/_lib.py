@@ -41,6 +41,8 @@ EXPORTS = [
     "tk_batch_variant_name", "tk_batch_variant", "tk_batch_select_variant",
     "tk_half_to_full_fan", "tk_half_to_parallel", "tk_kernel_launches", "tk_measure_fp32_fma_rate",
     "tk_filter_select_form", "tk_filter_form_for", "tk_batch_item_filter_form",
+    "tk_refine_checkpoint_bytes", "tk_refine_workspace_bytes", "tk_refine_checkpoint", "tk_refine_volume",
+    "tk_refine_step_size",
 ]
 
 
@@ -131,6 +133,13 @@ def _declare(L):
     L.tk_filter_select_form.argtypes = [ip]
     L.tk_filter_form_for.argtypes = [ip, ip]
     L.tk_batch_item_filter_form.argtypes = [vp, ip]
+    L.tk_refine_checkpoint_bytes.argtypes = [G, ip]
+    L.tk_refine_checkpoint_bytes.restype = ctypes.c_size_t
+    L.tk_refine_workspace_bytes.argtypes = [G]
+    L.tk_refine_workspace_bytes.restype = ctypes.c_size_t
+    L.tk_refine_checkpoint.argtypes = [G, vp, ip, ip, ctypes.POINTER(FlatField), ip, vp, ip, vp, ctypes.c_size_t, vp]
+    L.tk_refine_volume.argtypes = [G, vp, ip, fp, ip, vp, vp, vp, ctypes.c_size_t, vp]
+    L.tk_refine_step_size.argtypes = [G, ip, vp, vp, ctypes.c_size_t, ctypes.POINTER(fp), vp]
     L.tk_batch_create.argtypes = [ctypes.POINTER(vp)]
     L.tk_batch_destroy.argtypes = [vp]
     L.tk_batch_destroy.restype = None

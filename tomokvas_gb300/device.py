@@ -199,6 +199,51 @@ def fdk_backward(g, vol_grad, window=_lib.TK_WINDOW_RAMLAK, layout=_lib.TK_LAYOU
     return out
 
 
+def refine_workspace(g, device="cuda"):
+    torch = _torch()
+    return torch.empty(load().tk_refine_workspace_bytes(ctypes.byref(_geom(g))), dtype=torch.uint8, device=device)
+
+
+def refine_checkpoint(g, d_in, input_type=_lib.TK_INPUT_F32, layout=_lib.TK_LAYOUT_SINOGRAM, ff=None,
+                      window=_lib.TK_WINDOW_RAMLAK, precision=_lib.TK_F32, workspace=None, stream=None):
+    """Filtered projections q = F W p checkpointed as FP32 or FP16 samples [N][H][Wp]."""
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    dt = torch.float16 if precision == _lib.TK_F16 else torch.float32
+    ckpt = torch.empty((g.N, g.H, row_pitch(g.W)), dtype=dt, device=d_in.device)
+    ws = refine_workspace(g, d_in.device) if workspace is None else workspace
+    check(L.tk_refine_checkpoint(ctypes.byref(gc), d_in.data_ptr(), input_type, layout,
+                                 None if ff is None else ctypes.byref(ff), window, ckpt.data_ptr(), precision,
+                                 ws.data_ptr(), ws.numel(), _stream_ptr(stream)))
+    return ckpt
+
+
+def refine_step_size(g, iters=6, vol_tmp=None, workspace=None, stream=None) -> float:
+    """1 / lambda_max(B B^T) by power iteration (a step size that lowers the loss at every step)."""
+    torch = _torch()
+    L = load()
+    gc = _geom(g)
+    ws = refine_workspace(g) if workspace is None else workspace
+    v = torch.empty((g.Z, g.Y, g.X), dtype=torch.float32, device=ws.device) if vol_tmp is None else vol_tmp
+    a = ctypes.c_float(0.0)
+    check(L.tk_refine_step_size(ctypes.byref(gc), int(iters), v.data_ptr(), ws.data_ptr(), ws.numel(),
+                                ctypes.byref(a), _stream_ptr(stream)))
+    return float(a.value)
+
+
+def refine_volume(g, ckpt, vol, alpha, steps, loss=None, workspace=None, stream=None):
+    """`steps` data-consistency steps on vol in place; loss (float64 device tensor of `steps`) gets L(x_k)."""
+    L = load()
+    gc = _geom(g)
+    prec = _lib.TK_F16 if str(ckpt.dtype) == "torch.float16" else _lib.TK_F32
+    ws = refine_workspace(g, vol.device) if workspace is None else workspace
+    check(L.tk_refine_volume(ctypes.byref(gc), ckpt.data_ptr(), prec, float(alpha), int(steps), vol.data_ptr(),
+                             None if loss is None else loss.data_ptr(), ws.data_ptr(), ws.numel(),
+                             _stream_ptr(stream)))
+    return vol
+
+
 def phantom_project(g, ell: np.ndarray, layout=_lib.TK_LAYOUT_SINOGRAM, out=None, device="cuda", stream=None):
     """Analytic line integrals of ellipsoids on the GPU (FP32)."""
     torch = _torch()
