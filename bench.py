@@ -63,14 +63,15 @@ def half_math_variant():
                 L.tk_bp_variant_name(i).decode())
 
 
-# DRAM traffic of the default FP16 backprojection kernel: dram__bytes_read.sum + dram__bytes_write.sum
-# of one launch on the 64-slice, 180-projection slab case (bench.py --profile-bp f16, one ncu pass),
-# scaled to the 1024^3 / 720-projection launch by the ratio of voxel-projection updates (64: 16x the
-# z chunks, each streaming 4x the projections).  source_sha1 is the sha1 of tk_bp.cu + tk_bp_core.cuh
-# at capture: a later source reports the traffic as stale (null) instead of a frozen number.
-BP_TRAFFIC = {"kernel": None, "slab_bytes": None, "scale": 64, "source_sha1": None,
+# DRAM traffic of the default FP16 backprojection kernel at the 1024^3 / 720-projection launch:
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch, captured with those two metrics alone
+# (one ncu pass on the 64-slice slab case, so the full-size launch is captured in one pass, nothing saved or
+# restored).  source_sha1 is the sha1 of tk_bp.cu + tk_bp_core.cuh at capture: a later source reports the
+# traffic as stale (null) instead of a frozen number.
+BP_TRAFFIC = {"kernel": "bp_quad<f16,16,8,16,2,cap6144,f32i,issue1,geo1>", "bytes_per_launch": 261.87e9 + 4.30e9,
+              "source_sha1": "e13d18876fd965f5a98fcd1d512d396d08d0b2e6",
               "capture": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none "
-                         "-k regex:bp_quad -c 1 python bench.py --profile-bp f16"}
+                         "-k regex:bp_quad -c 1 python bench.py --steps 1 --warmup 1 --no-e2e --no-rmse --no-extras"}
 
 
 def bp_source_sha1():
@@ -91,6 +92,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-rmse", action="store_true", help="skip the FP64 oracle accuracy check")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batch and adjoint summaries")
     ap.add_argument("--variant", type=int, default=-1, help="backprojection kernel variant (-1 = default)")
     ap.add_argument("--adjoint", action="store_true",
                     help="differentiation workload: 512^3 (scale 1.5) from 360 x 768^2 FP32 projections, "
@@ -115,6 +117,9 @@ def parse():
                     help="small case for ncu: the u16 log + Hann filter of 90 x 1024^2 projections into one "
                          "storage format; one untimed and two timed launches")
     ap.add_argument("--sweep", action="store_true", help="with --profile-bp: time every variant of that precision")
+    ap.add_argument("--filter-width", type=int, default=1024, help="with --profile-filter: detector width (and height)")
+    ap.add_argument("--filter-form", choices=["auto", "fft", "toeplitz"], default="auto",
+                    help="with --profile-filter: the filter form (tk_filter_select_form)")
     ap.add_argument("--profile-bp", choices=["f32", "f16", "bf16", "f32c"], default=None,
                     help="small case for ncu: 180 x 1024^2 projections, a 64-slice slab of the 1024^2 volume; "
                          "one untimed and two timed backprojection launches")
@@ -383,6 +388,14 @@ def run_ours(args):
     plain_alt = {k: {"ms_per_step": v[0][0], "bp_ms": v[0][2], "filter_ms": v[0][1],
                      "kernel": bp_kernel_name(-1, _lib.TK_F32 if k == "f32" else _lib.TK_F32_COEF)}
                  for k, v in plain_runs.items()}
+    # the FP32-coefficient quarter-turn kernel (selectable; the general walk is the faster FP32 form): the
+    # chosen form's algorithm with FP32 storage, for the ratio on matched kernels
+    qf32 = next(i for i in range(L.tk_bp_variant_count()) if L.tk_bp_variant_name(i).decode().startswith("quad<f32c,"))
+    _lib.check(L.tk_bp_select_variant(qf32))
+    try:
+        ms_q32, _, q32_bp, _ = timed(_lib.TK_F32_COEF, K, W)
+    finally:
+        _lib.check(L.tk_bp_select_variant(args.variant))
     # the selectable FP16 half-math form (FP16 interpolation arithmetic): reported beside, not the headline
     hm = half_math_variant()
     _lib.check(L.tk_bp_select_variant(hm))
@@ -461,6 +474,16 @@ def run_ours(args):
             dist.destroy_process_group()
         return 0
 
+    # compact summaries of the batched (64 uneven volumes) and differentiation (512^3 from
+    # 360 x 768^2) workloads, after the headline's timed regions
+    extras = {}
+    if not args.no_extras:
+        torch.cuda.empty_cache()
+        extras["c3_batch"] = batch_summary(steps=3, warmup=1)
+        torch.cuda.empty_cache()
+        extras["c4_adjoint"] = adjoint_summary(steps=3, warmup=1)
+        torch.cuda.empty_cache()
+
     # accuracy on sampled slices vs the FP64 oracle (untimed)
     rmse = None
     if not args.no_rmse:
@@ -491,11 +514,10 @@ def run_ours(args):
     fp32_peak = fma_peak.value
     kname = bp_kernel_name(args.variant)
     traffic, traffic_note = None, "no capture recorded for this kernel"
-    if BP_TRAFFIC["kernel"] == kname and BP_TRAFFIC["slab_bytes"]:
+    if BP_TRAFFIC["kernel"] == kname:
         if BP_TRAFFIC["source_sha1"] == bp_source_sha1():
-            traffic = int(BP_TRAFFIC["slab_bytes"] * BP_TRAFFIC["scale"])
-            traffic_note = (f"ncu capture of the 64-slice / 180-projection slab case scaled x{BP_TRAFFIC['scale']} "
-                            f"by updates; {BP_TRAFFIC['capture']}")
+            traffic = int(BP_TRAFFIC["bytes_per_launch"])
+            traffic_note = f"one-pass ncu capture of a full-size launch: {BP_TRAFFIC['capture']}"
         else:
             traffic_note = "stale: the backprojection source changed after the capture"
     peaks = {}
@@ -520,6 +542,10 @@ def run_ours(args):
                   "filter_ms": f32_filter, "bp_ms": f32_bp, "formats": plain_alt},
         "chosen_vs_plain": plain and value / plain,
         "chosen_vs_plain_kernels": [kname, plain_alt[plain_name]["kernel"]],
+        "chosen_vs_plain_matched": {"ratio": ms_q32 / ms16, "kernels": [kname, "bp_" + L.tk_bp_variant_name(qf32).decode()],
+                                    "plain_ms_per_step": ms_q32, "plain_bp_ms": q32_bp,
+                                    "note": "both quarter-turn kernels with FP32 interpolation; storage FP16 vs FP32 "
+                                            "coefficients (8 vs 16 B per entry)"},
         "bf16": {"value": replica_gups(upd, world, ms_bf * 1e-3), "unit": "GUPS", "ms_per_step": ms_bf,
                  "bp_ms": bf_bp, "filter_ms": bf_filter, "kernel": bp_kernel_name(-1, _lib.TK_BF16),
                  "dtype": "bf16-stored filtered projections, f32 bilinear interpolation and accumulation",
@@ -551,6 +577,7 @@ def run_ours(args):
         "cpu_baseline": {"value": cpu_gups, "unit": "GUPS", "cores": cores, "kind": "port", "sample": sample,
                          "seconds": cpu_s},
         "clocks": clocks,
+        **extras,
     }
     emit(out)
     if dist:
@@ -609,7 +636,14 @@ def run_profile_filter(args):
     _build.build()
     torch.cuda.set_device(0)
     g = workload().replace(N=90, dfi=float(np.float32(2.0 * np.pi / 90)))
+    if args.filter_width != g.W:  # 360 frames of W x W at the same geometry
+        Wf = args.filter_width
+        g = g.replace(N=360, dfi=float(np.float32(2.0 * np.pi / 360)), W=Wf, H=Wf, cX=(Wf - 1) / 2.0,
+                      cZ=(Wf - 1) / 2.0, X=min(g.X, Wf), Y=min(g.Y, Wf), Z=min(g.Z, Wf))
     prec = _lib.PRECISIONS[args.profile_filter]
+    L = _lib.load()
+    _lib.check(L.tk_filter_select_form({"auto": _lib.TK_FILTER_AUTO, "fft": _lib.TK_FILTER_FFT,
+                                        "toeplitz": _lib.TK_FILTER_TOEPLITZ}[args.filter_form]))
     line = device.phantom_project(g, phantom(g), _lib.TK_LAYOUT_PROJECTION)
     gen = torch.Generator(device="cuda").manual_seed(PHANTOM_SEED)
     raw = torch.poisson(I0 * torch.exp(-line), generator=gen).clamp_(0, 65535).to(torch.int32).to(torch.int16)
@@ -632,25 +666,27 @@ def run_profile_filter(args):
     ms = e0.elapsed_time(e1) / 2
     samples = g.N * g.H * g.W
     out_bytes = device.filtered_bytes(g, prec)
-    emit({"profile_filter": args.profile_filter, "ms_per_call": ms, "samples": samples,
+    emit({"profile_filter": args.profile_filter, "W": g.W, "N": g.N,
+          "form": "toeplitz" if L.tk_filter_form_for(g.W, prec) == _lib.TK_FILTER_TOEPLITZ else "fft",
+          "ms_per_call": ms, "samples": samples,
           "gsamples_per_s": samples / (ms * 1e-3) / 1e9,
           "hbm_algorithmic_gbs": (samples * 2 + out_bytes) / (ms * 1e-3) / 1e9,
           "flags": device.device_error_flags()})
     return 0
 
 
-def run_adjoint(args):
-    """A and A^T on the 512^3 / 360 x 768^2 differentiation workload."""
+def adjoint_summary(steps, warmup, column_lanes=False, descent_p=False, refine_steps=20, profile=False):
+    """A and A^T on the 512^3 / 360 x 768^2 differentiation workload: times, the full-size dot-product
+    test, and data-consistency steps on the volume from the FDK volume (tk_refine_volume, filtered
+    projections checkpointed in FP16)."""
     import torch
 
-    from tomokvas_gb300 import _build, _lib, device
+    from tomokvas_gb300 import _lib, device
     from tomokvas_gb300.geometry import FDKGeometry, config
     from tomokvas_gb300.phantom import random_ellipsoids
 
-    _build.build()
-    torch.cuda.set_device(0)
     g = config("c4")
-    if args.profile_adjoint:
+    if profile:
         g = FDKGeometry.circular(120, 768, 768, 0.2, 400.0, 800.0, (512, 512, 512), 0.15)
     ell = random_ellipsoids(20, g.fov_radius_cm, g.Z * g.voxel_cm / 2, seed=4)
     p = device.phantom_project(g, ell, _lib.TK_LAYOUT_SINOGRAM)
@@ -667,41 +703,37 @@ def run_adjoint(args):
     def bwd():
         device.fdk_backward(g, y, workspace=ws, out=grad)
 
+    def timeit(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
     res = {}
     L = _lib.load()
-    try:  # the column-lane forward projector, timed beside the default
-        _lib.check(L.tk_fp_select_variant(1))
-        for _ in range(args.warmup):
-            bwd()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(args.steps):
-            bwd()
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
-        res["backward_column_lanes"] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
-    finally:
-        _lib.check(L.tk_fp_select_variant(0))
+    if column_lanes:  # the column-lane forward projector, timed beside the default
+        try:
+            _lib.check(L.tk_fp_select_variant(1))
+            ms = timeit(bwd)
+            res["backward_column_lanes"] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
+        finally:
+            _lib.check(L.tk_fp_select_variant(0))
     for name, fn in (("forward", fwd), ("backward", bwd)):
-        for _ in range(args.warmup):
-            fn()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(args.steps):
-            fn()
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
+        ms = timeit(fn)
         res[name] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
+    res["backward_over_forward"] = res["backward"]["ms"] / res["forward"]["ms"]
     lhs = float(torch.sum(vol.double() * y.double()).item())
     rhs = float(torch.sum(p.double() * grad.double()).item())
-    descent = None
-    if not args.profile_adjoint:
-        # 20 data-consistency steps p <- p - a grad ||A p - t||^2 from the noisy projections toward the
-        # volume of the noise-free ones (t = A p_clean); a from a power-iteration estimate of ||A||^2
+    res["dot_product_rel_err"] = abs(lhs - rhs) / abs(lhs)
+    if descent_p:
+        # 20 steps p <- p - a grad ||A p - t||^2 from the noisy projections toward the volume of the
+        # noise-free ones (t = A p_clean); a from a power-iteration estimate of ||A||^2
         clean = device.phantom_project(g, ell, _lib.TK_LAYOUT_SINOGRAM)
         t = torch.empty_like(vol)
         device.fdk_device(g, clean, workspace=ws, vol=t)
@@ -717,10 +749,6 @@ def run_adjoint(args):
         pk = p.clone()
         losses = []
         float(torch.sum(t.double() ** 2).item())  # the loss reduction's first use loads its kernel (seconds)
-        uuid = str(getattr(torch.cuda.get_device_properties(0), "uuid", "") or "")
-        sampler = ClockSampler(uuid or None)
-        sampler.start()
-        time.sleep(0.4)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -732,17 +760,50 @@ def run_adjoint(args):
             pk.add_(grad, alpha=-a)
         e1.record()
         torch.cuda.synchronize()
-        clocks = sampler.stop()
         ls = [float(x.item()) for x in losses]
-        descent = {"steps": 20, "ms_per_step": e0.elapsed_time(e1) / 20, "step_size": a,
-                   "loss_first": ls[0], "loss_last": ls[-1], "loss_ratio": ls[-1] / ls[0],
-                   "monotone": all(b < c for c, b in zip(ls, ls[1:])), "clocks": clocks,
-                   "per_step": "A (fdk_device, FP32 samples) + residual + A^T (fdk_backward) + update; the "
-                               "linear A needs no activations of the forward for the gradient, so nothing is "
-                               "checkpointed: one workspace of filtered projections serves A and A^T"}
-    emit({"workload": f"fdk_adjoint_512cube_scale1.5_from_{g.N}x768sq_f32", "updates": g.updates, **res,
-          "dot_product_rel_err": abs(lhs - rhs) / abs(lhs), "descent": descent,
-          "flags": device.device_error_flags()})
+        res["descent_on_projections"] = {
+            "steps": 20, "ms_per_step": e0.elapsed_time(e1) / 20, "step_size": a, "loss_ratio": ls[-1] / ls[0],
+            "monotone": all(b < c for c, b in zip(ls, ls[1:]))}
+        del pk, t
+    if refine_steps > 0:
+        # volume refinement x <- x - alpha B (B^T x - q) from the FDK volume, q checkpointed in FP16
+        del grad
+        rws = device.refine_workspace(g)
+        ck = device.refine_checkpoint(g, p, precision=_lib.TK_F16, workspace=rws)
+        alpha = device.refine_step_size(g, iters=6, vol_tmp=y, workspace=rws)
+        x = torch.empty((g.Z, g.Y, g.X), device="cuda")
+        device.fdk_device(g, p, workspace=ws, vol=x)
+        loss = torch.zeros(refine_steps, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = L.tk_kernel_launches()
+        e0.record()
+        device.refine_volume(g, ck, x, alpha, refine_steps, loss=loss, workspace=rws)
+        e1.record()
+        torch.cuda.synchronize()
+        ls = loss.cpu().numpy()
+        res["refine_volume"] = {
+            "steps": refine_steps, "ms_per_step": e0.elapsed_time(e1) / refine_steps, "step_size": alpha,
+            "loss_first": float(ls[0]), "loss_last": float(ls[-1]), "loss_ratio": float(ls[-1] / ls[0]),
+            "monotone": bool(np.all(np.diff(ls) < 0)),
+            "launches_per_step": (L.tk_kernel_launches() - n0) / refine_steps,
+            "checkpoint": "filtered projections q = F W p as FP16 samples (0.42 GB instead of 0.85 GB FP32)",
+            "per_step": "B^T x (scatter forward projector) + residual -alpha (B^T x - q) with the loss + "
+                        "B r accumulated into x (FP32 backprojector)"}
+        del rws, ck, x
+    res["flags"] = device.device_error_flags()
+    return {"workload": f"fdk_adjoint_512cube_scale1.5_from_{g.N}x768sq_f32", "updates": g.updates, **res}
+
+
+def run_adjoint(args):
+    import torch
+
+    from tomokvas_gb300 import _build
+
+    _build.build()
+    torch.cuda.set_device(0)
+    emit(adjoint_summary(args.steps, args.warmup, column_lanes=True, descent_p=not args.profile_adjoint,
+                         refine_steps=0 if args.profile_adjoint else 20, profile=args.profile_adjoint))
     return 0
 
 
@@ -838,18 +899,16 @@ def batch_geometries(n=64, seed=3):
     return out
 
 
-def run_batch(args):
+def batch_summary(steps, warmup, items=64):
     """64 uneven reconstructions: one launch per volume vs the batched persistent launch (eager and as a
-    CUDA graph), after the autotuner picked the batch's tile shape."""
+    CUDA graph), after the autotuner picked each item's filter form and the batch's tile shape."""
     import torch
 
-    from tomokvas_gb300 import _build, _lib, device
+    from tomokvas_gb300 import _lib, device
     from tomokvas_gb300.batch import Batch
     from tomokvas_gb300.phantom import random_ellipsoids
 
-    _build.build()
-    torch.cuda.set_device(0)
-    geos = batch_geometries()[:max(1, args.items)]
+    geos = batch_geometries()[:max(1, items)]
     prec = _lib.TK_F16
     ins, vols, wss = [], [], []
     for k, g in enumerate(geos):
@@ -861,16 +920,16 @@ def run_batch(args):
     stream = torch.cuda.current_stream()
 
     def timeit(fn):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             fn()
         e1.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / args.steps
+        return e0.elapsed_time(e1) / steps
 
     def per_volume():
         for g, x, v, w in zip(geos, ins, vols, wss):
@@ -883,21 +942,36 @@ def run_batch(args):
         b.submit(g, x, v)
     b.plan()
     tuned, tune_ms = b.autotune()
+    forms = b.filter_forms()
     ms_eager = timeit(lambda: b.run(graph=False))
     ms_graph = timeit(lambda: b.run(graph=True))
     diff = max(float(np.abs(v[v.shape[0] // 2].cpu().numpy() - r).max() / max(np.abs(r).max(), 1e-30))
                for v, r in zip(vols, ref))
     flags = device.device_error_flags()
-    emit({"workload": f"batch_{len(geos)}_uneven_fdk", "metric": "GUPS", "unit": "GUPS", "items": len(geos),
-          "updates": updates, "storage": "f16 coefficients", "steps": args.steps, "warmup": args.warmup,
-          "per_volume": {"ms": ms_single, "gups": updates / (ms_single * 1e-3) / 1e9},
-          "batch_eager": {"ms": ms_eager, "gups": updates / (ms_eager * 1e-3) / 1e9},
-          "batch_graph": {"ms": ms_graph, "gups": updates / (ms_graph * 1e-3) / 1e9},
-          "speedup_graph_vs_per_volume": ms_single / ms_graph, "autotuned_variant": tuned,
-          "autotune_ms": tune_ms, "max_rel_diff_vs_per_volume_mid_slices": diff, "flags": flags,
-          "detector_widths": sorted({g.W for g in geos}),
-          "data": f"synthetic: {len(geos)} seeded 20-ellipsoid phantoms, analytic FP32 line integrals (no dataset)"})
+    by_width = {}
+    for g, f in zip(geos, forms):
+        k = "toeplitz" if f == _lib.TK_FILTER_TOEPLITZ else "fft"
+        by_width.setdefault(str(g.W), {"fft": 0, "toeplitz": 0})[k] += 1
     b.close()
+    return {"workload": f"batch_{len(geos)}_uneven_fdk", "metric": "GUPS", "unit": "GUPS", "items": len(geos),
+            "updates": updates, "storage": "f16 coefficients, f32 interpolation", "steps": steps, "warmup": warmup,
+            "per_volume": {"ms": ms_single, "gups": updates / (ms_single * 1e-3) / 1e9},
+            "batch_eager": {"ms": ms_eager, "gups": updates / (ms_eager * 1e-3) / 1e9},
+            "batch_graph": {"ms": ms_graph, "gups": updates / (ms_graph * 1e-3) / 1e9},
+            "speedup_graph_vs_per_volume": ms_single / ms_graph, "autotuned_variant": tuned,
+            "autotune_ms": tune_ms, "filter_forms_by_width": by_width,
+            "max_rel_diff_vs_per_volume_mid_slices": diff, "flags": flags,
+            "data": f"synthetic: {len(geos)} seeded 20-ellipsoid phantoms, analytic FP32 line integrals (no dataset)"}
+
+
+def run_batch(args):
+    import torch
+
+    from tomokvas_gb300 import _build
+
+    _build.build()
+    torch.cuda.set_device(0)
+    emit(batch_summary(args.steps, args.warmup, args.items))
     return 0
 
 

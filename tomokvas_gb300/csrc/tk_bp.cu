@@ -1125,7 +1125,7 @@ struct BPVariant {
 // The first entry of each storage format is its default.  Every default
 // interpolates in FP32 (FP32 geometry, interpolation weights, interpolation and
 // accumulation; 16-bit storage converted exactly to FP32).  Where a format has
-// quarter-turn variants its first entry is one; the automatic quarter-turn
+// automatic quarter-turn variants (FP16 and BF16) its first entry is one; the automatic quarter-turn
 // alternatives (qauto, in table order) take larger footprints, and a scan
 // without the symmetry runs the format's first general entry.  FP16 storage:
 // the quarter-turn kernel with 16 x 8 tiles, else walk 4.  The half-math
@@ -1136,13 +1136,15 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG_F(TK_F16, "f16", 16, 16, 64, 3, 2),
     TK_BP_QUADF(TK_BF16, "bf16", 6144, 2, true, 8),
     TK_BP_CIMG_F(TK_BF16, "bf16", 16, 16, 64, 3, 2),
-    TK_BP_QUADF(TK_F32_COEF, "f32c", 13312, 2, true, 16),
     TK_BP_CIMG_PK(TK_F32_COEF, "f32c", 16, 16, 64, 2, 2),
     TK_BP_DIRECT(16, 16, 32, 4),
     TK_BP_QUADF(TK_F16, "f16", 8192, 2, true, 16),   // 16 x 16 tiles when a 16 x 8 tile's footprint exceeds 6 KB
     TK_BP_QUADF(TK_F16, "f16", 13824, 2, true, 16),  // footprints of up to 13.5 KB (scales near 1.5)
     TK_BP_QUADF(TK_BF16, "bf16", 8192, 2, true, 16),
     TK_BP_QUADF(TK_BF16, "bf16", 13824, 2, true, 16),
+    // FP32 coefficients by quarter turns (selectable): 16 bytes of shared memory per voxel update keep
+    // it at the shared-memory bandwidth, where it runs slower than the general walk above
+    TK_BP_QUADF(TK_F32_COEF, "f32c", 13312, 2, false, 16),
     TK_BP_QUADH(6144, 2, 1, 1, false, 1, 8),  // the FP16 half-math forms
     TK_BP_QUADH(8192, 2, 1, 1, false, 1, 16),
     TK_BP_QUADH(13824, 2, 1, 1, false, 1, 16),
