@@ -251,9 +251,13 @@ int tk_refine_step_size(const tk_geometry *g, int iters, float *d_vol_tmp, void 
  * TK_ERR_UNSUPPORTED and a message.  The caller still passes the input and
  * the output volume.  Every GPU that loads the library holds the array until
  * the process exits.  The first call on a device looks the array up (with
- * that device current), so make it before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race and must be serialised.
- * Allocates nothing.  No counterpart in the reference. */
+ * that device current) and, with lazy module loading, loads the kernels it
+ * runs: make one warm-up call per device before fixing the memory budget or
+ * starting a stream capture.  A cudaDeviceReset after it invalidates the
+ * looked-up address.  All calls share the array: calls that overlap on the
+ * GPU race and must be serialised.  Allocates no device memory (the first call
+ * with a new filter setting fills a host-side cache of its spectrum).  No
+ * counterpart in the reference. */
 int tk_fdk_device_noalloc(const tk_geometry *g, const void *d_in, int input_type, int layout,
                           const tk_flatfield *ff, int window, int precision, float *d_vol, void *stream);
 
@@ -366,6 +370,16 @@ int tk_batch_item_filter_form(const tk_batch *b, int i);
  * FP32-pipe ceiling the backprojection is measured against.  Synchronous. */
 unsigned long long tk_kernel_launches(void);
 int tk_measure_fp32_fma_rate(double *tflops_out);
+/* Self-check exercises (tests of the failure reporting; nothing faults):
+ * tk_diag_wait_timeout launches one CTA that waits, with the library's bounded
+ * wait and the given limit, on an mbarrier armed for copies that are never
+ * issued; it leaves ERR_WAIT_TIMEOUT (0x2) in the device error word, read by
+ * tk_device_error_flags.  tk_diag_shrink_box(rows) takes `rows` rows off every
+ * backprojection's staged footprint box from then on (0 restores it): the
+ * kernels' bounds checks then skip the reads that fall outside and report
+ * ERR_BOX_OVERFLOW (0x1), which the handle returns as TK_ERR_DEVICE. */
+int tk_diag_wait_timeout(double limit_ms, void *stream);
+int tk_diag_shrink_box(int rows);
 
 /* ------------------------------ FilteredBackProjection mirror (handle) */
 /* One handle = one FilteredBackProjection object (kernel.cuh:82-151).
@@ -390,6 +404,7 @@ int tk_fdk_set_allocation_limit(tk_fdk *h, long long bytes);       /* SetAllocat
 int tk_fdk_set_collecting(tk_fdk *h, int collecting);              /* SetCollecting kernel.cu:293-296 */
 int tk_fdk_set_show_info(tk_fdk *h, int show);                     /* SetShowInfo kernel.cu:298-301 */
 int tk_fdk_set_axis_direction(tk_fdk *h, int x, int y, int z);     /* SetAxisDirection kernel.cu:499-507 */
+int tk_fdk_show_info(tk_fdk *h);                                   /* fShowInfo kernel.cu:901-913, on stdout */
 int tk_fdk_set_sinogram_properties(tk_fdk *h, const float *sinogram, int W, float cX, int N, int H,
                                    float cZ, float dfi, float D, float tau); /* kernel.cu:479-497 */
 int tk_fdk_set_reconstruction_properties(tk_fdk *h, int X, float cx, int Y, float cy, int Z, float cz,

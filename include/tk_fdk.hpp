@@ -69,6 +69,14 @@ public:
         return status(tk_fdk_calculate_reconstruction(h_, get_block_, this));
     }
 
+    // The reference uploads its per-angle sin/cos tables here (kernel.cu:430-471);
+    // this engine forms them on the host for every launch (the same FP64 sin/cos
+    // of the FP32 angle), so there is nothing to prepare ahead of the call.
+    cudaError_t CalcSinCos() { return cudaSuccess; }
+
+    // Device summary on stdout, as kernel.cu:901-913 prints it.
+    void fShowInfo() { report(tk_fdk_show_info(h_)); }
+
     static size_t GetFreeMemInfo(int _GPUId) { return tk_get_free_mem_info(_GPUId); }
 
     // access to the extensions of the C ABI (filters, storage, raw input)

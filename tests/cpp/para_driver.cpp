@@ -52,6 +52,11 @@ int main(int argc, char **argv)
         delete FBP;
         return 1;
     }
+    if (FBP->CalcSinCos() != cudaSuccess) {
+        delete FBP;
+        return 1;
+    }
+    FBP->fShowInfo();
     std::vector<float>().swap(data);  // the data now lives on the GPU (para_TC.cpp:150)
     const cudaError_t rc = FBP->CalculateReconstruction();
     delete FBP;

@@ -48,5 +48,6 @@ def test_cpp_driver_reconstructs(orc, cuda, driver, tmp_path):
     sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=3), G, "sino")
     r, dst = run(driver, tmp_path, g, sino)
     assert r.returncode == 0, r.stderr
+    assert "Multi-Processors" in r.stdout  # fShowInfo
     vol = np.fromfile(dst, dtype=np.float32).reshape(g.Z, g.Y, g.X)
     assert rel_rmse(vol, orc.fdk_f32(sino, G)) < 1e-5

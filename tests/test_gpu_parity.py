@@ -276,6 +276,36 @@ def test_quarter_turn_half_math_forms(orc, cuda, Z):
     assert rel_rmse(vols[0], ref) <= rel_rmse(vols[3], ref) * 1.05
 
 
+def test_quarter_turn_integer_widening(orc, cuda):
+    """The FP16 quarter-turn forms that widen the stored halves on the integer
+    pipe (values scaled by 2^-112, the scale undone by the row fraction or by
+    U^2, powers of two) do the default form's FP32 operations: the volumes agree
+    to the last bits (a subnormal scaled intermediate would differ by 2^-37 of
+    its unscaled value)."""
+    import torch
+
+    L = _lib.load()
+    names = _names(L)
+    forms = [i for i, n in enumerate(names) if n.startswith("quad<f16,") and ",f32i_int" in n]
+    assert len(forms) == 2
+    g = small_geometry(W=64, N=120, H=64, vol=(64, 64, 40))
+    G = orc.geom_from(g)
+    sino = orc.project_ellipsoids(head_phantom(g.fov_radius_cm * 0.8, seed=11), G, "sino")
+    d_in = to_dev(sino, torch)
+    vols = []
+    try:
+        for sel in [-1] + forms:
+            _lib.check(L.tk_bp_select_variant(sel))
+            vols.append(device.fdk_device(g, d_in, precision=_lib.TK_F16).cpu().numpy())
+    finally:
+        _lib.check(L.tk_bp_select_variant(-1))
+    assert device.device_error_flags() == 0
+    peak = float(np.abs(vols[0]).max())
+    for v in vols[1:]:
+        assert float(np.abs(v - vols[0]).max()) <= 1e-6 * peak
+    assert rel_rmse(vols[1], orc.fdk_f64(sino, G)) < F16_RMSE
+
+
 @pytest.mark.parametrize("N,rot,Z", [(8, 0.3, 24),       # two projections per quarter, rotated scan
                                       (360, 1.0, 40),     # a rotation of about a radian
                                       (3200, 0.0, 8)])    # the most angles one launch carries

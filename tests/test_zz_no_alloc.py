@@ -44,6 +44,13 @@ def test_noalloc_matches_workspace_entry_point(orc, cuda):
             got = vol.cpu().numpy()
             assert np.isfinite(got).all()
             assert rel_rmse(got, ref) <= F32_RMSE, (prec, call)
+        # a warmed-up call takes no device memory: the free bytes do not move across one more call
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        rc = L.tk_fdk_device_noalloc(ctypes.byref(gc), d_in.data_ptr(), _lib.TK_INPUT_F32, _lib.TK_LAYOUT_SINOGRAM,
+                                     None, _lib.TK_WINDOW_RAMLAK, prec, vol.data_ptr(), stream)
+        torch.cuda.synchronize()
+        assert rc == _lib.TK_OK and torch.cuda.mem_get_info()[0] == free0
     assert device.device_error_flags() == 0
 
 

@@ -31,7 +31,7 @@ EXPORTS = [
     "tk_forward_project", "tk_filter_transpose", "tk_fdk_forward", "tk_fdk_backward", "tk_phantom_project", "tk_bp_variant_count",
     "tk_bp_variant_name", "tk_bp_variant_precision", "tk_bp_select_variant", "tk_fp_select_variant", "tk_fdk_create", "tk_fdk_destroy",
     "tk_fdk_set_gpu_id", "tk_fdk_set_block_size", "tk_fdk_set_allocation_limit", "tk_fdk_set_collecting",
-    "tk_fdk_set_show_info", "tk_fdk_set_axis_direction", "tk_fdk_set_sinogram_properties",
+    "tk_fdk_set_show_info", "tk_fdk_show_info", "tk_fdk_set_axis_direction", "tk_fdk_set_sinogram_properties",
     "tk_fdk_set_reconstruction_properties", "tk_fdk_set_scale_xyz", "tk_fdk_set_projections_u16",
     "tk_fdk_set_input_layout", "tk_fdk_set_filter", "tk_fdk_set_precision", "tk_fdk_set_stream",
     "tk_fdk_set_pipeline",
@@ -42,7 +42,7 @@ EXPORTS = [
     "tk_half_to_full_fan", "tk_half_to_parallel", "tk_kernel_launches", "tk_measure_fp32_fma_rate",
     "tk_filter_select_form", "tk_filter_form_for", "tk_batch_item_filter_form",
     "tk_refine_checkpoint_bytes", "tk_refine_workspace_bytes", "tk_refine_checkpoint", "tk_refine_volume",
-    "tk_refine_step_size",
+    "tk_refine_step_size", "tk_diag_wait_timeout", "tk_diag_shrink_box",
 ]
 
 
@@ -140,6 +140,8 @@ def _declare(L):
     L.tk_refine_checkpoint.argtypes = [G, vp, ip, ip, ctypes.POINTER(FlatField), ip, vp, ip, vp, ctypes.c_size_t, vp]
     L.tk_refine_volume.argtypes = [G, vp, ip, fp, ip, vp, vp, vp, ctypes.c_size_t, vp]
     L.tk_refine_step_size.argtypes = [G, ip, vp, vp, ctypes.c_size_t, ctypes.POINTER(fp), vp]
+    L.tk_diag_wait_timeout.argtypes = [ctypes.c_double, vp]
+    L.tk_diag_shrink_box.argtypes = [ip]
     L.tk_batch_create.argtypes = [ctypes.POINTER(vp)]
     L.tk_batch_destroy.argtypes = [vp]
     L.tk_batch_destroy.restype = None
@@ -167,7 +169,7 @@ def _declare(L):
     for name, args in [
         ("tk_fdk_set_gpu_id", [ip]), ("tk_fdk_set_block_size", [ip]),
         ("tk_fdk_set_allocation_limit", [ctypes.c_longlong]), ("tk_fdk_set_collecting", [ip]),
-        ("tk_fdk_set_show_info", [ip]), ("tk_fdk_set_axis_direction", [ip, ip, ip]),
+        ("tk_fdk_set_show_info", [ip]), ("tk_fdk_show_info", []), ("tk_fdk_set_axis_direction", [ip, ip, ip]),
         ("tk_fdk_set_sinogram_properties", [vp, ip, fp, ip, ip, fp, fp, fp, fp]),
         ("tk_fdk_set_reconstruction_properties", [ip, fp, ip, fp, ip, fp, fp]),
         ("tk_fdk_set_scale_xyz", [fp]),

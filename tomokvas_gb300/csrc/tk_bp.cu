@@ -527,6 +527,7 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
         float fvp[2][2], wp[2][2];
         uint32_t fvh[2], wh[2];
         const __half2 U2h2 = __float2half2_rn(U2);
+        const float U2w = INTERP == 3 ? U2 * kF16IntScale : U2;  // INTERP 3: every value scaled by 2^-112
         const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
         auto fetch = [&](int z, int bi) {
             const bool bin = !PARTIAL || z + 1 <= zlast;
@@ -538,11 +539,12 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
             const uint32_t rb = (uint32_t)__float_as_int(flb) * row_bytes + sbase;
             const bool ina = all_in || (va >= 0.f && va <= Hm1);  // kernel.cu:130-131
             const bool inb = bin && (all_in || (vb >= 0.f && vb <= Hm1));
-            if constexpr (INTERP == 1) {
-                fvp[bi][0] = fva;
-                fvp[bi][1] = fvb;
-                wp[bi][0] = ina ? U2 : 0.f;
-                wp[bi][1] = inb ? U2 : 0.f;
+            if constexpr (INTERP >= 1) {
+                // INTERP 2: B comes out scaled by 2^-112 (its halves widened on the integer pipe)
+                fvp[bi][0] = INTERP == 2 ? fva * kF16IntScale : fva;
+                fvp[bi][1] = INTERP == 2 ? fvb * kF16IntScale : fvb;
+                wp[bi][0] = ina ? U2w : 0.f;
+                wp[bi][1] = inb ? U2w : 0.f;
             } else {
                 const __half2 f2 = __floats2half2_rn(fva, fvb);
                 fvh[bi] = *reinterpret_cast<const uint32_t *>(&f2);
@@ -567,12 +569,32 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
             if (z + 2 < TZ && (!PARTIAL || z + 2 <= zlast)) fetch(z + 2, bi ^ 1);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                if constexpr (INTERP == 1) {
+                if constexpr (INTERP >= 1) {
                     float qa, dva, dua, duva, qb, dvb, dub, duvb;
-                    unpack_pair<PREC>(e[bi][k][0], qa, dva);
-                    unpack_pair<PREC>(e[bi][k][1], dua, duva);
-                    unpack_pair<PREC>(e[bi][k][2], qb, dvb);
-                    unpack_pair<PREC>(e[bi][k][3], dub, duvb);
+                    if constexpr (INTERP == 1) {
+                        unpack_pair<PREC>(e[bi][k][0], qa, dva);
+                        unpack_pair<PREC>(e[bi][k][1], dua, duva);
+                        unpack_pair<PREC>(e[bi][k][2], qb, dvb);
+                        unpack_pair<PREC>(e[bi][k][3], dub, duvb);
+                    } else {
+                        // the upper halves (dV, dUV) widened on the integer pipe, scaled by 2^-112;
+                        // INTERP 2 converts the lower halves (Q, dU) exactly, INTERP 3 as the upper
+                        dva = f16_hi_scaled(e[bi][k][0]);
+                        duva = f16_hi_scaled(e[bi][k][1]);
+                        dvb = f16_hi_scaled(e[bi][k][2]);
+                        duvb = f16_hi_scaled(e[bi][k][3]);
+                        if constexpr (INTERP == 2) {
+                            qa = __low2float(*reinterpret_cast<const __half2 *>(&e[bi][k][0]));
+                            dua = __low2float(*reinterpret_cast<const __half2 *>(&e[bi][k][1]));
+                            qb = __low2float(*reinterpret_cast<const __half2 *>(&e[bi][k][2]));
+                            dub = __low2float(*reinterpret_cast<const __half2 *>(&e[bi][k][3]));
+                        } else {
+                            qa = f16_lo_scaled(e[bi][k][0]);
+                            dua = f16_lo_scaled(e[bi][k][1]);
+                            qb = f16_lo_scaled(e[bi][k][2]);
+                            dub = f16_lo_scaled(e[bi][k][3]);
+                        }
+                    }
                     interp4_acc_x2(qa, qb, dua, dub, dva, dvb, duva, duvb, fu, fvp[bi][0], fvp[bi][1], wp[bi][0],
                                    wp[bi][1], acc[k][z], acc[k][z + 1]);
                 } else {
@@ -618,6 +640,12 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
 //     LDS.64 (the pair's entries), the eight 16-bit values converted exactly
 //     to FP32, then FP32 interpolation and accumulation as four fma.rn.f32x2
 //     (interp4_acc_x2): per voxel the operations of update_cimg's walk 4;
+//   TK_F16, INTERP 2 / 3: as INTERP 1, with the upper halves (INTERP 2) or all
+//     halves (INTERP 3) widened on the integer pipe (f16_hi_scaled,
+//     f16_lo_scaled: values scaled by 2^-112) and the scale undone by the row
+//     fraction (INTERP 2) or the weight U^2 (INTERP 3), powers of two: the
+//     same FP32 operations and results while the scaled intermediates stay
+//     normal FP32 numbers;
 //   TK_F16, INTERP 0 (selectable half-math form): update_cimg's walk 3 --
 //     column interpolation by HFMA2, row interpolation by one FP16 FMA, U^2
 //     rounded to FP16 and applied by fma.rn.f32.f16;
@@ -632,7 +660,7 @@ __global__ void __launch_bounds__(16 * TYQ, (PREC == TK_F32_COEF ? 2 : 32 / TYQ)
     // tiles of 16 x TYQ columns (TYQ 16: 2 CTAs of 8 warps per SM; TYQ 8: 4 CTAs of 4 warps)
     constexpr int TX = 16, TY = TYQ, TZ = 16, NT = TX * TY, ES = Cimg<PREC>::kBytes;
     static_assert(ISSUE == 0 || NT / 32 >= 4, "four issuing warps");
-    static_assert(INTERP == 1 || PREC == TK_F16, "the half-math walk is FP16 only");
+    static_assert(INTERP == 1 || PREC == TK_F16, "the half-math walk and the integer widenings are FP16 only");
     extern __shared__ __align__(128) unsigned char smem[];
     const int NQ = P.N / 4;  // a quarter turn in projections
     const int steps = 4 * P.qlen;
@@ -1109,6 +1137,7 @@ struct BPVariant {
      reinterpret_cast<const void *>(&bp_quad_kernel<P, IN, CAP, ST, true, ROWI, ISSUE, GEO, TY>), P, 16, TY, 16, ST, \
      true, "quad<" PN ",16," #TY ",16," #ST ",cap" #CAP "," INAME ",issue" #ISSUE ",geo" #GEO ">", CAP, AUTO}
 #define TK_BP_QUADF(P, PN, CAP, ST, AUTO, TY) TK_BP_QUAD_T(P, PN, 1, "f32i", CAP, ST, 1, 1, AUTO, 1, TY)
+#define TK_BP_QUADI(IN, CAP, ST, AUTO, TY) TK_BP_QUAD_T(TK_F16, "f16", IN, "f32i_int" #IN, CAP, ST, 1, 1, AUTO, 1, TY)
 #define TK_BP_QUADH(CAP, ST, ROWI, ISSUE, AUTO, GEO, TY) \
     TK_BP_QUAD_T(TK_F16, "f16", 0, "h16row" #ROWI, CAP, ST, ROWI, ISSUE, AUTO, GEO, TY)
 // FP16 half-math walks (update_cimg WALK 2 and 3, same bits): not bit-identical to the FP32 walks
@@ -1145,6 +1174,8 @@ static const BPVariant kVariants[] = {
     // FP32 coefficients by quarter turns (selectable): 16 bytes of shared memory per voxel update keep
     // it at the shared-memory bandwidth, where it runs slower than the general walk above
     TK_BP_QUADF(TK_F32_COEF, "f32c", 13312, 2, false, 16),
+    TK_BP_QUADI(2, 6144, 2, false, 8),  // FP16 halves widened on the integer pipe
+    TK_BP_QUADI(3, 6144, 2, false, 8),
     TK_BP_QUADH(6144, 2, 1, 1, false, 1, 8),  // the FP16 half-math forms
     TK_BP_QUADH(8192, 2, 1, 1, false, 1, 16),
     TK_BP_QUADH(13824, 2, 1, 1, false, 1, 16),
@@ -1165,6 +1196,7 @@ static const BPVariant kVariants[] = {
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
+static int g_diag_box_shrink = 0;    // rows taken off every staged box (tk_diag_shrink_box)
 static int g_fp_variant = 0;  // forward projector: 0 slice lanes (fp_scatter_col_kernel), 1 column lanes
 
 static const BPVariant *pick_variant(int precision)
@@ -1288,6 +1320,7 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
     const int align = v->coef ? (ES >= 16 ? 1 : 16 / ES) : 4;
     int BW, BH;
     if (int rc = bp_box_dims(g, nz, zoff, v->TX, v->TY, v->TZ, v->coef, align, &BW, &BH)) return rc;
+    BH = std::max(1, BH - g_diag_box_shrink);  // 0 unless a self-check test shrinks the staged box
     TK_CHECK(!v->coef || BW * ES / 4 <= 256, TK_ERR_UNSUPPORTED, "tile footprint of %d entries too wide", BW);
 
     TK_CHECK(angle0 >= 0, TK_ERR_INVALID, "backproject: negative first angle index");
@@ -1524,5 +1557,15 @@ extern "C" int tk_bp_select_variant(int i)
         return TK_ERR_INVALID;
     }
     tk::g_variant_override = i;
+    return TK_OK;
+}
+
+extern "C" int tk_diag_shrink_box(int rows)
+{
+    if (rows < 0) {
+        tk::set_error("tk_diag_shrink_box: rows < 0");
+        return TK_ERR_INVALID;
+    }
+    tk::g_diag_box_shrink = rows;
     return TK_OK;
 }

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <mutex>
 #include <vector>
 
 namespace tk {
@@ -76,9 +77,11 @@ __device__ unsigned g_device_err;
 
 unsigned *device_error_word()
 {
+    static std::mutex mu;  // host threads making their first call on a device at once
     static unsigned *addr[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(mu);
     if (!addr[dev]) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_device_err) != cudaSuccess) return nullptr;
@@ -515,6 +518,23 @@ extern "C" int tk_fdk_set_show_info(tk_fdk *h, int show)
 {
     TK_H(h);
     h->show = show ? 1 : 0;
+    return TK_OK;
+}
+// fShowInfo (kernel.cu:901-913): the device summary on stdout.
+extern "C" int tk_fdk_show_info(tk_fdk *h)
+{
+    TK_H(h);
+    cudaDeviceProp p{};
+    TK_CUDA(cudaGetDeviceProperties(&p, h->dev));
+    const size_t fr = tk_get_free_mem_info(h->dev);
+    fprintf(stdout, "\nGPU:\n  CUDA device %s has %d Multi-Processors\n", p.name, p.multiProcessorCount);
+    fprintf(stdout, "  Each Multi-Processor has %d threads\n", p.maxThreadsPerMultiProcessor);
+    fprintf(stdout, "  Max threads per block %d\n", p.maxThreadsPerBlock);
+    fprintf(stdout, "  Max threads per dim x %d\n                      y %d\n                      z %d\n",
+            p.maxThreadsDim[0], p.maxThreadsDim[1], p.maxThreadsDim[2]);
+    fprintf(stdout, "  Total     RAM         %zuMiB\n\n  Free      RAM         %zuMiB\n\n",
+            p.totalGlobalMem / 1024 / 1024, fr / 1024 / 1024);
+    fflush(stdout);
     return TK_OK;
 }
 extern "C" int tk_fdk_set_axis_direction(tk_fdk *h, int x, int y, int z)

@@ -30,9 +30,37 @@ __global__ void __launch_bounds__(256) fma_rate_kernel(float *out, float s, int 
     out[blockIdx.x * blockDim.x + threadIdx.x] = r;
 }
 
+// A wait that nothing completes: one thread arms an mbarrier for 1024 bytes of
+// asynchronous copies and issues none, then waits with the library's bounded
+// wait; when the limit runs out it reports ERR_WAIT_TIMEOUT in the error word
+// and the CTA returns (no copy is in flight), as every kernel of the library
+// does when a stage never lands.
+__global__ void wait_timeout_kernel(unsigned *err, unsigned long long limit_ns)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        mbar_arrive_expect_tx(&bar, 1024);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait_bounded(&bar, 0, limit_ns)) atomicOr(err, ERR_WAIT_TIMEOUT);
+}
+
 }  // namespace tk
 
 using namespace tk;
+
+extern "C" int tk_diag_wait_timeout(double limit_ms, void *stream)
+{
+    TK_CHECK(limit_ms > 0 && limit_ms <= 1000, TK_ERR_INVALID, "tk_diag_wait_timeout: limit outside (0, 1000] ms");
+    unsigned *err = device_error_word();
+    TK_CHECK(err, TK_ERR_CUDA, "device error word unavailable");
+    wait_timeout_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(err, (unsigned long long)(limit_ms * 1e6));
+    TK_CUDA(cudaGetLastError());
+    count_launch();
+    return TK_OK;
+}
 
 extern "C" unsigned long long tk_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
