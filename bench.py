@@ -120,6 +120,8 @@ def parse():
     ap.add_argument("--filter-width", type=int, default=1024, help="with --profile-filter: detector width (and height)")
     ap.add_argument("--filter-form", choices=["auto", "fft", "toeplitz"], default="auto",
                     help="with --profile-filter: the filter form (tk_filter_select_form)")
+    ap.add_argument("--probe-link", action="store_true",
+                    help="time host<->device copies of the e2e leg's buffer sizes, alone and beside a busy GPU")
     ap.add_argument("--profile-bp", choices=["f32", "f16", "bf16", "f32c"], default=None,
                     help="small case for ncu: 180 x 1024^2 projections, a 64-slice slab of the 1024^2 volume; "
                          "one untimed and two timed backprojection launches")
@@ -626,6 +628,124 @@ def run_profile_bp(args):
     return 0
 
 
+def run_probe_link(args):
+    """The host link, for the e2e leg's step-to-step spread: the 1.51 GB uint16 projections
+    host -> device and the 4.29 GB volume device -> host, as one copy each and as eight chunk copies,
+    from the same page-locked buffers in a loop with no kernel launched; the same copies while
+    device-to-device copies or the backprojection kernel run on another stream; the e2e leg's
+    handle steps, each after a bare upload of the same buffer; then copies from buffers page-locked
+    afresh for every copy.  CUDA events on the copy stream time each copy."""
+    import torch
+
+    torch.cuda.set_device(0)
+    g = workload()
+    n_in, n_vol = g.N * g.H * g.W, g.X * g.Y * g.Z
+    raw_h = torch.empty(n_in, dtype=torch.int16, pin_memory=True)
+    vol_h = torch.empty(n_vol, dtype=torch.float32, pin_memory=True)
+    raw_d = torch.randint(0, 32767, (n_in,), dtype=torch.int16, device="cuda")
+    raw_h.copy_(raw_d)  # filled from the device, as the e2e leg fills its buffer
+    vol_d = torch.zeros(n_vol, dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+    reps = max(args.steps, 4)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st):
+            e0.record(st)
+            fn()
+            e1.record(st)
+        e1.synchronize()
+        return round(e0.elapsed_time(e1), 2)
+
+    def chunks(dst, src, k=8):
+        step = (dst.numel() + k - 1) // k
+        for a in range(0, dst.numel(), step):
+            dst[a:a + step].copy_(src[a:a + step], non_blocking=True)
+
+    out = {"h2d_ms": [], "d2h_ms": [], "h2d_chunked_ms": [], "d2h_chunked_ms": [], "h2d_fresh_ms": [],
+           "d2h_fresh_ms": []}
+    for _ in range(reps):
+        out["h2d_ms"].append(timed(lambda: raw_d.copy_(raw_h, non_blocking=True)))
+        out["d2h_ms"].append(timed(lambda: vol_h.copy_(vol_d, non_blocking=True)))
+    for _ in range(reps):
+        out["h2d_chunked_ms"].append(timed(lambda: chunks(raw_d, raw_h)))
+        out["d2h_chunked_ms"].append(timed(lambda: chunks(vol_h, vol_d)))
+    # the same copies while the GPU is busy on another stream: device-to-device copies (HBM bound),
+    # then the backprojection kernel of the 1024^3 workload (on zero-filled FP16 entries)
+    busy = torch.cuda.Stream()
+    big_a = torch.zeros(1 << 30, dtype=torch.float32, device="cuda")
+    big_b = torch.empty_like(big_a)
+    out["h2d_under_d2d_ms"], out["h2d_under_bp_ms"], out["d2h_under_bp_ms"] = [], [], []
+    for _ in range(reps):
+        with torch.cuda.stream(busy):
+            for _ in range(8):
+                big_b.copy_(big_a)
+        out["h2d_under_d2d_ms"].append(timed(lambda: raw_d.copy_(raw_h, non_blocking=True)))
+        torch.cuda.synchronize()
+    del big_a, big_b
+    from tomokvas_gb300 import _lib, device
+
+    q, sc = device.alloc_filtered(g, _lib.TK_F16)
+    q.zero_()
+    vol = torch.empty((g.Z, g.Y, g.X), dtype=torch.float32, device="cuda")
+    for _ in range(reps):
+        device.backproject(g, q, sc, _lib.TK_F16, vol=vol, stream=busy)
+        out["h2d_under_bp_ms"].append(timed(lambda: raw_d.copy_(raw_h, non_blocking=True)))
+        out["d2h_under_bp_ms"].append(timed(lambda: vol_h.copy_(vol_d, non_blocking=True)))
+        torch.cuda.synchronize()
+    del q, vol
+    # the e2e leg's handle steps, each preceded by a 1 MB and a whole bare upload, of the handle's
+    # buffer or of another buffer of the same size: whether the first upload after a step is slow
+    # whoever issues it and whatever it reads, and whether a small copy takes the delay
+    from tomokvas_gb300.fbp import FilteredBackProjection, VolumeSink
+
+    sink = VolumeSink(g.X, g.Y, g.Z, 128, out=vol_h.numpy().reshape(g.Z, g.Y, g.X))
+    fbp = FilteredBackProjection(raise_on_error=True)
+    fbp.SetBlockSize(128)
+    fbp.SetSinogramProperties(None, g.W, g.cX, g.N, g.H, g.cZ, g.dfi, g.D, g.tau)
+    fbp.SetReconstructionProperties(sink, g.X, g.cx, g.Y, g.cy, g.Z, g.cz, g.rot)
+    fbp.SetScaleXYZ(g.scale)
+    fbp.SetFilter("hann")
+    fbp.SetPrecision("f16")
+    fbp.SetPipeline(True)
+    raw_np = raw_h.numpy().view(np.uint16)
+    out["h2d_1mb_before_handle_ms"], out["before_handle_source"] = [], []
+    out["h2d_before_handle_ms"], out["handle_upload_ms"], out["handle_step_s"] = [], [], []
+    small = 1 << 19  # 1 MB of the same buffer
+    other_h = torch.empty_like(raw_h, pin_memory=True)  # a second page-locked buffer of the same size
+    other_h.copy_(raw_d)
+    for i in range(reps + 2):
+        src = raw_h if i % 2 else other_h  # the bare upload reads the handle's buffer or another one
+        pre_small = timed(lambda: raw_d[:small].copy_(src[:small], non_blocking=True))
+        pre = timed(lambda: raw_d.copy_(src, non_blocking=True))
+        fbp.SetProjectionsU16(raw_np, "projection", flat_value=I0)
+        t0 = time.perf_counter()
+        fbp.Initialize()
+        fbp.CalculateReconstruction()
+        dt = time.perf_counter() - t0
+        if i >= 2:  # two warm-up steps
+            out["h2d_1mb_before_handle_ms"].append(pre_small)
+            out["before_handle_source"].append("same" if i % 2 else "other")
+            out["h2d_before_handle_ms"].append(pre)
+            out["handle_upload_ms"].append(round(fbp.Timings()["h2d_ms"], 2))
+            out["handle_step_s"].append(round(dt, 4))
+    fbp.close()
+    del raw_h, vol_h, other_h
+    for _ in range(min(reps, 4)):
+        rh = torch.zeros(n_in, dtype=torch.int16, pin_memory=True)
+        vh = torch.empty(n_vol, dtype=torch.float32, pin_memory=True)
+        out["h2d_fresh_ms"].append(timed(lambda: raw_d.copy_(rh, non_blocking=True)))
+        out["d2h_fresh_ms"].append(timed(lambda: vh.copy_(vol_d, non_blocking=True)))
+        del rh, vh
+    gb_in, gb_vol = n_in * 2 / 1e9, n_vol * 4 / 1e9
+    out["h2d_gbs"] = [round(gb_in / (t * 1e-3), 1) for t in out["h2d_ms"]]
+    out["d2h_gbs"] = [round(gb_vol / (t * 1e-3), 1) for t in out["d2h_ms"]]
+    emit({"probe_link": out, "h2d_bytes": n_in * 2, "d2h_bytes": n_vol * 4,
+          "note": "each copy timed with CUDA events on its own stream; *_under_* copies run beside "
+                  "device-to-device copies or the backprojection kernel on another stream"})
+    return 0
+
+
 def run_profile_filter(args):
     """Filter-only case small enough for an ncu capture: 90 x 1024^2 uint16 projections (189 MB in,
     0.38-1.5 GB out, above L2)."""
@@ -1060,6 +1180,8 @@ def main():
         return run_outofcore(args)
     if args.profile_bp:
         return run_profile_bp(args)
+    if args.probe_link:
+        return run_probe_link(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -480,11 +480,10 @@ __global__ void __launch_bounds__(TX *TY, MINB)
 // v_z = fma(z, dv, v0) are shared by the four.  Past the chunk's last slice
 // (a partial chunk ending on an even slice) the pair's second slice repeats
 // the first, whose rows are inside the box, at weight 0.
-template <int PREC, int INTERP, int CAPB, bool PARTIAL, int ROWI>
+template <int PREC, int INTERP, int CAPB, bool PARTIAL, int ROWI, int TZ>
 __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, float v0, float dv, float fu, float U2,
-                                          float Hm1, bool all_in, int zlast, float (&acc)[4][16])
+                                          float Hm1, bool all_in, int zlast, float (&acc)[4][TZ])
 {
-    constexpr int TZ = 16;
     if constexpr (PREC == TK_F32_COEF) {
         // shared-memory bound (a 16-byte load per voxel): no software pipeline
 #pragma unroll
@@ -527,7 +526,6 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
         float fvp[2][2], wp[2][2];
         uint32_t fvh[2], wh[2];
         const __half2 U2h2 = __float2half2_rn(U2);
-        const float U2w = INTERP == 3 ? U2 * kF16IntScale : U2;  // INTERP 3: every value scaled by 2^-112
         const uint32_t w_all = *reinterpret_cast<const uint32_t *>(&U2h2);
         auto fetch = [&](int z, int bi) {
             const bool bin = !PARTIAL || z + 1 <= zlast;
@@ -539,12 +537,11 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
             const uint32_t rb = (uint32_t)__float_as_int(flb) * row_bytes + sbase;
             const bool ina = all_in || (va >= 0.f && va <= Hm1);  // kernel.cu:130-131
             const bool inb = bin && (all_in || (vb >= 0.f && vb <= Hm1));
-            if constexpr (INTERP >= 1) {
-                // INTERP 2: B comes out scaled by 2^-112 (its halves widened on the integer pipe)
-                fvp[bi][0] = INTERP == 2 ? fva * kF16IntScale : fva;
-                fvp[bi][1] = INTERP == 2 ? fvb * kF16IntScale : fvb;
-                wp[bi][0] = ina ? U2w : 0.f;
-                wp[bi][1] = inb ? U2w : 0.f;
+            if constexpr (INTERP == 1) {
+                fvp[bi][0] = fva;
+                fvp[bi][1] = fvb;
+                wp[bi][0] = ina ? U2 : 0.f;
+                wp[bi][1] = inb ? U2 : 0.f;
             } else {
                 const __half2 f2 = __floats2half2_rn(fva, fvb);
                 fvh[bi] = *reinterpret_cast<const uint32_t *>(&f2);
@@ -569,32 +566,16 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
             if (z + 2 < TZ && (!PARTIAL || z + 2 <= zlast)) fetch(z + 2, bi ^ 1);
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                if constexpr (INTERP >= 1) {
+                if constexpr (INTERP == 1 && PREC == TK_F16) {
+                    // scalar FMAs: 2 % faster than the f32x2 form for FP16, 6 % slower for BF16
+                    interp_scalar_acc<PREC>(e[bi][k][0], e[bi][k][1], e[bi][k][2], e[bi][k][3], fu, fvp[bi][0],
+                                            fvp[bi][1], wp[bi][0], wp[bi][1], acc[k][z], acc[k][z + 1]);
+                } else if constexpr (INTERP == 1) {
                     float qa, dva, dua, duva, qb, dvb, dub, duvb;
-                    if constexpr (INTERP == 1) {
-                        unpack_pair<PREC>(e[bi][k][0], qa, dva);
-                        unpack_pair<PREC>(e[bi][k][1], dua, duva);
-                        unpack_pair<PREC>(e[bi][k][2], qb, dvb);
-                        unpack_pair<PREC>(e[bi][k][3], dub, duvb);
-                    } else {
-                        // the upper halves (dV, dUV) widened on the integer pipe, scaled by 2^-112;
-                        // INTERP 2 converts the lower halves (Q, dU) exactly, INTERP 3 as the upper
-                        dva = f16_hi_scaled(e[bi][k][0]);
-                        duva = f16_hi_scaled(e[bi][k][1]);
-                        dvb = f16_hi_scaled(e[bi][k][2]);
-                        duvb = f16_hi_scaled(e[bi][k][3]);
-                        if constexpr (INTERP == 2) {
-                            qa = __low2float(*reinterpret_cast<const __half2 *>(&e[bi][k][0]));
-                            dua = __low2float(*reinterpret_cast<const __half2 *>(&e[bi][k][1]));
-                            qb = __low2float(*reinterpret_cast<const __half2 *>(&e[bi][k][2]));
-                            dub = __low2float(*reinterpret_cast<const __half2 *>(&e[bi][k][3]));
-                        } else {
-                            qa = f16_lo_scaled(e[bi][k][0]);
-                            dua = f16_lo_scaled(e[bi][k][1]);
-                            qb = f16_lo_scaled(e[bi][k][2]);
-                            dub = f16_lo_scaled(e[bi][k][3]);
-                        }
-                    }
+                    unpack_pair<PREC>(e[bi][k][0], qa, dva);
+                    unpack_pair<PREC>(e[bi][k][1], dua, duva);
+                    unpack_pair<PREC>(e[bi][k][2], qb, dvb);
+                    unpack_pair<PREC>(e[bi][k][3], dub, duvb);
                     interp4_acc_x2(qa, qb, dua, dub, dva, dvb, duva, duvb, fu, fvp[bi][0], fvp[bi][1], wp[bi][0],
                                    wp[bi][1], acc[k][z], acc[k][z + 1]);
                 } else {
@@ -638,14 +619,9 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
 // Storage and arithmetic (PREC, INTERP):
 //   TK_F16 / TK_BF16, INTERP 1 (the default): per slice pair and turn k, two
 //     LDS.64 (the pair's entries), the eight 16-bit values converted exactly
-//     to FP32, then FP32 interpolation and accumulation as four fma.rn.f32x2
-//     (interp4_acc_x2): per voxel the operations of update_cimg's walk 4;
-//   TK_F16, INTERP 2 / 3: as INTERP 1, with the upper halves (INTERP 2) or all
-//     halves (INTERP 3) widened on the integer pipe (f16_hi_scaled,
-//     f16_lo_scaled: values scaled by 2^-112) and the scale undone by the row
-//     fraction (INTERP 2) or the weight U^2 (INTERP 3), powers of two: the
-//     same FP32 operations and results while the scaled intermediates stay
-//     normal FP32 numbers;
+//     to FP32, then FP32 interpolation and accumulation (FP16: scalar FMAs,
+//     interp_scalar_acc; BF16: four fma.rn.f32x2, interp4_acc_x2): per voxel
+//     the operations of update_cimg's walk 4;
 //   TK_F16, INTERP 0 (selectable half-math form): update_cimg's walk 3 --
 //     column interpolation by HFMA2, row interpolation by one FP16 FMA, U^2
 //     rounded to FP16 and applied by fma.rn.f32.f16;
@@ -653,14 +629,15 @@ __device__ __forceinline__ void quad_walk(uint32_t sbase, uint32_t row_bytes, fl
 //     operations as scalar FMAs.
 // The 8-byte forms are software-pipelined: pair p+1's coordinates, fractions
 // and eight loads are issued before pair p's arithmetic.
-template <int PREC, int INTERP, int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE, int GEO = 0, int TYQ = 16>
+template <int PREC, int INTERP, int CAPB, int STAGES, bool PARTIAL, int ROWI, int ISSUE, int GEO = 0, int TYQ = 16,
+          int TZQ = 16>
 __global__ void __launch_bounds__(16 * TYQ, (PREC == TK_F32_COEF ? 2 : 32 / TYQ))
     bp_quad_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P)
 {
     // tiles of 16 x TYQ columns (TYQ 16: 2 CTAs of 8 warps per SM; TYQ 8: 4 CTAs of 4 warps)
-    constexpr int TX = 16, TY = TYQ, TZ = 16, NT = TX * TY, ES = Cimg<PREC>::kBytes;
+    constexpr int TX = 16, TY = TYQ, TZ = TZQ, NT = TX * TY, ES = Cimg<PREC>::kBytes;
     static_assert(ISSUE == 0 || NT / 32 >= 4, "four issuing warps");
-    static_assert(INTERP == 1 || PREC == TK_F16, "the half-math walk and the integer widenings are FP16 only");
+    static_assert(INTERP == 1 || PREC == TK_F16, "the half-math walk is FP16 only");
     extern __shared__ __align__(128) unsigned char smem[];
     const int NQ = P.N / 4;  // a quarter turn in projections
     const int steps = 4 * P.qlen;
@@ -784,7 +761,7 @@ __global__ void __launch_bounds__(16 * TYQ, (PREC == TK_F32_COEF ? 2 : 32 / TYQ)
                                            (uint32_t)(kMagicBits + by0) * row_bytes;
                     const float U2 = __fmul_rn(U, U);
                     const bool all_in = vlo >= 0.f && vhi <= Hm1;
-                    quad_walk<PREC, INTERP, CAPB, PARTIAL, ROWI>(sbase, row_bytes, v0, dv, fu, U2, Hm1, all_in,
+                    quad_walk<PREC, INTERP, CAPB, PARTIAL, ROWI, TZ>(sbase, row_bytes, v0, dv, fu, U2, Hm1, all_in,
                                                                 zlast, acc);
                 } else {
                     atomicOr(P.err, ERR_BOX_OVERFLOW);
@@ -1132,12 +1109,13 @@ struct BPVariant {
      "cimg_x2<" PN "," #TX "," #TY "," #TZ "," #ST ",occ" #MB ">"}
 // quarter-turn kernels, for symmetric scans only: PREC storage, INTERP 1 FP32 interpolation
 // (update_cimg walk 4's operations), INTERP 0 the FP16 half-math walk 3 (ROWI 1) or 2 (ROWI 0)
+#define TK_BP_QUAD_TZ(P, PN, IN, INAME, CAP, ST, ROWI, ISSUE, AUTO, GEO, TY, TZ) \
+    {reinterpret_cast<const void *>(&bp_quad_kernel<P, IN, CAP, ST, false, ROWI, ISSUE, GEO, TY, TZ>), \
+     reinterpret_cast<const void *>(&bp_quad_kernel<P, IN, CAP, ST, true, ROWI, ISSUE, GEO, TY, TZ>), P, 16, TY, TZ, \
+     ST, true, "quad<" PN ",16," #TY "," #TZ "," #ST ",cap" #CAP "," INAME ",issue" #ISSUE ",geo" #GEO ">", CAP, AUTO}
 #define TK_BP_QUAD_T(P, PN, IN, INAME, CAP, ST, ROWI, ISSUE, AUTO, GEO, TY) \
-    {reinterpret_cast<const void *>(&bp_quad_kernel<P, IN, CAP, ST, false, ROWI, ISSUE, GEO, TY>), \
-     reinterpret_cast<const void *>(&bp_quad_kernel<P, IN, CAP, ST, true, ROWI, ISSUE, GEO, TY>), P, 16, TY, 16, ST, \
-     true, "quad<" PN ",16," #TY ",16," #ST ",cap" #CAP "," INAME ",issue" #ISSUE ",geo" #GEO ">", CAP, AUTO}
+    TK_BP_QUAD_TZ(P, PN, IN, INAME, CAP, ST, ROWI, ISSUE, AUTO, GEO, TY, 16)
 #define TK_BP_QUADF(P, PN, CAP, ST, AUTO, TY) TK_BP_QUAD_T(P, PN, 1, "f32i", CAP, ST, 1, 1, AUTO, 1, TY)
-#define TK_BP_QUADI(IN, CAP, ST, AUTO, TY) TK_BP_QUAD_T(TK_F16, "f16", IN, "f32i_int" #IN, CAP, ST, 1, 1, AUTO, 1, TY)
 #define TK_BP_QUADH(CAP, ST, ROWI, ISSUE, AUTO, GEO, TY) \
     TK_BP_QUAD_T(TK_F16, "f16", 0, "h16row" #ROWI, CAP, ST, ROWI, ISSUE, AUTO, GEO, TY)
 // FP16 half-math walks (update_cimg WALK 2 and 3, same bits): not bit-identical to the FP32 walks
@@ -1174,8 +1152,6 @@ static const BPVariant kVariants[] = {
     // FP32 coefficients by quarter turns (selectable): 16 bytes of shared memory per voxel update keep
     // it at the shared-memory bandwidth, where it runs slower than the general walk above
     TK_BP_QUADF(TK_F32_COEF, "f32c", 13312, 2, false, 16),
-    TK_BP_QUADI(2, 6144, 2, false, 8),  // FP16 halves widened on the integer pipe
-    TK_BP_QUADI(3, 6144, 2, false, 8),
     TK_BP_QUADH(6144, 2, 1, 1, false, 1, 8),  // the FP16 half-math forms
     TK_BP_QUADH(8192, 2, 1, 1, false, 1, 16),
     TK_BP_QUADH(13824, 2, 1, 1, false, 1, 16),
@@ -1246,7 +1222,8 @@ int bp_box_dims(const tk_geometry &g, int nz, float zoff, int TX, int TY, int TZ
 // launch with projection (q + k N/4) mod N at beta_q + k pi/2 (mod 2 pi) to within 1e-5 rad
 // (angles as build_trig forms them; 1e-5 rad is 0.01 pixel at 1000 pixels
 // from the axis), and a box that fits its slot.
-static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, int cap, int TY, int precision)
+static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, int cap, int TY, int TZ,
+                          int precision)
 {
     if (g.X != g.Y || g.X % 32 != 0 || g.dirx || g.diry) return false;
     if (g.W >= (1 << 14) || g.H >= (1 << 14)) return false;  // footprint origins kept as 16-bit pairs
@@ -1261,7 +1238,7 @@ static bool quad_eligible(const tk_geometry &g, int nz, float zoff, int angle0, 
         }
     const int ES = (int)entry_size(precision);
     int BW = 0, BH = 0;
-    if (bp_box_dims(g, nz, zoff, 16, TY, 16, true, 16 / ES, &BW, &BH) != TK_OK) return false;
+    if (bp_box_dims(g, nz, zoff, 16, TY, TZ, true, 16 / ES, &BW, &BH) != TK_OK) return false;
     return BW * BH * ES <= cap;
 }
 
@@ -1272,10 +1249,11 @@ static const BPVariant *pick_quad(const tk_geometry &g, int precision, int nz, f
 {
     if (g_variant_override >= 0 && kVariants[g_variant_override].precision == precision) {
         const BPVariant *v = &kVariants[g_variant_override];
-        return v->qcap && quad_eligible(g, nz, zoff, angle0, v->qcap, v->TY, precision) ? v : nullptr;
+        return v->qcap && quad_eligible(g, nz, zoff, angle0, v->qcap, v->TY, v->TZ, precision) ? v : nullptr;
     }
     for (const auto &c : kVariants)
-        if (c.precision == precision && c.qcap && c.qauto && quad_eligible(g, nz, zoff, angle0, c.qcap, c.TY, precision))
+        if (c.precision == precision && c.qcap && c.qauto &&
+            quad_eligible(g, nz, zoff, angle0, c.qcap, c.TY, c.TZ, precision))
             return &c;
     return nullptr;
 }

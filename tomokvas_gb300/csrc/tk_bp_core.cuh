@@ -80,30 +80,6 @@ template <int PREC> __device__ __forceinline__ void unpack_pair(uint32_t w, floa
         hi = f.y;
     }
 }
-// FP16 halves widened on the integer pipe, scaled by 2^-112: for an FP16 pattern
-// s e4..e0 m9..m0 the FP32 pattern s 000 e4..e0 m9..m0 0^13 has the value
-// 2^-112 times the FP16 value, exactly (normal and subnormal halves alike; no
-// infinities occur in the stored images).  The upper half is one arithmetic
-// shift right by 3 (sign to bit 31, copies in bits 30..28) and one mask; the
-// lower half is first moved up by a byte permute.  Products with a factor
-// scaled by 2^112 undo the scale exactly while the intermediate stays a
-// normal FP32 number (below 2^-126 the subnormal keeps an absolute error of
-// 2^-149, i.e. 2^-37 of the unscaled value).
-constexpr float kF16IntScale = 0x1p112f;
-__device__ __forceinline__ float f16_hi_scaled(uint32_t w)
-{
-    uint32_t r;
-    asm("{\n\t.reg .b32 t;\n\tshr.s32 t, %1, 3;\n\tand.b32 %0, t, 0x8FFFE000;\n\t}" : "=r"(r) : "r"(w));
-    return __uint_as_float(r);
-}
-__device__ __forceinline__ float f16_lo_scaled(uint32_t w)
-{
-    uint32_t r;
-    asm("{\n\t.reg .b32 t;\n\tprmt.b32 t, %1, 0, 0x1044;\n\tshr.s32 t, t, 3;\n\tand.b32 %0, t, 0x8FFFE000;\n\t}"
-        : "=r"(r)
-        : "r"(w));
-    return __uint_as_float(r);
-}
 // FP32 interpolation of a 16-bit entry {(Q, dV), (dU, dUV)}: the four values
 // converted exactly to FP32, then A = fma(fu, dU, Q), B = fma(fu, dUV, dV) --
 // the operations of the FP32 coefficient format on the stored values.
@@ -229,6 +205,26 @@ __device__ __forceinline__ void interp4_acc_x2(float qa, float qb, float dua, fl
         : "+f"(acc0), "+f"(acc1)
         : "f"(qa), "f"(qb), "f"(dua), "f"(dub), "f"(dva), "f"(dvb), "f"(duva), "f"(duvb), "f"(fu), "f"(fva),
           "f"(fvb), "f"(wa), "f"(wb));
+}
+
+// FP32 bilinear interpolation and accumulation of two slices a, b from their
+// 16-bit entries {(Q, dV), (dU, dUV)} (low word, high word), the values
+// converted exactly to FP32; per slice
+//   A = fma(fu, dU, Q), B = fma(fu, dUV, dV), acc = fma(w, fma(fv, B, A), acc):
+// the operations of interp4_acc_x2 as scalar FMAs (same bits).
+template <int PREC>
+__device__ __forceinline__ void interp_scalar_acc(uint32_t loa, uint32_t hia, uint32_t lob, uint32_t hib, float fu,
+                                                  float fva, float fvb, float wa, float wb, float &acc0, float &acc1)
+{
+    float qa, dva, dua, duva, qb, dvb, dub, duvb;
+    unpack_pair<PREC>(loa, qa, dva);
+    unpack_pair<PREC>(hia, dua, duva);
+    unpack_pair<PREC>(lob, qb, dvb);
+    unpack_pair<PREC>(hib, dub, duvb);
+    const float Aa = fmaf(fu, dua, qa), Ba = fmaf(fu, duva, dva);
+    const float Ab = fmaf(fu, dub, qb), Bb = fmaf(fu, duvb, dvb);
+    acc0 = fmaf(wa, fmaf(fva, Ba, Aa), acc0);
+    acc1 = fmaf(wb, fmaf(fvb, Bb, Ab), acc1);
 }
 
 // acc0 += w.lo * val.lo and acc1 += w.hi * val.hi: FP16 products (exact in
