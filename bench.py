@@ -1064,6 +1064,7 @@ def batch_summary(steps, warmup, items=64):
     tuned, tune_ms = b.autotune()
     forms = b.filter_forms()
     ms_eager = timeit(lambda: b.run(graph=False))
+    filt_ms, bp_ms = b.timings()  # phases of the last eager run
     ms_graph = timeit(lambda: b.run(graph=True))
     diff = max(float(np.abs(v[v.shape[0] // 2].cpu().numpy() - r).max() / max(np.abs(r).max(), 1e-30))
                for v, r in zip(vols, ref))
@@ -1076,7 +1077,8 @@ def batch_summary(steps, warmup, items=64):
     return {"workload": f"batch_{len(geos)}_uneven_fdk", "metric": "GUPS", "unit": "GUPS", "items": len(geos),
             "updates": updates, "storage": "f16 coefficients, f32 interpolation", "steps": steps, "warmup": warmup,
             "per_volume": {"ms": ms_single, "gups": updates / (ms_single * 1e-3) / 1e9},
-            "batch_eager": {"ms": ms_eager, "gups": updates / (ms_eager * 1e-3) / 1e9},
+            "batch_eager": {"ms": ms_eager, "gups": updates / (ms_eager * 1e-3) / 1e9,
+                            "filter_phase_ms": filt_ms, "backprojection_ms": bp_ms},
             "batch_graph": {"ms": ms_graph, "gups": updates / (ms_graph * 1e-3) / 1e9},
             "speedup_graph_vs_per_volume": ms_single / ms_graph, "autotuned_variant": tuned,
             "autotune_ms": tune_ms, "filter_forms_by_width": by_width,

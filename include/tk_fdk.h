@@ -361,6 +361,10 @@ int tk_batch_select_variant(tk_batch *b, int i);
  * (the tensor-core Toeplitz product only where it supports the width); -1 for
  * a bad index. */
 int tk_batch_item_filter_form(const tk_batch *b, int i);
+/* Phase times of the last eager tk_batch_run (use_graph = 0): from the run's
+ * start until every item's filter has finished, and the persistent
+ * backprojection launch after it (waits for that run to finish). */
+int tk_batch_timings(tk_batch *b, float *filter_ms, float *bp_ms);
 
 /* ------------------------------------------------------------ diagnostics
  * tk_kernel_launches: kernels this library has launched in this process (a

@@ -59,6 +59,12 @@ class Batch:
         """Filter form of every item (TK_FILTER_*): what tk_batch_autotune chose by timing."""
         return [int(self._L.tk_batch_item_filter_form(self._h, i)) for i in range(self._L.tk_batch_size(self._h))]
 
+    def timings(self):
+        """(filter phase ms, backprojection ms) of the last eager run."""
+        f, b = ctypes.c_float(0.0), ctypes.c_float(0.0)
+        check(self._L.tk_batch_timings(self._h, ctypes.byref(f), ctypes.byref(b)))
+        return float(f.value), float(b.value)
+
     def select_variant(self, i: int):
         check(self._L.tk_batch_select_variant(self._h, int(i)))
 

@@ -300,6 +300,9 @@ struct tk_batch {
     std::vector<cudaStream_t> fstreams;
     std::vector<cudaEvent_t> fdone;
     cudaEvent_t fork = nullptr;
+    // phase timing of the last eager run (tk_batch_timings): start, filters joined, backprojection done
+    cudaEvent_t t_ev[3] = {nullptr, nullptr, nullptr};
+    bool timed = false;
 };
 
 namespace {
@@ -468,6 +471,16 @@ int enqueue(tk_batch *b, cudaStream_t st)
         b->fstreams.push_back(s);
         b->fdone.push_back(e);
     }
+    // phase events on eager runs only (a captured graph records none)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    TK_CUDA(cudaStreamIsCapturing(st, &cs));
+    const bool timing = cs == cudaStreamCaptureStatusNone;
+    if (timing) {
+        for (auto &e : b->t_ev)
+            if (!e) TK_CUDA(cudaEventCreate(&e));
+        TK_CUDA(cudaEventRecord(b->t_ev[0], st));
+    }
+    b->timed = false;
     // item i's filter chain (storage scale, filter) on stream i mod K; each item writes only its
     // own coefficient image and scale, so the chains are independent
     TK_CUDA(cudaEventRecord(b->fork, st));
@@ -483,6 +496,7 @@ int enqueue(tk_batch *b, cudaStream_t st)
         TK_CUDA(cudaEventRecord(b->fdone[k], b->fstreams[k]));
         TK_CUDA(cudaStreamWaitEvent(st, b->fdone[k], 0));
     }
+    if (timing) TK_CUDA(cudaEventRecord(b->t_ev[1], st));
     int *counter = reinterpret_cast<int *>(b->ws);
     TK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
     const BatchVariant &V = kBatchVariants[b->used_variant];
@@ -493,6 +507,10 @@ int enqueue(tk_batch *b, cudaStream_t st)
     void *args[] = {&items, &nitems, &nunits, &counter, &err, &maxN, &slot};
     TK_CUDA(cudaLaunchKernel(V.fn, dim3((unsigned)b->grid), dim3((unsigned)(V.TX * V.TY)), args, b->smem, st));
     count_launch();
+    if (timing) {
+        TK_CUDA(cudaEventRecord(b->t_ev[2], st));
+        b->timed = true;
+    }
     return TK_OK;
 }
 
@@ -515,6 +533,8 @@ extern "C" void tk_batch_destroy(tk_batch *b)
         cudaStreamDestroy(s);
     }
     for (cudaEvent_t e : b->fdone) cudaEventDestroy(e);
+    for (cudaEvent_t e : b->t_ev)
+        if (e) cudaEventDestroy(e);
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->cap) cudaStreamDestroy(b->cap);
     delete b;
@@ -611,6 +631,16 @@ extern "C" int tk_batch_run(tk_batch *b, int use_graph, void *stream)
         TK_CUDA(ei);
     }
     TK_CUDA(cudaGraphLaunch(b->gexec, st));
+    return TK_OK;
+}
+
+extern "C" int tk_batch_timings(tk_batch *b, float *filter_ms, float *bp_ms)
+{
+    TK_CHECK(b && filter_ms && bp_ms, TK_ERR_INVALID, "tk_batch_timings: null argument");
+    TK_CHECK(b->timed, TK_ERR_STATE, "tk_batch_timings: no eager run since the last plan");
+    TK_CUDA(cudaEventSynchronize(b->t_ev[2]));
+    TK_CUDA(cudaEventElapsedTime(filter_ms, b->t_ev[0], b->t_ev[1]));
+    TK_CUDA(cudaEventElapsedTime(bp_ms, b->t_ev[1], b->t_ev[2]));
     return TK_OK;
 }
 
