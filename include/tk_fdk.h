@@ -220,11 +220,12 @@ int tk_fdk_backward(const tk_geometry *g, const float *d_vol_grad, int layout, i
  * checkpointed once after the filter (tk_refine_checkpoint) as FP32 samples,
  * or as FP16 samples where HBM is short (half the bytes; the residual is
  * formed in FP32).  A step is B^T x, one residual pass (r = -alpha (B^T x - q)
- * and the loss), and B r accumulated into x.  alpha < 2 / lambda_max(B B^T)
+ * and the loss's block partials), and B r accumulated into x; the loss is
+ * summed in compensated FP32 when d_loss is given.  alpha < 2 / lambda_max(B B^T)
  * decreases L at every step; tk_refine_step_size returns 1 / lambda_max from a
  * power iteration.  The workspace (tk_refine_workspace_bytes, 256-byte
- * aligned) holds the FP32 residual.  No counterpart in the reference, which
- * stops at the FDK volume. */
+ * aligned) holds the FP32 residual and the partial sums.  No counterpart in the
+ * reference, which stops at the FDK volume. */
 size_t tk_refine_checkpoint_bytes(const tk_geometry *g, int precision); /* TK_F32 or TK_F16 samples [N][H][Wp] */
 size_t tk_refine_workspace_bytes(const tk_geometry *g);
 /* q = F W p (the FFT filter of the FP32 FDK) into d_ckpt [N][H][Wp]. */

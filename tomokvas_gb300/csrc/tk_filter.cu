@@ -588,19 +588,21 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
 }
 
 // max |preprocessed sample| over the whole input, as float bits in *maxbits.
+// Each warp takes whole detector rows (lanes on consecutive columns), so the
+// row's offset is formed once per row rather than by a division per sample.
 __global__ void __launch_bounds__(256) prescan_kernel(const __grid_constant__ LoadParams L, long long nrows,
                                                       unsigned *maxbits)
 {
     float m = 0.f;
-    const long long total = nrows * L.W;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long row = i / L.W;
-        const int x = (int)(i - row * L.W);
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; row < nrows; row += nwarps) {
         int r;
         const long long off = in_row_offset(L, row, r);
-        const float v = fabsf(load_pre(L, off, r, x));
-        if (v == v) m = fmaxf(m, v);  // NaN input leaves the bound unchanged
+        for (int x = lane; x < L.W; x += 32) {
+            const float v = fabsf(load_pre(L, off, r, x));
+            if (v == v) m = fmaxf(m, v);  // NaN input leaves the bound unchanged
+        }
     }
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     __shared__ float wm[8];
@@ -612,16 +614,19 @@ __global__ void __launch_bounds__(256) prescan_kernel(const __grid_constant__ Lo
     }
 }
 
-// Turns the bound into a power-of-two storage scale: |q| <= max * L1K.
-__global__ void scale_finalize_kernel(float *scale, double L1K)
+// Turns the bound into a power-of-two storage scale: |q| <= max * L1K.  With
+// bound = f 2^eb (f in [0.5, 1)), 2^(14 - eb) is the largest power of two s
+// with s bound <= 2^14 = kScaleTarget (exact exponent arithmetic, FP32).
+__global__ void scale_finalize_kernel(float *scale, float L1K)
 {
     const float m = __uint_as_float(*reinterpret_cast<unsigned *>(scale));
     float s = 1.f;
-    const double bound = (double)m * L1K;
-    if (bound > 0.0 && isfinite(bound)) {
-        int e = (int)floor(log2((double)kScaleTarget / bound));
-        e = max(-100, min(100, e));
-        s = (float)ldexp(1.0, e);
+    const float bound = m * L1K * (1.f + 0x1p-20f);  // rounded up past the two FP32 roundings
+    if (bound > 0.f && isfinite(bound)) {
+        int eb = 0;
+        (void)frexpf(bound, &eb);
+        const int e = max(-100, min(100, 14 - eb));
+        s = ldexpf(1.f, e);
     }
     *scale = s;
 }
@@ -846,7 +851,7 @@ int launch_filter(const tk_geometry &g, const void *d_in, int input_type, int la
         TK_CUDA(cudaGetDevice(&dev));
         TK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         prescan_kernel<<<sms * 4, 256, 0, stream>>>(L, P.nrows, reinterpret_cast<unsigned *>(d_q_scale));
-        scale_finalize_kernel<<<1, 1, 0, stream>>>(d_q_scale, sp.L1K);
+        scale_finalize_kernel<<<1, 1, 0, stream>>>(d_q_scale, (float)sp.L1K);
         count_launch(2);  // prescan + finalize
         P.q_scale = d_q_scale;
     }

@@ -13,8 +13,9 @@
 // the filter: in FP32 samples, or where HBM is short in FP16 samples (half the
 // bytes, the residual formed in FP32).  A step is three launches: B^T x into
 // the FP32 residual buffer, the residual kernel (r = -alpha (B^T x - q) and
-// the loss, one pass), and B r accumulated into x.  No counterpart in the
-// reference, which stops at the FDK volume.
+// the loss's block partials, one pass), and B r accumulated into x; a fourth
+// sums the loss when it is asked for.  Sums are compensated FP32 (no FP64 on
+// the device).  No counterpart in the reference, which stops at the FDK volume.
 #include "tk_common.cuh"
 #include "tk_internal.h"
 
@@ -30,42 +31,74 @@ __global__ void ckpt_to_half_kernel(const float *__restrict__ q, __half *__restr
         out[i] = __float2half_rn(q[i]);
 }
 
-// Block sum of a per-thread FP64 value added to *out (256 threads).
-__device__ __forceinline__ void block_add(double acc, double *out)
+// Sums in FP32 with compensation (no FP64 on the device): each thread keeps a
+// Kahan sum of its terms, each block writes its threads' total to a partial
+// slot, and one block adds the partials (again compensated).  Relative error
+// about 1e-6 for the sums here, far below the loss changes a step makes.
+struct KahanF {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x)
+    {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+// Block sum (256 threads) of per-thread values into partial[blockIdx.x].
+__device__ __forceinline__ void block_partial(float v, float *partial)
 {
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    __shared__ double wsum[8];
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __shared__ float wsum[8];
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
     __syncthreads();
-    if (threadIdx.x == 0 && out) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) acc += wsum[w];
-        atomicAdd(out, acc);
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v += wsum[w];
+        partial[blockIdx.x] = v;
     }
 }
 
-// r <- -alpha (r - q) over n samples, and loss += sum (r - q)^2 (FP64).
+// r <- -alpha (r - q) over n samples; partial[block] = its part of sum (r - q)^2.
 template <bool HALF>
 __global__ void __launch_bounds__(256) residual_kernel(float *__restrict__ r, const void *__restrict__ ckpt,
-                                                       long long n, float alpha, double *loss)
+                                                       long long n, float alpha, float *partial)
 {
-    double acc = 0.0;
+    KahanF acc;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const float q = HALF ? __half2float(static_cast<const __half *>(ckpt)[i]) : static_cast<const float *>(ckpt)[i];
         const float d = r[i] - q;
-        acc += (double)d * (double)d;
+        acc.add(d * d);
         r[i] = -alpha * d;
     }
-    block_add(acc, loss);
+    block_partial(acc.s - acc.c, partial);
 }
 
-// sum x^2 (FP64) into *out.
-__global__ void __launch_bounds__(256) sumsq_kernel(const float *__restrict__ x, long long n, double *out)
+// partial[block] = its part of sum x^2.
+__global__ void __launch_bounds__(256) sumsq_kernel(const float *__restrict__ x, long long n, float *partial)
 {
-    double acc = 0.0;
+    KahanF acc;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        acc += (double)x[i] * (double)x[i];
-    block_add(acc, out);
+        acc.add(x[i] * x[i]);
+    block_partial(acc.s - acc.c, partial);
+}
+
+// *out = sum of the np partials (one block of 256 threads), widened to FP64 for the caller's loss array.
+__global__ void __launch_bounds__(256) partial_sum_kernel(const float *__restrict__ partial, int np, double *out)
+{
+    KahanF acc;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) acc.add(partial[i]);
+    float v = acc.s - acc.c;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __shared__ float wsum[8];
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        KahanF t;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t.add(wsum[w]);
+        *out = (double)(t.s - t.c);
+    }
 }
 
 __global__ void scale_kernel(float *__restrict__ x, long long n, float s)
@@ -74,7 +107,8 @@ __global__ void scale_kernel(float *__restrict__ x, long long n, float s)
         x[i] *= s;
 }
 
-// Deterministic pseudo-random start vector in [-1, 1) (a hash of the index).
+// Deterministic pseudo-random start vector in [-1, 1) (a hash of the index): the top 24 bits of
+// the hash times 2^-23, exact in FP32.
 __global__ void hash_fill_kernel(float *__restrict__ x, long long n)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -83,7 +117,7 @@ __global__ void hash_fill_kernel(float *__restrict__ x, long long n)
         h ^= h >> 31;
         h *= 0xBF58476D1CE4E5B9ull;
         h ^= h >> 29;
-        x[i] = (float)((double)(h >> 40) * (1.0 / 8388608.0)) - 1.f;
+        x[i] = (float)(unsigned)(h >> 40) * 0x1p-23f - 1.f;
     }
 }
 
@@ -108,10 +142,16 @@ extern "C" size_t tk_refine_checkpoint_bytes(const tk_geometry *g, int precision
     return (size_t)residual_elems(*g) * (precision == TK_F16 ? 2 : 4);
 }
 
+constexpr int kMaxPartials = 4096;  // block partial sums (grid_of never exceeds 8 blocks per SM)
+
+// The workspace: a TK_F32 FDK workspace (its filtered-projection area is the FP32 residual),
+// then kMaxPartials FP32 block partials.
+static size_t partials_offset(const tk_geometry *g) { return (tk_fdk_workspace_bytes(g, TK_F32) + 255) & ~(size_t)255; }
+
 extern "C" size_t tk_refine_workspace_bytes(const tk_geometry *g)
 {
     if (!g || validate_geometry(g) != TK_OK) return 0;
-    return tk_fdk_workspace_bytes(g, TK_F32);
+    return partials_offset(g) + kMaxPartials * sizeof(float);
 }
 
 static int check_workspace(const tk_geometry *g, void *d_workspace, size_t ws_bytes)
@@ -127,6 +167,10 @@ static int check_workspace(const tk_geometry *g, void *d_workspace, size_t ws_by
 // The residual buffer: the FP32 filtered-projection area of a TK_F32 workspace
 // (after its 256-byte header, which tk_refine_step_size uses for its norm).
 static float *residual_of(void *d_workspace) { return reinterpret_cast<float *>(static_cast<char *>(d_workspace) + 256); }
+static float *partials_of(const tk_geometry *g, void *d_workspace)
+{
+    return reinterpret_cast<float *>(static_cast<char *>(d_workspace) + partials_offset(g));
+}
 
 extern "C" int tk_refine_checkpoint(const tk_geometry *g, const void *d_in, int input_type, int layout,
                                     const tk_flatfield *ff, int window, void *d_ckpt, int precision,
@@ -163,19 +207,25 @@ extern "C" int tk_refine_volume(const tk_geometry *g, const void *d_ckpt, int pr
     TK_CHECK(std::isfinite(alpha) && alpha > 0.f, TK_ERR_INVALID, "refine: step size must be positive");
     if (int rc = check_workspace(g, d_workspace, workspace_bytes)) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    float *r = residual_of(d_workspace);
+    float *r = residual_of(d_workspace), *partials = partials_of(g, d_workspace);
     const long long n = residual_elems(*g);
+    const int grid = grid_of(n);
+    TK_CHECK(grid <= kMaxPartials, TK_ERR_UNSUPPORTED, "refine: %d blocks exceed the partial sums", grid);
     const float zoff = tk_default_zoff(g);
-    if (d_loss && steps > 0) TK_CUDA(cudaMemsetAsync(d_loss, 0, sizeof(double) * (size_t)steps, st));
     for (int k = 0; k < steps; ++k) {
-        // B^T x, then r = -alpha (B^T x - q) with the loss, then x += B r
+        // B^T x, then r = -alpha (B^T x - q) with the loss's block partials, then x += B r
         if (int rc = launch_forward_project(*g, d_vol, g->Z, zoff, r, 0, st)) return rc;
         if (precision == TK_F16)
-            residual_kernel<true><<<grid_of(n), 256, 0, st>>>(r, d_ckpt, n, alpha, d_loss ? d_loss + k : nullptr);
+            residual_kernel<true><<<grid, 256, 0, st>>>(r, d_ckpt, n, alpha, partials);
         else
-            residual_kernel<false><<<grid_of(n), 256, 0, st>>>(r, d_ckpt, n, alpha, d_loss ? d_loss + k : nullptr);
+            residual_kernel<false><<<grid, 256, 0, st>>>(r, d_ckpt, n, alpha, partials);
         TK_CUDA(cudaGetLastError());
         count_launch();
+        if (d_loss) {
+            partial_sum_kernel<<<1, 256, 0, st>>>(partials, grid, d_loss + k);
+            TK_CUDA(cudaGetLastError());
+            count_launch();
+        }
         if (int rc = launch_backproject(*g, r, TK_F32, nullptr, g->Z, zoff, d_vol, 1, st)) return rc;
     }
     return TK_OK;
@@ -189,9 +239,11 @@ extern "C" int tk_refine_step_size(const tk_geometry *g, int iters, float *d_vol
     TK_CHECK(iters >= 1, TK_ERR_INVALID, "refine: iters < 1");
     if (int rc = check_workspace(g, d_workspace, workspace_bytes)) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    float *r = residual_of(d_workspace);
+    float *r = residual_of(d_workspace), *partials = partials_of(g, d_workspace);
     double *acc = reinterpret_cast<double *>(d_workspace);  // the workspace header holds the norm
     const long long nv = (long long)g->X * g->Y * g->Z;
+    const int grid = grid_of(nv);
+    TK_CHECK(grid <= kMaxPartials, TK_ERR_UNSUPPORTED, "refine: %d blocks exceed the partial sums", grid);
     const float zoff = tk_default_zoff(g);
     // power iteration on B B^T from a fixed pseudo-random volume: lambda = ||B B^T x|| for ||x|| = 1
     hash_fill_kernel<<<grid_of(nv), 256, 0, st>>>(d_vol_tmp, nv);
@@ -202,10 +254,10 @@ extern "C" int tk_refine_step_size(const tk_geometry *g, int iters, float *d_vol
             if (int rc = launch_forward_project(*g, d_vol_tmp, g->Z, zoff, r, 0, st)) return rc;
             if (int rc = launch_backproject(*g, r, TK_F32, nullptr, g->Z, zoff, d_vol_tmp, 0, st)) return rc;
         }
-        TK_CUDA(cudaMemsetAsync(acc, 0, sizeof(double), st));
-        sumsq_kernel<<<grid_of(nv), 256, 0, st>>>(d_vol_tmp, nv, acc);
+        sumsq_kernel<<<grid, 256, 0, st>>>(d_vol_tmp, nv, partials);
+        partial_sum_kernel<<<1, 256, 0, st>>>(partials, grid, acc);
         TK_CUDA(cudaGetLastError());
-        count_launch();
+        count_launch(2);
         TK_CUDA(cudaMemcpyAsync(&norm, acc, sizeof(double), cudaMemcpyDeviceToHost, st));
         TK_CUDA(cudaStreamSynchronize(st));
         norm = std::sqrt(norm);
