@@ -43,7 +43,8 @@ struct __align__(64) BatchItem {
     int unit0;            // first work unit of this item
     float cX, cZ, D, dX, dY, zoff, scale, Wm1, Hm1, fscale;
     unsigned dirx, diry, dirz;
-    double halfW;         // W / 2. (kernel.cu:100)
+    float halfW;          // W / 2. (kernel.cu:100 compares in double; W / 2 and the sqrtf result are
+                          // exact in FP32, so the FP32 comparison decides the same)
 };
 
 template <int TX, int TY, int ALIGN>
@@ -427,7 +428,7 @@ int build_tables(tk_batch *b, int vi, cudaStream_t st)
         I.dirx = g.dirx ? 0x80000000u : 0u;
         I.diry = g.diry ? 0x80000000u : 0u;
         I.dirz = g.dirz ? 0x80000000u : 0u;
-        I.halfW = g.W / 2.;
+        I.halfW = (float)g.W * 0.5f;
         maxN = std::max(maxN, g.N);
         slot = std::max(slot, (BW * BH + 15) / 16 * 16);
     }

@@ -51,7 +51,8 @@ struct BPParams {
     float dX, dY, zoff, scale;
     unsigned dirx, diry, dirz;  // 0 or 0x80000000 (sign flip, kernel.cu:86-88)
     float Wm1, Hm1;             // W-1, H-1
-    double halfW;               // W / 2. (kernel.cu:100)
+    float halfW;                // W / 2. (kernel.cu:100 compares in double; W / 2 is exact in FP32, as is
+                                // the sqrtf result, so the FP32 comparison decides the same)
     float fscale;               // dfi * (1/p)  (kernel.cu:113)
     const float *q_scale;       // device storage scale of the filtered projections, or null (= 1)
     int qbase, qlen;  // quarter-turn kernel: steps q = qbase + (t mod qlen) + (t / qlen) N/4, t < 4 qlen
@@ -1340,7 +1341,7 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
     P.dirz = g.dirz ? 0x80000000u : 0u;
     P.Wm1 = (float)(g.W - 1);
     P.Hm1 = (float)(g.H - 1);
-    P.halfW = g.W / 2.;
+    P.halfW = (float)g.W * 0.5f;
     // result *= delta_f * scaling, with scaling = 1/p (kernel.cu:113, 575)
     P.fscale = g.dfi * (1.f / (float)p);
     P.q_scale = (precision == TK_F16 || precision == TK_BF16) ? d_q_scale : nullptr;
@@ -1467,7 +1468,7 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     P.dirz = g.dirz ? 0x80000000u : 0u;
     P.Wm1 = (float)(g.W - 1);
     P.Hm1 = (float)(g.H - 1);
-    P.halfW = g.W / 2.;
+    P.halfW = (float)g.W * 0.5f;
     P.fscale = g.dfi * (1.f / (float)p);  // the backprojection's scale, transposed
 
     for (int b0 = 0; b0 < g.N; b0 += kMaxParamProj) {
