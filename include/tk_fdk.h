@@ -379,8 +379,9 @@ int tk_measure_fp32_fma_rate(double *tflops_out);
  * tk_diag_wait_timeout launches one CTA that waits, with the library's bounded
  * wait and the given limit, on an mbarrier armed for copies that are never
  * issued; it leaves ERR_WAIT_TIMEOUT (0x2) in the device error word, read by
- * tk_device_error_flags.  tk_diag_shrink_box(rows) takes `rows` rows off every
- * backprojection's staged footprint box from then on (0 restores it): the
+ * tk_device_error_flags.  tk_diag_shrink_box(rows) takes `rows` rows off the
+ * staged footprint box of every per-volume backprojection launch (tk_backproject,
+ * tk_fdk_device, the handle) from then on (0 restores it): the
  * kernels' bounds checks then skip the reads that fall outside and report
  * ERR_BOX_OVERFLOW (0x1), which the handle returns as TK_ERR_DEVICE. */
 int tk_diag_wait_timeout(double limit_ms, void *stream);
