@@ -117,10 +117,13 @@ __global__ void __launch_bounds__(TX *TY, MINB)
         const int2 tc = tile_of(tile, I.tilesX, I.ntiles / I.tilesX);
         const int x0 = tc.x * TX, y0 = tc.y * TY;
         const int nz = I.nz;
-        const bool partial = nz < TZ;
+        // the z chunks of the per-volume kernel (tk_bp.cu bp_cimg_kernel), so that the results are
+        // the same bits: 16-bit storage walks only the slices left in a ragged last chunk; FP32
+        // coefficients move the last chunk down to end at nz (partial only for nz < TZ)
         const int zc = zci * TZ;
-        const int z0 = partial ? 0 : min(zc, nz - TZ);  // the last chunk ends at nz
-        const int zlast = partial ? nz - 1 : TZ - 1;
+        const bool partial = PREC != TK_F32_COEF ? zc + TZ > nz : nz < TZ;
+        const int z0 = PREC != TK_F32_COEF ? zc : (partial ? 0 : min(zc, nz - TZ));
+        const int zlast = partial ? nz - 1 - z0 : TZ - 1;
         const int x = x0 + tx, y = y0 + ty;
         const float aX = flip(I.scale * ((float)x + I.dX), I.dirx);
         const float aY = flip(I.scale * ((float)y + I.dY), I.diry);

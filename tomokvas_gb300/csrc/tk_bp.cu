@@ -359,11 +359,16 @@ __global__ void __launch_bounds__(TX *TY, MINB)
     const int tx = tid % TX, ty = tid / TX;
     const int2 tile = tile_of(blockIdx.x, P.tilesX, P.tilesY);
     const int x0 = tile.x * TX, y0 = tile.y * TY;
-    // Full chunks: the last one is moved down to end at nz and stores only
-    // the slices no earlier chunk owns.  PARTIAL handles nz < TZ.
+    // Full chunks of TZ slices.  16-bit storage: the last chunk, when fewer than
+    // TZ slices are left, walks only those slices (always with PARTIAL, for
+    // nz < TZ).  FP32 coefficients (the plain form, TZ | nz at the sizes it is
+    // timed on): the last chunk is moved down to end at nz and stores only the
+    // slices no earlier chunk owns, which keeps its walk free of the runtime choice.
     const int zc = blockIdx.y * TZ;
-    const int z0 = PARTIAL ? zc : min(zc, P.nz - TZ);
-    const int zlast = PARTIAL ? P.nz - 1 - z0 : TZ - 1;
+    constexpr bool kRuntimeRagged = PREC != TK_F32_COEF;
+    const bool ragged = PARTIAL || (kRuntimeRagged && zc + TZ > P.nz);
+    const int z0 = (PARTIAL || kRuntimeRagged) ? zc : min(zc, P.nz - TZ);
+    const int zlast = ragged ? P.nz - 1 - z0 : TZ - 1;
     const int x = x0 + tx, y = y0 + ty;
     const float aX = flip(P.scale * ((float)x + P.dX), P.dirx);
     const float aY = flip(P.scale * ((float)y + P.dY), P.diry);
@@ -433,9 +438,18 @@ __global__ void __launch_bounds__(TX *TY, MINB)
                                            (uint32_t)(kMagicBits + by0) * row_bytes;
                     const float U2 = __fmul_rn(U, U);
                     if (vlo >= 0.f && vhi <= Hm1)
-                        update_cimg<PREC, TZ, true, PARTIAL, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                        if (ragged)
+                            update_cimg<PREC, TZ, true, true, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                        else
+                            update_cimg<PREC, TZ, true, false, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
+                                                                      acc);
                     else
-                        update_cimg<PREC, TZ, false, PARTIAL, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast, acc);
+                        if (ragged)
+                            update_cimg<PREC, TZ, false, true, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
+                                                                      acc);
+                        else
+                            update_cimg<PREC, TZ, false, false, WALK>(sbase, row_bytes, v0, dv, fu, U2, Hm1, zlast,
+                                                                       acc);
                 } else {
                     atomicOr(P.err, ERR_BOX_OVERFLOW);
                 }
