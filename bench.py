@@ -108,7 +108,7 @@ def parse():
                     help="time the reference's own kernels (FBPG/kernel.cu built for sm_103a, cuFFT) on this GPU "
                          "at the 256^3 and 1024^3 workloads beside ours on the same log sinograms (Ram-Lak), "
                          "with the relative RMSE between the two")
-    ap.add_argument("--chunk", type=int, default=64, help="projections per streamed chunk (--outofcore)")
+    ap.add_argument("--chunk", type=int, default=480, help="projections per streamed chunk (--outofcore)")
     ap.add_argument("--items", type=int, default=64, help="with --batch: only the first ITEMS volumes (small case for ncu)")
     ap.add_argument("--profile-adjoint", action="store_true",
                     help="with --adjoint: small case for ncu, 120 instead of 360 projections (same 512^3 volume, "
