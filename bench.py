@@ -837,13 +837,14 @@ def adjoint_summary(steps, warmup, column_lanes=False, descent_p=False, refine_s
 
     res = {}
     L = _lib.load()
-    if column_lanes:  # the column-lane forward projector, timed beside the default
-        try:
-            _lib.check(L.tk_fp_select_variant(1))
-            ms = timeit(bwd)
-            res["backward_column_lanes"] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
-        finally:
-            _lib.check(L.tk_fp_select_variant(0))
+    if column_lanes:  # the other forward-projector forms, timed beside the default
+        for v, key in ((1, "backward_column_lanes"), (2, "backward_fp32_atomics")):
+            try:
+                _lib.check(L.tk_fp_select_variant(v))
+                ms = timeit(bwd)
+                res[key] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
+            finally:
+                _lib.check(L.tk_fp_select_variant(0))
     for name, fn in (("forward", fwd), ("backward", bwd)):
         ms = timeit(fn)
         res[name] = {"ms": ms, "gups": g.updates / (ms * 1e-3) / 1e9}
@@ -851,6 +852,14 @@ def adjoint_summary(steps, warmup, column_lanes=False, descent_p=False, refine_s
     lhs = float(torch.sum(vol.double() * y.double()).item())
     rhs = float(torch.sum(p.double() * grad.double()).item())
     res["dot_product_rel_err"] = abs(lhs - rhs) / abs(lhs)
+    if column_lanes:
+        try:
+            _lib.check(L.tk_fp_select_variant(2))
+            bwd()
+            rhs2 = float(torch.sum(p.double() * grad.double()).item())
+            res["backward_fp32_atomics"]["dot_product_rel_err"] = abs(lhs - rhs2) / abs(lhs)
+        finally:
+            _lib.check(L.tk_fp_select_variant(0))
     if descent_p:
         # 20 steps p <- p - a grad ||A p - t||^2 from the noisy projections toward the volume of the
         # noise-free ones (t = A p_clean); a from a power-iteration estimate of ||A||^2

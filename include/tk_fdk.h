@@ -294,9 +294,13 @@ int tk_bp_variant_precision(int i);
 int tk_bp_select_variant(int i);
 /* Forward projector (the scatter of tk_forward_project / tk_fdk_backward):
  * 0 (default) lanes on 32 consecutive slices of one voxel column, the warp
- * walking its columns; 1 lanes on 32 voxel columns, each walking its slices.
- * Same weights and masks (FP32 shared atomics); the sums differ by FP32
- * rounding order only. */
+ * walking its columns, accumulating each projection's box in two-word fixed
+ * point with integer shared atomics (2^-34 or finer of the tile's largest
+ * contribution; FP32 atomics when the source lies inside the field of view);
+ * 1 lanes on 32 voxel columns, each walking its slices (FP32 shared
+ * atomics); 2 the slice-lane form with FP32 shared atomics.  Same weights
+ * and masks; the sums differ by FP32 rounding only.  The fixed-point form
+ * expects finite volume values. */
 int tk_fp_select_variant(int i);
 
 /* Analytic cone-beam line integrals of ellipsoids (seeded synthetic input).

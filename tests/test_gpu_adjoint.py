@@ -32,10 +32,21 @@ GEOMS = {
 }
 
 
+@pytest.mark.parametrize("fp_variant", [0, 2])
 @pytest.mark.parametrize("name", list(GEOMS))
-def test_forward_project_is_transpose_of_backproject(cuda, name):
+def test_forward_project_is_transpose_of_backproject(cuda, name, fp_variant):
+    """<B q, y> = <q, B^T y> for the FP32-atomic and the fixed-point scatter."""
     import torch
 
+    L = _lib.load()
+    _lib.check(L.tk_fp_select_variant(fp_variant))
+    try:
+        _transpose_check(name, torch)
+    finally:
+        _lib.check(L.tk_fp_select_variant(0))
+
+
+def _transpose_check(name, torch):
     g = small_geometry(**GEOMS[name])
     rng = np.random.default_rng(1)
     q = np.zeros((g.N, g.H, device.row_pitch(g.W)), dtype=np.float32)
@@ -51,9 +62,9 @@ def test_forward_project_is_transpose_of_backproject(cuda, name):
 
 @pytest.mark.parametrize("name", list(GEOMS))
 def test_forward_projector_forms_agree(cuda, name):
-    """Slice lanes (default) and column lanes scatter the same weights: the
-    projections agree to FP32 rounding of the summation order, including a
-    partial z chunk (Z not a multiple of 32)."""
+    """Slice lanes (default), column lanes and the fixed-point slice-lane box
+    scatter the same weights: the projections agree to FP32 rounding of the
+    summation order, including a partial z chunk (Z not a multiple of 32)."""
     import torch
 
     L = _lib.load()
@@ -61,12 +72,13 @@ def test_forward_projector_forms_agree(cuda, name):
     y = np.random.default_rng(4).normal(size=(g.Z, g.Y, g.X)).astype(np.float32)
     out = []
     try:
-        for v in (0, 1):
+        for v in (0, 1, 2):
             _lib.check(L.tk_fp_select_variant(v))
             out.append(device.forward_project(g, dev(y, torch)).cpu().numpy()[:, :, :g.W])
     finally:
         _lib.check(L.tk_fp_select_variant(0))
     assert rel_rmse(out[0], out[1]) < 1e-6
+    assert rel_rmse(out[2], out[0]) < 1e-6
     assert device.device_error_flags() == 0
 
 

@@ -962,20 +962,37 @@ __global__ void __launch_bounds__(TX *TY, 2)
 // distinct banks for rows less than 32 apart.  The column geometry of a
 // projection is computed once per column (lane j for column j) into a
 // per-warp table in shared memory and read back as a broadcast.
-template <int TX, int TY, bool PARTIAL>
+//
+// FIXED: the box accumulates two-word fixed point with native integer shared
+// atomics instead of FP32 shared atomics (an FP32 add to shared memory is a
+// load and compare-and-swap loop).  Each CTA scales its contributions by a
+// power of two s chosen from the tile's largest possible contribution
+// max|g| U^2_max, so that each scaled contribution c has |c| <= 2^hb,
+// hb = min(30 - cbits, 22), where at most 2^cbits <= 2^13 contributions reach
+// one cell of one projection (bound formed on the host from the row step and
+// the ray strip).  c is split exactly into round(c) (the hi word) and the
+// remainder c - round(c), |.| <= 1/2 (<= 1 where rounding lifts |c| a few
+// ulps past 2^22), which is rounded to 2^-kb units (kb = hb; the lo word).
+// Neither word's cell sum can pass 2^30, the integer sums are exact, and the
+// resolution is 2^-(hb + kb) of the tile's largest contribution (2^-34 or
+// finer) against FP32 atomics' rounding of every partial sum.  The drain
+// forms (hi + lo 2^-kb) / s in FP32.  For finite inputs.
+template <int TX, int TY, bool PARTIAL, bool FIXED = false>
 __global__ void __launch_bounds__(TX *TY, 2)
     fp_scatter_col_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P,
-                          const float *__restrict__ vin)
+                          const float *__restrict__ vin, float u2max, int cbits)
 {
     constexpr int NT = TX * TY, NW = NT / 32, TZ = 32;
     static_assert(TX == 16 && NT == 256, "a warp owns two tile rows of 16 columns");
     extern __shared__ __align__(128) unsigned char smem[];
     const int BW = P.BW, BWp = P.BW + 1, BH = P.BH;
     float *staging = reinterpret_cast<float *>(smem);  // 2 x [BH][BW]
-    float *acc = staging + 2 * (size_t)P.stage_elems;   // [BH][BW + 1]
+    float *acc = staging + 2 * (size_t)P.stage_elems;   // [BH][BW + 1] (FIXED: hi words, then lo words)
     const int acc_elems = (BH * BWp + 31) & ~31;
-    float4 *geo = reinterpret_cast<float4 *>(acc + acc_elems);  // [NW][32] (U, fu, col, U^2)
+    int *acc_hi = reinterpret_cast<int *>(acc), *acc_lo = acc_hi + acc_elems;
+    float4 *geo = reinterpret_cast<float4 *>(acc + (FIXED ? 2 : 1) * acc_elems);  // [NW][32] (U, fu, col, U^2)
     int2 *boxo = reinterpret_cast<int2 *>(geo + NW * 32);
+    __shared__ float s_gmax[NW];
 
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int2 tile = tile_of(blockIdx.x, P.tilesX, P.tilesY);
@@ -997,6 +1014,8 @@ __global__ void __launch_bounds__(TX *TY, 2)
         boxo[b] = o;
     }
     for (int i = tid; i < BH * BWp; i += NT) acc[i] = 0.f;
+    if constexpr (FIXED)
+        for (int i = tid; i < BH * BWp; i += NT) acc_lo[i] = 0;
     // this lane's slice of the warp's 32 columns (0 for slices owned by another chunk or past the end)
     const unsigned act = __ballot_sync(0xffffffffu, gactive);
     const bool zown = lane <= zlast && z0 + lane >= zc;
@@ -1008,12 +1027,39 @@ __global__ void __launch_bounds__(TX *TY, 2)
         if (((act >> j) & 1u) && zown)
             g[j] = P.fscale * vin[(size_t)(z0 + lane) * P.slice_stride + (size_t)y * P.X + x];
     }
+    if constexpr (FIXED) {
+        float m = 0.f;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) m = fmaxf(m, fabsf(g[j]));
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) s_gmax[w] = m;
+    }
     const float aZ = flip(P.scale * ((float)min(z0 + lane, P.nz - 1) + P.zoff), P.dirz);
     const float aZf = flip(P.scale * ((float)z0 + P.zoff), P.dirz);
     const float aZl = flip(P.scale * ((float)(z0 + zlast) + P.zoff), P.dirz);
     const float cZ = P.cZ, Hm1 = P.Hm1;
     float4 *gw = geo + w * 32;
     __syncthreads();
+    float fx_inv = 1.f, lo_scale = 1.f, lo_unit = 1.f;  // FIXED: 1/s, 2^kb, 2^-kb
+    if constexpr (FIXED) {
+        float m = 0.f;
+#pragma unroll
+        for (int k = 0; k < NW; ++k) m = fmaxf(m, s_gmax[k]);
+        const float cmax = m * u2max;
+        const int hb = min(30 - cbits, 22), kb = hb;
+        int e = 0;
+        if (cmax > 0.f && cmax <= 3.0e38f) {
+            int ex;
+            (void)frexpf(cmax, &ex);  // cmax < 2^ex
+            e = max(-126, min(126, hb - ex));
+        }
+        const float fx_s = ldexpf(1.f, e);
+        fx_inv = ldexpf(1.f, -e);
+        lo_scale = ldexpf(1.f, kb);
+        lo_unit = ldexpf(1.f, -kb);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) g[j] *= fx_s;
+    }
 
     for (int b = 0; b < P.N; ++b) {
         const int bx0 = boxo[b].x, by0 = boxo[b].y;
@@ -1052,11 +1098,28 @@ __global__ void __launch_bounds__(TX *TY, 2)
                     const int row = __float_as_int(fl) - kMagicBits - by0;
                     const float wt = e.w * g[j];
                     const float w1 = wt * e.y, w0 = wt - w1;  // columns col, col+1
-                    float *r0 = acc + row * BWp + col;
-                    atomicAdd(r0, w0 - w0 * fv);
-                    atomicAdd(r0 + 1, w1 - w1 * fv);
-                    atomicAdd(r0 + BWp, w0 * fv);
-                    atomicAdd(r0 + BWp + 1, w1 * fv);
+                    const int o = row * BWp + col;
+                    if constexpr (FIXED) {
+                        // c = round(c) + r exactly (|c| <= 2^22: adding 1.5 2^23 rounds to an integer);
+                        // the words take round(c) and round(r 2^kb)
+                        auto put = [&](int k, float c) {
+                            const float hm = __fadd_rn(c, kMagic);
+                            const float r = __fsub_rn(c, __fsub_rn(hm, kMagic));
+                            const float lm = __fmaf_rn(r, lo_scale, kMagic);
+                            atomicAdd(acc_hi + k, __float_as_int(hm) - kMagicBits);
+                            atomicAdd(acc_lo + k, __float_as_int(lm) - kMagicBits);
+                        };
+                        put(o, w0 - w0 * fv);
+                        put(o + 1, w1 - w1 * fv);
+                        put(o + BWp, w0 * fv);
+                        put(o + BWp + 1, w1 * fv);
+                    } else {
+                        float *r0 = acc + o;
+                        atomicAdd(r0, w0 - w0 * fv);
+                        atomicAdd(r0 + 1, w1 - w1 * fv);
+                        atomicAdd(r0 + BWp, w0 * fv);
+                        atomicAdd(r0 + BWp + 1, w1 * fv);
+                    }
                 }
             }
         }
@@ -1065,9 +1128,15 @@ __global__ void __launch_bounds__(TX *TY, 2)
         __syncthreads();  // also: every warp is done with its geometry table
         for (int i = tid; i < BH * BW; i += NT) {
             const int r = i / BW, c = i - r * BW;
-            float *a = acc + r * BWp + c;
-            st[i] = *a;
-            *a = 0.f;
+            const int k = r * BWp + c;
+            if constexpr (FIXED) {
+                st[i] = fmaf((float)acc_lo[k], lo_unit, (float)acc_hi[k]) * fx_inv;
+                acc_hi[k] = 0;
+                acc_lo[k] = 0;
+            } else {
+                st[i] = acc[k];
+                acc[k] = 0.f;
+            }
         }
         fence_proxy_async_smem();
         __syncthreads();
@@ -1188,7 +1257,8 @@ static const BPVariant kVariants[] = {
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
 static int g_diag_box_shrink = 0;    // rows taken off every staged box (tk_diag_shrink_box)
-static int g_fp_variant = 0;  // forward projector: 0 slice lanes (fp_scatter_col_kernel), 1 column lanes
+static int g_fp_variant = 0;  // forward projector: 0 slice lanes, fixed-point box; 1 column lanes; 2 slice lanes,
+                              // FP32 atomics
 
 static const BPVariant *pick_variant(int precision)
 {
@@ -1450,12 +1520,40 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     TK_CHECK((long long)tilesX * tilesY < (1ll << 31) && zchunks < 65536, TK_ERR_UNSUPPORTED,
              "volume too large for one launch");
     const bool partial = nz < TZ;
-    // slice lanes (variant 0, the default) or column lanes (1)
-    const bool cols = g_fp_variant == 0;
-    const void *fn = cols ? (partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true>)
-                                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false>))
-                          : (partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
-                                     : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>));
+    // Slice lanes with the two-word fixed-point box (variant 0, the default), column lanes (1), or
+    // slice lanes with FP32 shared atomics (2).  The fixed-point box needs a bound on the contributions that
+    // reach one cell of one projection from one tile (a cell takes the voxels whose u lies in a
+    // 2-pixel band and whose v lies in a 2-row band):
+    //  - the columns whose u falls in a 2-pixel band lie between two rays from the source, a strip
+    //    at most w = 2 / (U_min |scale|) voxels wide; a 16 x 16 grid holds at most
+    //    16 (floor(sqrt(2) w) + 1) points of such a strip (per grid line, floor(w / max(|cos|,
+    //    |sin|)) + 1 points), and at most 256;
+    //  - per column, the slices whose row falls in a 2-row band, at most floor(2 / dv_min) + 2,
+    //    dv_min = |scale| U_min the smallest row step, and at most the 32 slices of a chunk;
+    //  with U = D / (D - S), |S| < W/2 inside the FOV: U_min = D / (D + W/2), U_max = D / (D - W/2).
+    const bool cols = g_fp_variant != 1;
+    const double hw = 0.5 * g.W;
+    const bool fixed = g_fp_variant == 0 && (double)g.D > hw;  // else U has no bound: FP32 atomics
+    int cbits = 0;
+    float u2max = 0.f;
+    if (fixed) {
+        const double umin = g.D / (g.D + hw), umax = g.D / (g.D - hw);
+        const double dv_min = std::max(std::fabs((double)g.scale) * umin, 1e-6);
+        const double ncols = std::min(256.0, 16.0 * (std::floor(std::sqrt(2.0) * 2.0 / dv_min) + 1.0));
+        const double count = ncols * std::min(32.0, std::floor(2.0 / dv_min) + 2.0);
+        while ((double)(1 << cbits) < count) ++cbits;  // <= 13
+        u2max = (float)(1.0001 * umax * umax);
+    }
+    const void *fn;
+    if (!cols)
+        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
+                     : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>);
+    else if (fixed)
+        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, true>)
+                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, true>);
+    else
+        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, false>)
+                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, false>);
 
     static thread_local BPParams P;
     std::memset(&P, 0, sizeof(P));
@@ -1499,7 +1597,8 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         TK_CHECK(cr == CUDA_SUCCESS, TK_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)cr);
-        const size_t acc_elems = (size_t)((BH * (BW + 1) + 31) & ~31);  // odd-pitch accumulation box
+        // odd-pitch accumulation box (two words per cell in the fixed-point form)
+        const size_t acc_elems = (size_t)((BH * (BW + 1) + 31) & ~31) * (fixed ? 2 : 1);
         const size_t geo_bytes = cols ? (size_t)(TX * TY / 32) * 32 * sizeof(float4) : 0;  // slice-lane form
         const size_t smem = (2 * (size_t)P.stage_elems + acc_elems) * sizeof(float) + geo_bytes +
                             (size_t)nb * sizeof(int2) + 16;
@@ -1507,8 +1606,11 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
         TK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         dim3 grid((unsigned)(tilesX * tilesY), partial ? 1u : (unsigned)zchunks, 1);
         const float *vin = d_vol;
-        void *args[] = {&tmap, &P, &vin};
-        TK_CUDA(cudaLaunchKernel(fn, grid, dim3(TX * TY), args, smem, stream));
+        float u2 = u2max;
+        int cb = cbits;
+        void *args_cols[] = {&tmap, &P, &vin, &u2, &cb};
+        void *args_rows[] = {&tmap, &P, &vin};
+        TK_CUDA(cudaLaunchKernel(fn, grid, dim3(TX * TY), cols ? args_cols : args_rows, smem, stream));
         count_launch();
     }
     return TK_OK;
@@ -1535,7 +1637,7 @@ extern "C" int tk_bp_variant_precision(int i)
 
 extern "C" int tk_fp_select_variant(int i)
 {
-    if (i < 0 || i > 1) {
+    if (i < 0 || i > 2) {
         tk::set_error("no forward-projector variant %d", i);
         return TK_ERR_INVALID;
     }
