@@ -294,8 +294,16 @@ __device__ __forceinline__ void fft_pass_c(const float2 *__restrict__ x, float2 
     }
 }
 
+// Barrier of the TPF threads of transform group grp (named barrier 1 + grp):
+// the groups of a CTA share only read-only tables, so none waits on another.
+template <int TPF>
+__device__ __forceinline__ void group_sync(int grp)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "n"(TPF) : "memory");
+}
+
 template <int LG, int M>
-__device__ __forceinline__ void fft_passes_c(float2 *&a, float2 *&b, const float2 *twp, int t)
+__device__ __forceinline__ void fft_passes_c(float2 *&a, float2 *&b, const float2 *twp, int t, int grp)
 {
     if constexpr (LG - 4 * M > 0) {
         constexpr int rem = LG - 4 * M;
@@ -303,21 +311,21 @@ __device__ __forceinline__ void fft_passes_c(float2 *&a, float2 *&b, const float
         constexpr int NS = 1 << (4 * M);
         constexpr int OFF = M >= 1 ? (1 << (4 * M)) - 16 : 0;
         fft_pass_c<R, (1 << LG), NS>(a, b, twp + OFF, t);
-        __syncthreads();
+        group_sync<fft_threads_c(1 << LG)>(grp);
         float2 *s2 = a;
         a = b;
         b = s2;
-        fft_passes_c<LG, M + 1>(a, b, twp, t);
+        fft_passes_c<LG, M + 1>(a, b, twp, t, grp);
     }
 }
 
 // Forward FFT of length 2^LG (padded buffers); ping-pongs between a and b and
-// returns the buffer holding the result.  Every thread of the CTA calls it
-// (barriers inside).
+// returns the buffer holding the result.  Every thread of the transform group
+// calls it (group barriers inside).
 template <int LG>
-__device__ __forceinline__ float2 *fft_forward_c(float2 *a, float2 *b, const float2 *twp, int t)
+__device__ __forceinline__ float2 *fft_forward_c(float2 *a, float2 *b, const float2 *twp, int t, int grp)
 {
-    fft_passes_c<LG, 0>(a, b, twp, t);
+    fft_passes_c<LG, 0>(a, b, twp, t, grp);
     return a;
 }
 
@@ -423,8 +431,8 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
             for (int x = p / 2 + t; x < p; x += TPF) bufA[pidx(x)] = make_float2(0.f, 0.f);  // zero padding
         }
         if ((pg + gridDim.x) * G < P.npairs) fetch(pg + gridDim.x);
-        __syncthreads();
-        float2 *R = fft_forward_c<LG>(bufA, bufB, twp, t);
+        group_sync<TPF>(grp);
+        float2 *R = fft_forward_c<LG>(bufA, bufB, twp, t, grp);
         float2 *Sb = (R == bufA) ? bufB : bufA;
         // conj(Z) * Hf (Hf real and even)
 #pragma unroll 4
@@ -433,8 +441,8 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
             const float2 z = R[pidx(k)];
             R[pidx(k)] = make_float2(z.x * h, -z.y * h);
         }
-        __syncthreads();
-        float2 *Q = fft_forward_c<LG>(R, Sb, twp, t);
+        group_sync<TPF>(grp);
+        float2 *Q = fft_forward_c<LG>(R, Sb, twp, t, grp);
         if (valid) {
             int r_a, r_b;
             T *qa = out + out_row_offset(P, ra, r_a);
@@ -452,7 +460,7 @@ __global__ void __launch_bounds__(kFiltThreads) filter_fft_kernel(const __grid_c
                 }
             }
         }
-        __syncthreads();  // buffers are reused by the next pair group
+        group_sync<TPF>(grp);  // buffers are reused by the next pair group
     }
 }
 
@@ -497,7 +505,7 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
         const int r1 = min(r0 + RC, H);         // coefficient rows [r0, r1)
         const int rend = min(r0 + RC, H - 1);   // last filtered row (includes the next unit's first)
         const int npair = valid ? (rend - r0 + 2) / 2 : 0;
-        // every group runs the same number of pair steps (CTA-wide barriers inside)
+        // every group runs the same number of pair steps
         const int steps = (min(RC, H - 1) + 2) / 2;
         // Raw samples x0 .. x0 + NV - 1 (x0 = t NV; NV TPF = p/2 >= W) of the
         // next step's two rows, fetched one step ahead so that their latency
@@ -541,8 +549,8 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
                 for (int x = p / 2 + t; x < p; x += TPF) bufA[pidx(x)] = make_float2(0.f, 0.f);  // zero padding
             }
             if (k + 1 < steps) fetch(k + 1);
-            __syncthreads();
-            float2 *R = fft_forward_c<LG>(bufA, bufB, twp, t);
+            group_sync<TPF>(grp);
+            float2 *R = fft_forward_c<LG>(bufA, bufB, twp, t, grp);
             float2 *Sb = (R == bufA) ? bufB : bufA;
 #pragma unroll 4
             for (int kk = t; kk < p; kk += TPF) {
@@ -550,8 +558,8 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
                 const float2 z = R[pidx(kk)];
                 R[pidx(kk)] = make_float2(z.x * h, -z.y * h);
             }
-            __syncthreads();
-            const float2 *Q = fft_forward_c<LG>(R, Sb, twp, t);
+            group_sync<TPF>(grp);
+            const float2 *Q = fft_forward_c<LG>(R, Sb, twp, t, grp);
             if (live) {
                 const size_t base = (size_t)bf * H;
                 const float zero[3] = {0.f, 0.f, 0.f};
@@ -582,7 +590,7 @@ __global__ void __launch_bounds__(kFiltThreads) filter_coef_kernel(const __grid_
                     }
                 }
             }
-            __syncthreads();  // the buffers are rewritten by the next step
+            group_sync<TPF>(grp);  // the buffers are rewritten by the next step
         }
     }
 }
