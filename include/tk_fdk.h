@@ -330,7 +330,8 @@ int tk_half_to_parallel(const float *d_in, int W, int N, int rows, int axis_move
  * output volume, geometry, filter), plan them onto one device workspace, then
  * run: each item is filtered (one launch per item), then ONE persistent
  * kernel backprojects the voxel tiles of all items, taken from a shared work
- * counter, larger items first.  tk_batch_run(use_graph = 1) captures the run
+ * counter, larger items first (items with the quarter-turn symmetry instead
+ * get tk_fdk_device's quarter-turn launch beside it, tk_batch_item_quarter_turn).  tk_batch_run(use_graph = 1) captures the run
  * into a CUDA graph on first use and replays it afterwards (inputs are read
  * from the submitted pointers at every run).  tk_batch_autotune times every
  * compiled tile shape of the batch's storage format on the planned batch and
@@ -366,9 +367,17 @@ int tk_batch_select_variant(tk_batch *b, int i);
  * (the tensor-core Toeplitz product only where it supports the width); -1 for
  * a bad index. */
 int tk_batch_item_filter_form(const tk_batch *b, int i);
+/* 1 when item i of the planned batch has the quarter-turn symmetry that
+ * tk_fdk_device's quarter-turn kernel needs (square centred unflipped volume,
+ * N divisible by 4, the storage format's quarter-turn variant selected or
+ * default): such items are backprojected by that same launch, on their filter
+ * stream beside the persistent kernel, with the per-volume bits; 0 for items
+ * of the persistent kernel; -1 for a bad index or an unplanned batch. */
+int tk_batch_item_quarter_turn(const tk_batch *b, int i);
 /* Phase times of the last eager tk_batch_run (use_graph = 0): from the run's
- * start until every item's filter has finished, and the persistent
- * backprojection launch after it (waits for that run to finish). */
+ * start until every item's filter has finished, and the backprojection after
+ * it (the persistent launch and the quarter-turn items' launches; waits for
+ * that run to finish). */
 int tk_batch_timings(tk_batch *b, float *filter_ms, float *bp_ms);
 
 /* ------------------------------------------------------------ diagnostics

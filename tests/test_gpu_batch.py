@@ -5,7 +5,8 @@ CUDA graph.
 Checks:
   * every item equals tk_fdk_device on the same input bit for bit, for each
     storage format's default tile shape (the arithmetic and its order are the
-    per-volume kernel's); items cover sinogram and projection layouts, FP32
+    per-volume kernel's; an item with the quarter-turn symmetry gets the
+    per-volume quarter-turn launch); items cover sinogram and projection layouts, FP32
     line integrals and raw uint16 counts, Ram-Lak and Hann, axis flips and a
     rotation offset, scale != 1, a volume thinner than one z chunk and one
     whose depth is not a multiple of it;
@@ -32,7 +33,11 @@ ITEMS = [
     dict(geo=dict(W=32, N=40, H=32, vol=(24, 24, 24)), layout="projection", window="hann", raw=True),
     dict(geo=dict(W=96, N=60, H=80, vol=(64, 64, 70), voxel_mm=1.0, diry=1, dirz=1), layout="sinogram",
          window="shepp_logan", raw=False),
+    # quarter-turn symmetry (square centred volume of whole 32-column tile pairs, N divisible by 4):
+    # backprojected by tk_fdk_device's quarter-turn launch inside the batch run
+    dict(geo=dict(W=64, N=80, H=56, vol=(64, 64, 40)), layout="projection", window="hann", raw=False),
 ]
+QUAD = [False] * 5 + [True]
 I0 = 60000.0
 
 
@@ -82,6 +87,9 @@ def test_batch_equals_per_volume(items, precision):
     import torch
 
     b, vols = make_batch(items, precision)
+    # the 16-bit formats take the quarter-turn launch where it applies; FP32 coefficients keep
+    # their general walk (their quarter-turn variant is selectable only), as tk_fdk_device does
+    assert b.quarter_turn_items() == (QUAD if precision != _lib.TK_F32_COEF else [False] * len(QUAD))
     b.run(graph=False)
     torch.cuda.synchronize()
     for it, v in zip(items, vols):

@@ -40,7 +40,8 @@ EXPORTS = [
     "tk_batch_workspace_bytes", "tk_batch_plan", "tk_batch_run", "tk_batch_autotune", "tk_batch_variant_count",
     "tk_batch_variant_name", "tk_batch_variant", "tk_batch_select_variant",
     "tk_half_to_full_fan", "tk_half_to_parallel", "tk_kernel_launches", "tk_measure_fp32_fma_rate",
-    "tk_filter_select_form", "tk_filter_form_for", "tk_batch_item_filter_form", "tk_batch_timings",
+    "tk_filter_select_form", "tk_filter_form_for", "tk_batch_item_filter_form", "tk_batch_item_quarter_turn",
+    "tk_batch_timings",
     "tk_refine_checkpoint_bytes", "tk_refine_workspace_bytes", "tk_refine_checkpoint", "tk_refine_volume",
     "tk_refine_step_size", "tk_diag_wait_timeout", "tk_diag_shrink_box",
 ]
@@ -133,6 +134,7 @@ def _declare(L):
     L.tk_filter_select_form.argtypes = [ip]
     L.tk_filter_form_for.argtypes = [ip, ip]
     L.tk_batch_item_filter_form.argtypes = [vp, ip]
+    L.tk_batch_item_quarter_turn.argtypes = [vp, ip]
     L.tk_batch_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
     L.tk_refine_checkpoint_bytes.argtypes = [G, ip]
     L.tk_refine_checkpoint_bytes.restype = ctypes.c_size_t

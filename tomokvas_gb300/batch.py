@@ -59,6 +59,11 @@ class Batch:
         """Filter form of every item (TK_FILTER_*): what tk_batch_autotune chose by timing."""
         return [int(self._L.tk_batch_item_filter_form(self._h, i)) for i in range(self._L.tk_batch_size(self._h))]
 
+    def quarter_turn_items(self) -> list:
+        """Per item: True where the planned batch backprojects it with tk_fdk_device's quarter-turn launch."""
+        return [int(self._L.tk_batch_item_quarter_turn(self._h, i)) == 1
+                for i in range(self._L.tk_batch_size(self._h))]
+
     def timings(self):
         """(filter phase ms, backprojection ms) of the last eager run."""
         f, b = ctypes.c_float(0.0), ctypes.c_float(0.0)

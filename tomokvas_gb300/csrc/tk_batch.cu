@@ -282,6 +282,7 @@ struct tk_batch {
         bool has_ff;
         float *d_vol;
         int filter_form = TK_FILTER_AUTO;  // chosen per item by tk_batch_autotune
+        bool quad = false;  // backprojected by the per-volume quarter-turn launch, not the persistent kernel
     };
     std::vector<Input> in;
     int precision = TK_F16;
@@ -386,6 +387,13 @@ int build_tables(tk_batch *b, int vi, cudaStream_t st)
         const tk_geometry &g = b->in[i].g;
         BatchItem &I = b->h_items[r];
         const float zoff = tk_default_zoff(&g);
+        // Items with the quarter-turn symmetry get the per-volume quarter-turn launch (the same
+        // kernel and bits as tk_fdk_device); they own no unit of the persistent kernel.
+        b->in[i].quad = backproject_quarter_ok(g, b->precision, g.Z, zoff);
+        if (b->in[i].quad) {
+            I.unit0 = units;
+            continue;
+        }
         int BW, BH;
         if (int rc = bp_box_dims(g, g.Z, zoff, V.TX, V.TY, V.TZ, true, align, &BW, &BH)) return rc;
         TK_CHECK(BW * ES / 4 <= 256, TK_ERR_UNSUPPORTED, "batch item %d: tile footprint of %d entries too wide", i,
@@ -501,16 +509,34 @@ int enqueue(tk_batch *b, cudaStream_t st)
         TK_CUDA(cudaStreamWaitEvent(st, b->fdone[k], 0));
     }
     if (timing) TK_CUDA(cudaEventRecord(b->t_ev[1], st));
-    int *counter = reinterpret_cast<int *>(b->ws);
-    TK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
-    const BatchVariant &V = kBatchVariants[b->used_variant];
-    const BatchItem *items = reinterpret_cast<const BatchItem *>(b->ws + b->off_items);
-    unsigned *err = device_error_word();
-    TK_CHECK(err, TK_ERR_CUDA, "device error word unavailable");
-    int nitems = n, nunits = b->nunits, maxN = b->maxN, slot = b->slot_elems;
-    void *args[] = {&items, &nitems, &nunits, &counter, &err, &maxN, &slot};
-    TK_CUDA(cudaLaunchKernel(V.fn, dim3((unsigned)b->grid), dim3((unsigned)(V.TX * V.TY)), args, b->smem, st));
-    count_launch();
+    // the quarter-turn items' launches follow the filters on their streams, beside the persistent
+    // kernel
+    bool any_quad = false;
+    for (int i = 0; i < n; ++i) {
+        const auto &it = b->in[i];
+        if (!it.quad) continue;
+        any_quad = true;
+        if (int rc = launch_backproject(it.g, b->ws + b->off_q[i], b->precision, scales + i, it.g.Z,
+                                        tk_default_zoff(&it.g), it.d_vol, 0, b->fstreams[i % K]))
+            return rc;
+    }
+    if (b->nunits > 0) {
+        int *counter = reinterpret_cast<int *>(b->ws);
+        TK_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
+        const BatchVariant &V = kBatchVariants[b->used_variant];
+        const BatchItem *items = reinterpret_cast<const BatchItem *>(b->ws + b->off_items);
+        unsigned *err = device_error_word();
+        TK_CHECK(err, TK_ERR_CUDA, "device error word unavailable");
+        int nitems = n, nunits = b->nunits, maxN = b->maxN, slot = b->slot_elems;
+        void *args[] = {&items, &nitems, &nunits, &counter, &err, &maxN, &slot};
+        TK_CUDA(cudaLaunchKernel(V.fn, dim3((unsigned)b->grid), dim3((unsigned)(V.TX * V.TY)), args, b->smem, st));
+        count_launch();
+    }
+    if (any_quad)
+        for (int k = 0; k < K; ++k) {
+            TK_CUDA(cudaEventRecord(b->fdone[k], b->fstreams[k]));
+            TK_CUDA(cudaStreamWaitEvent(st, b->fdone[k], 0));
+        }
     if (timing) {
         TK_CUDA(cudaEventRecord(b->t_ev[2], st));
         b->timed = true;
@@ -747,6 +773,12 @@ extern "C" int tk_batch_autotune(tk_batch *b, void *stream, int *variant_out, fl
     if (variant_out) *variant_out = best;
     if (ms_out) *ms_out = best_ms;
     return TK_OK;
+}
+
+extern "C" int tk_batch_item_quarter_turn(const tk_batch *b, int i)
+{
+    if (!b || i < 0 || i >= (int)b->in.size() || !b->planned) return -1;
+    return b->in[(size_t)i].quad ? 1 : 0;
 }
 
 extern "C" int tk_batch_item_filter_form(const tk_batch *b, int i)
