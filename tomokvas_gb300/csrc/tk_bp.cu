@@ -977,7 +977,14 @@ __global__ void __launch_bounds__(TX *TY, 2)
 // resolution is 2^-(hb + kb) of the tile's largest contribution (2^-34 or
 // finer) against FP32 atomics' rounding of every partial sum.  The drain
 // forms (hi + lo 2^-kb) / s in FP32.  For finite inputs.
-template <int TX, int TY, bool PARTIAL, bool FIXED = false>
+// FIXED 2 (cbits <= 9) drops the hi word's bias subtraction: the bits of
+// c + 1.5 2^23 are 0x4B400000 + round(c), and 0x4B400000 is a multiple of
+// 2^22, so the low 22 bits of a cell's sum of raw bits are its sum of round(c)
+// modulo 2^22, exact while that sum stays inside +-2^21 (hb = 20 - cbits); the
+// drain sign-extends them.  The lo word keeps its subtraction, with
+// kb = min(22, 30 - cbits): resolution 2^-(hb + kb), 2^-32 or finer.
+// FIXED 1 takes both subtractions (any cbits <= 13); 0 the FP32 atomics.
+template <int TX, int TY, bool PARTIAL, int FIXED = 0>
 __global__ void __launch_bounds__(TX *TY, 2)
     fp_scatter_col_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P,
                           const float *__restrict__ vin, float u2max, int cbits)
@@ -1046,7 +1053,8 @@ __global__ void __launch_bounds__(TX *TY, 2)
 #pragma unroll
         for (int k = 0; k < NW; ++k) m = fmaxf(m, s_gmax[k]);
         const float cmax = m * u2max;
-        const int hb = min(30 - cbits, 22), kb = hb;
+        const int hb = FIXED == 2 ? 20 - cbits : min(30 - cbits, 22);
+        const int kb = FIXED == 2 ? min(22, 30 - cbits) : hb;
         int e = 0;
         if (cmax > 0.f && cmax <= 3.0e38f) {
             int ex;
@@ -1106,7 +1114,10 @@ __global__ void __launch_bounds__(TX *TY, 2)
                             const float hm = __fadd_rn(c, kMagic);
                             const float r = __fsub_rn(c, __fsub_rn(hm, kMagic));
                             const float lm = __fmaf_rn(r, lo_scale, kMagic);
-                            atomicAdd(acc_hi + k, __float_as_int(hm) - kMagicBits);
+                            if constexpr (FIXED == 2)
+                                atomicAdd(reinterpret_cast<unsigned *>(acc_hi) + k, __float_as_uint(hm));
+                            else
+                                atomicAdd(acc_hi + k, __float_as_int(hm) - kMagicBits);
                             atomicAdd(acc_lo + k, __float_as_int(lm) - kMagicBits);
                         };
                         put(o, w0 - w0 * fv);
@@ -1130,7 +1141,8 @@ __global__ void __launch_bounds__(TX *TY, 2)
             const int r = i / BW, c = i - r * BW;
             const int k = r * BWp + c;
             if constexpr (FIXED) {
-                st[i] = fmaf((float)acc_lo[k], lo_unit, (float)acc_hi[k]) * fx_inv;
+                const int hs = FIXED == 2 ? (int)((unsigned)acc_hi[k] << 10) >> 10 : acc_hi[k];
+                st[i] = fmaf((float)acc_lo[k], lo_unit, (float)hs) * fx_inv;
                 acc_hi[k] = 0;
                 acc_lo[k] = 0;
             } else {
@@ -1548,12 +1560,15 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     if (!cols)
         fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
                      : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>);
+    else if (fixed && cbits <= 9)
+        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, 2>)
+                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, 2>);
     else if (fixed)
-        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, true>)
-                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, true>);
+        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, 1>)
+                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, 1>);
     else
-        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, false>)
-                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, false>);
+        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, 0>)
+                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, 0>);
 
     static thread_local BPParams P;
     std::memset(&P, 0, sizeof(P));
