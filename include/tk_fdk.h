@@ -295,7 +295,7 @@ int tk_bp_select_variant(int i);
 /* Forward projector (the scatter of tk_forward_project / tk_fdk_backward):
  * 0 (default) lanes on 32 consecutive slices of one voxel column, the warp
  * walking its columns, accumulating each projection's box in two-word fixed
- * point with integer shared atomics (2^-32 or finer of the tile's largest
+ * point with integer shared atomics (2^-25 or finer of the tile's largest
  * contribution; FP32 atomics when the source lies inside the field of view);
  * 1 lanes on 32 voxel columns, each walking its slices (FP32 shared
  * atomics); 2 the slice-lane form with FP32 shared atomics.  Same weights

@@ -983,7 +983,9 @@ __global__ void __launch_bounds__(TX *TY, 2)
 // modulo 2^22, exact while that sum stays inside +-2^21 (hb = 20 - cbits); the
 // drain sign-extends them.  The lo word keeps its subtraction, with
 // kb = min(22, 30 - cbits): resolution 2^-(hb + kb), 2^-32 or finer.
-// FIXED 1 takes both subtractions (any cbits <= 13); 0 the FP32 atomics.
+// FIXED 3 (cbits <= 8) windows the lo word the same way (kb = 21 - cbits, its
+// cell sums also inside +-2^20): no subtraction at all, resolution 2^-25 or
+// finer.  FIXED 1 takes both subtractions (any cbits <= 13); 0 the FP32 atomics.
 template <int TX, int TY, bool PARTIAL, int FIXED = 0>
 __global__ void __launch_bounds__(TX *TY, 2)
     fp_scatter_col_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ BPParams P,
@@ -1053,8 +1055,8 @@ __global__ void __launch_bounds__(TX *TY, 2)
 #pragma unroll
         for (int k = 0; k < NW; ++k) m = fmaxf(m, s_gmax[k]);
         const float cmax = m * u2max;
-        const int hb = FIXED == 2 ? 20 - cbits : min(30 - cbits, 22);
-        const int kb = FIXED == 2 ? min(22, 30 - cbits) : hb;
+        const int hb = FIXED >= 2 ? 20 - cbits : min(30 - cbits, 22);
+        const int kb = FIXED == 3 ? 21 - cbits : FIXED == 2 ? min(22, 30 - cbits) : hb;
         int e = 0;
         if (cmax > 0.f && cmax <= 3.0e38f) {
             int ex;
@@ -1114,11 +1116,14 @@ __global__ void __launch_bounds__(TX *TY, 2)
                             const float hm = __fadd_rn(c, kMagic);
                             const float r = __fsub_rn(c, __fsub_rn(hm, kMagic));
                             const float lm = __fmaf_rn(r, lo_scale, kMagic);
-                            if constexpr (FIXED == 2)
+                            if constexpr (FIXED >= 2)
                                 atomicAdd(reinterpret_cast<unsigned *>(acc_hi) + k, __float_as_uint(hm));
                             else
                                 atomicAdd(acc_hi + k, __float_as_int(hm) - kMagicBits);
-                            atomicAdd(acc_lo + k, __float_as_int(lm) - kMagicBits);
+                            if constexpr (FIXED == 3)
+                                atomicAdd(reinterpret_cast<unsigned *>(acc_lo) + k, __float_as_uint(lm));
+                            else
+                                atomicAdd(acc_lo + k, __float_as_int(lm) - kMagicBits);
                         };
                         put(o, w0 - w0 * fv);
                         put(o + 1, w1 - w1 * fv);
@@ -1141,8 +1146,9 @@ __global__ void __launch_bounds__(TX *TY, 2)
             const int r = i / BW, c = i - r * BW;
             const int k = r * BWp + c;
             if constexpr (FIXED) {
-                const int hs = FIXED == 2 ? (int)((unsigned)acc_hi[k] << 10) >> 10 : acc_hi[k];
-                st[i] = fmaf((float)acc_lo[k], lo_unit, (float)hs) * fx_inv;
+                const int hs = FIXED >= 2 ? (int)((unsigned)acc_hi[k] << 10) >> 10 : acc_hi[k];
+                const int ls = FIXED == 3 ? (int)((unsigned)acc_lo[k] << 10) >> 10 : acc_lo[k];
+                st[i] = fmaf((float)ls, lo_unit, (float)hs) * fx_inv;
                 acc_hi[k] = 0;
                 acc_lo[k] = 0;
             } else {
@@ -1560,6 +1566,9 @@ int launch_forward_project(const tk_geometry &g, const float *d_vol, int nz, flo
     if (!cols)
         fn = partial ? reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, true>)
                      : reinterpret_cast<const void *>(&fp_scatter_kernel<TX, TY, false>);
+    else if (fixed && cbits <= 8)
+        fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, 3>)
+                     : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, 3>);
     else if (fixed && cbits <= 9)
         fn = partial ? reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, true, 2>)
                      : reinterpret_cast<const void *>(&fp_scatter_col_kernel<TX, TY, false, 2>);
