@@ -26,7 +26,9 @@
 // consecutive tiles overlapping by one row so that every coefficient entry's
 // next row is in its own tile):
 //   warps 0-7    producers: read the raw rows (uint16 counts or FP32 line
-//                integrals), apply flat field + log and the cosine weight
+//                integrals; with 16-byte aligned rows copied into a per-thread
+//                two-stage shared buffer with cp.async one group of four rows
+//                ahead), apply flat field + log and the cosine weight
 //                (the FFT filter's load, tk_filter_core.cuh), split into
 //                bfloat16 parts and write 64-column chunks of G into a ring of
 //                shared-memory slots (mbarriers full/empty);
@@ -168,6 +170,19 @@ __device__ __forceinline__ void load8(const LoadParams &L, long long off, int j0
         if (j0 + e >= L.W) v[e] = 0.f;
 }
 
+// 16-byte asynchronous copy global -> shared (L2 only), and its groups.
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prior() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Raw-run staging of the producers (rows 16-byte aligned): per stage, item and
+// 16-byte half, one 16-byte slot per producer thread (consecutive threads on
+// consecutive slots), two stages.
+constexpr int kToepRawBytes = 2 * 4 * 2 * kToepProdWarps * 32 * 16;
+
 // Output row index of detector row gr = b H + r (frame groups: frame b at b/fgrp*fstride + b%fgrp).
 __device__ __forceinline__ long long frame_row(const ToepParams &P, long long gr, int &r)
 {
@@ -192,6 +207,8 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
     uint64_t *full = bars, *empty = bars + 4, *accf = bars + 8, *acce = bars + 9, *drain = bars + 10;
     volatile int *s_abort = reinterpret_cast<volatile int *>(bars + 11);
     uint32_t *s_tmem = reinterpret_cast<uint32_t *>(bars + 11) + 1;
+    unsigned char *raw = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(bars + 12) + 127) & ~static_cast<uintptr_t>(127));  // kToepRawBytes
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // Hankel cores of T: core s, row rr, element cc holds K[8 s + rr + cc - (Wk - 1)] (K even)
@@ -226,7 +243,112 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
     const uint32_t tmem = *s_tmem;
     const float sigma = P.q_scale ? *P.q_scale : 1.f;
 
-    if (warp < kToepProdWarps) {
+    if (warp < kToepProdWarps && P.L.vec) {
+        // ---------------------------------------------------------------- producers (aligned rows)
+        // As below, with each thread's runs of a group of four items copied into shared memory
+        // asynchronously one group ahead (cp.async), so that the global-load latency overlaps the
+        // conversion of the previous group.  Units u of a tile: chunk u / ngroups, group u % ngroups.
+        const int pt = tid;
+        constexpr int kMaxItems = 8;
+        const int nitems = R / 32, g8 = pt & 7, ngroups = (nitems + 3) / 4, nunits = nk * ngroups;
+        const bool f32in = P.L.input_type != TK_INPUT_U16;
+        const int esz = f32in ? 4 : 2;
+        auto slot16 = [&](int st, int m, int h) -> unsigned char * {
+            return raw + ((size_t)(((st * 4 + m) * 2 + h) * (kToepProdWarps * 32) + pt) << 4);
+        };
+        uint32_t cnt = 0;
+        for (long long tile = blockIdx.x; tile < P.ntiles && !*s_abort; tile += gridDim.x) {
+            const long long row0 = tile * (R - 1);
+            long long off[kMaxItems];
+            int rq[kMaxItems];
+#pragma unroll
+            for (int m = 0; m < kMaxItems; ++m) {
+                const long long gr = row0 + (pt >> 3) + 32 * m;
+                rq[m] = -1;
+                off[m] = 0;
+                if (m < nitems && gr < P.nrows) {
+                    int r, rr;
+                    off[m] = in_row_offset(P.L, frame_row(P, gr, r), rr);
+                    rq[m] = r;
+                }
+            }
+            auto issue = [&](int u) {
+                const int kc = u / ngroups, g = u - kc * ngroups, st = u & 1;
+                const int j0 = P.Wk - 8 - (kc * 64 + g8 * 8);
+                if (j0 >= W) return;  // the run lies past the row: zeros, nothing to copy
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    const int r = g ? rq[4 + m] : rq[m];
+                    if (r < 0) continue;
+                    const char *src = static_cast<const char *>(P.L.in) + ((g ? off[4 + m] : off[m]) + j0) * esz;
+                    cp_async16(smem_u32(slot16(st, m, 0)), src);
+                    if (f32in && j0 + 4 < W) cp_async16(smem_u32(slot16(st, m, 1)), src + 16);
+                }
+            };
+            issue(0);
+            cp_async_commit();
+            for (int u = 0; u < nunits; ++u) {
+                const int kc = u / ngroups, g = u - kc * ngroups, st = u & 1;
+                if (u + 1 < nunits) issue(u + 1);
+                cp_async_commit();
+                cp_async_wait_prior();  // this unit's copies have landed
+                const int slot = (int)(cnt % (uint32_t)S);
+                if (g == 0 && cnt >= (uint32_t)S && !mbar_wait_bounded(&empty[slot], ((cnt / S) - 1) & 1u, kWaitLimitNs)) {
+                    atomicOr(P.err, ERR_WAIT_TIMEOUT);
+                    *s_abort = 1;
+                }
+                if (*s_abort) break;
+                unsigned char *hi = ring + (size_t)slot * 2 * slot_part, *lo = hi + slot_part;
+                const int j0 = P.Wk - 8 - (kc * 64 + g8 * 8);
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    if (4 * g + m >= nitems) break;
+                    const int r = g ? rq[4 + m] : rq[m];
+                    float v[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) v[e] = 0.f;
+                    if (r >= 0 && j0 < W) {
+                        const uint4 a = *reinterpret_cast<const uint4 *>(slot16(st, m, 0));
+                        if (!f32in) {
+                            const uint32_t w4[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {  // count c as (2^23 + c) - 2^23: exact
+                                v[2 * e] = __uint_as_float(0x4B000000u | (w4[e] & 0xffffu)) - 8388608.f;
+                                v[2 * e + 1] = __uint_as_float(0x4B000000u | (w4[e] >> 16)) - 8388608.f;
+                            }
+                        } else {
+                            v[0] = __uint_as_float(a.x), v[1] = __uint_as_float(a.y);
+                            v[2] = __uint_as_float(a.z), v[3] = __uint_as_float(a.w);
+                            if (j0 + 4 < W) {
+                                const uint4 b2 = *reinterpret_cast<const uint4 *>(slot16(st, m, 1));
+                                v[4] = __uint_as_float(b2.x), v[5] = __uint_as_float(b2.y);
+                                v[6] = __uint_as_float(b2.z), v[7] = __uint_as_float(b2.w);
+                            }
+                        }
+                        const float rt = weight_row_term(P.L, r);
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) v[e] = (j0 + e < W) ? pre_from_raw(P.L, r, j0 + e, v[e], rt) : 0.f;
+                    }
+                    // core row: element cc holds column j0 + 7 - cc (the reversed K order)
+                    uint4 h, l;
+                    split_bf16x2(v[7], v[6], h.x, l.x);
+                    split_bf16x2(v[5], v[4], h.y, l.y);
+                    split_bf16x2(v[3], v[2], h.z, l.z);
+                    split_bf16x2(v[1], v[0], h.w, l.w);
+                    const int i = (pt >> 3) + 32 * (4 * g + m);
+                    const uint32_t o = (uint32_t)(i >> 3) * 1024u + (uint32_t)g8 * 128u + (uint32_t)(i & 7) * 16u;
+                    *reinterpret_cast<uint4 *>(hi + o) = h;
+                    *reinterpret_cast<uint4 *>(lo + o) = l;
+                }
+                if (g == ngroups - 1) {
+                    fence_proxy_async_smem();
+                    mbar_arrive(&full[slot]);
+                    ++cnt;
+                }
+            }
+            asm volatile("cp.async.wait_all;" ::: "memory");  // nothing in flight into the staging
+        }
+    } else if (warp < kToepProdWarps) {
         // ---------------------------------------------------------------- producers
         const int pt = tid;  // 0 .. 255
         // A thread's items of a chunk are rows (pt >> 3) + 32 m, m < R/32, at column group pt & 7:
@@ -514,7 +636,7 @@ int launch_filter_toeplitz(const LoadParams &L, const float *Hf, int p, void *d_
         P.khl[m] = (uint32_t)hi | ((uint32_t)lo << 16);
     }
     const size_t smem = 1024 + (size_t)P.ncores * 256 + (size_t)P.slots * 2 * P.R * 128 +
-                        (size_t)33 * kToepPitch * 4 + 12 * 8 + 16;
+                        (size_t)33 * kToepPitch * 4 + 12 * 8 + 128 + (L.vec ? kToepRawBytes : 0);
     TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "filter: Toeplitz form needs %zu B of shared memory", smem);
     const void *fn = nullptr;
     switch (precision) {
