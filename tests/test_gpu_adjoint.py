@@ -24,11 +24,15 @@ def dev(a, torch):
 
 # Row steps of consecutive slices, |scale| D / (D + W/2), below, near and
 # above one detector row: "fine_voxels" (0.36: several slices share a row, the
-# most shared-atomic collisions), "plain" (0.95) and "flips_scale" (1.43).
+# most shared-atomic collisions), "half_row" (0.60), "plain" (0.95) and
+# "flips_scale" (1.43).  They also cover the three forms of the fixed-point box
+# (at most 2^cbits contributions per cell): cbits 10 (both words with their
+# bias subtraction), 9 (the hi word windowed) and 8, 7 (both words windowed).
 GEOMS = {
     "plain": dict(W=64, N=72, H=56, vol=(48, 48, 40)),
     "flips_scale": dict(W=60, N=50, H=64, vol=(40, 36, 45), voxel_mm=1.2, dirx=1, dirz=1, rot=0.4),
     "fine_voxels": dict(W=64, N=40, H=48, vol=(48, 40, 36), voxel_mm=0.3),
+    "half_row": dict(W=64, N=48, H=56, vol=(40, 44, 38), voxel_mm=0.5, diry=1, rot=0.2),
 }
 
 
