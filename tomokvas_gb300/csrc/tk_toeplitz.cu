@@ -51,6 +51,9 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 namespace tk {
@@ -625,15 +628,32 @@ int launch_filter_toeplitz(const LoadParams &L, const float *Hf, int p, void *d_
     // kind::f16 descriptor: D F32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1), both K-major,
     // N >> 3 at bits 17-22, M >> 4 at bits 24-28
     P.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(P.R >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-    // spatial kernel of the float spectrum (the FFT filter's unnormalised inverse), FP64, split hi/lo
-    std::vector<double> ct(p);
-    for (int k = 0; k < p; ++k) ct[k] = std::cos(2.0 * M_PI * k / p);
-    for (int m = 0; m <= P.kmax; ++m) {
-        double s = (double)Hf[0] + (double)Hf[p / 2] * ((m & 1) ? -1.0 : 1.0);
-        for (int k = 1; k < p / 2; ++k) s += 2.0 * (double)Hf[k] * ct[(int)(((long long)k * m) % p)];
-        const uint16_t hi = bf16_rn(s);
-        const uint16_t lo = bf16_rn(s - bf16_value(hi));
-        P.khl[m] = (uint32_t)hi | ((uint32_t)lo << 16);
+    // spatial kernel of the float spectrum (the FFT filter's unnormalised inverse), FP64, split hi/lo;
+    // cached per (p, kmax, spectrum bytes): the sum costs about p kmax / 2 table terms, milliseconds
+    // at W = 512, which small filter launches would otherwise wait for on the host
+    {
+        static std::mutex mu;
+        static std::map<std::tuple<int, int, uint64_t>, std::vector<uint32_t>> cache;
+        uint64_t hsh = 1469598103934665603ull;  // FNV-1a over the spectrum's bytes
+        const unsigned char *hb = reinterpret_cast<const unsigned char *>(Hf);
+        for (size_t i = 0; i < (size_t)(p / 2 + 1) * sizeof(float); ++i) hsh = (hsh ^ hb[i]) * 1099511628211ull;
+        const auto key = std::make_tuple(p, P.kmax, hsh);
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it == cache.end()) {
+            std::vector<uint32_t> khl(P.kmax + 1);
+            std::vector<double> ct(p);
+            for (int k = 0; k < p; ++k) ct[k] = std::cos(2.0 * M_PI * k / p);
+            for (int m = 0; m <= P.kmax; ++m) {
+                double s = (double)Hf[0] + (double)Hf[p / 2] * ((m & 1) ? -1.0 : 1.0);
+                for (int k = 1; k < p / 2; ++k) s += 2.0 * (double)Hf[k] * ct[(size_t)k * m & (size_t)(p - 1)];
+                const uint16_t hi = bf16_rn(s);
+                const uint16_t lo = bf16_rn(s - bf16_value(hi));
+                khl[m] = (uint32_t)hi | ((uint32_t)lo << 16);
+            }
+            it = cache.emplace(key, std::move(khl)).first;
+        }
+        std::memcpy(P.khl, it->second.data(), it->second.size() * sizeof(uint32_t));
     }
     const size_t smem = 1024 + (size_t)P.ncores * 256 + (size_t)P.slots * 2 * P.R * 128 +
                         (size_t)33 * kToepPitch * 4 + 12 * 8 + 128 + (L.vec ? kToepRawBytes : 0);
