@@ -24,7 +24,9 @@
 //
 // CTA roles (one CTA per SM, persistent over row tiles of R detector rows,
 // consecutive tiles overlapping by one row so that every coefficient entry's
-// next row is in its own tile):
+// next row is in its own tile; two accumulators of mt x R columns in tensor
+// memory, so that a tile's MMAs run while the epilogue drains the previous
+// tile's):
 //   warps 0-7    producers: read the raw rows (uint16 counts or FP32 line
 //                integrals; with 16-byte aligned rows copied into a per-thread
 //                two-stage shared buffer with cp.async one group of four rows
@@ -35,8 +37,9 @@
 //   warp 12      tensor-memory allocation and, from one lane, the MMAs:
 //                per chunk 4 K-steps x 3 products x mt column tiles of
 //                tcgen05.mma.cta_group::1.kind::f16 (M = 128 output columns,
-//                N = R rows, K = 16); tcgen05.commit releases the slot, and
-//                after the last chunk signals the accumulator;
+//                N = R rows, K = 16) into the tile's accumulator (tile parity);
+//                tcgen05.commit releases the slot, and after the last chunk
+//                signals that accumulator;
 //   warps 8-11   epilogue (TMEM lane quarters 0-3): tcgen05.ld the
 //                accumulator 32 rows at a time, stage it in shared memory,
 //                write the storage format (FP32 samples or the bilinear
@@ -207,11 +210,12 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
     unsigned char *ring = hank_lo + (size_t)P.ncores * 128;  // slot s: hi at s*2*slot_part, lo after it
     float *stage = reinterpret_cast<float *>(ring + (size_t)S * 2 * slot_part);
     uint64_t *bars = reinterpret_cast<uint64_t *>(stage + 33 * kToepPitch);
-    uint64_t *full = bars, *empty = bars + 4, *accf = bars + 8, *acce = bars + 9, *drain = bars + 10;
-    volatile int *s_abort = reinterpret_cast<volatile int *>(bars + 11);
-    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(bars + 11) + 1;
+    // full/empty per ring slot (up to 8), accf/acce per accumulator buffer (2), drain
+    uint64_t *full = bars, *empty = bars + 8, *accf = bars + 16, *acce = bars + 18, *drain = bars + 20;
+    volatile int *s_abort = reinterpret_cast<volatile int *>(bars + 21);
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(bars + 21) + 1;
     unsigned char *raw = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(bars + 12) + 127) & ~static_cast<uintptr_t>(127));  // kToepRawBytes
+        (reinterpret_cast<uintptr_t>(bars + 22) + 127) & ~static_cast<uintptr_t>(127));  // kToepRawBytes
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // Hankel cores of T: core s, row rr, element cc holds K[8 s + rr + cc - (Wk - 1)] (K even)
@@ -227,8 +231,10 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
             mbar_init(&full[s], kToepProdWarps * 32);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accf, 1);
-        mbar_init(acce, 4 * 32);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], 4 * 32);
+        }
         mbar_init(drain, 1);
         *s_abort = 0;
         fence_mbar_init();
@@ -431,7 +437,8 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
         const int H = P.L.H;
         uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, ++it) {
-            if (!mbar_wait_bounded(accf, it & 1u, kWaitLimitNs)) {
+            // accumulator buffer it & 1, its (it >> 1)-th use
+            if (!mbar_wait_bounded(&accf[it & 1u], (it >> 1) & 1u, kWaitLimitNs)) {
                 atomicOr(P.err, ERR_WAIT_TIMEOUT);
                 *s_abort = 1;
             }
@@ -440,7 +447,7 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
             const long long row0 = tile * (R - 1);
             for (int m = 0; m < mt; ++m) {
                 for (int i0 = 0; i0 < R - 1; i0 += 32) {
-                    const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16);
+                    const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16) + (it & 1u) * (uint32_t)(mt * R);
                     const int ilast = min(i0 + 32, R - 1);
                     {
                         float v[32];
@@ -507,7 +514,7 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
                 }
             }
             tc_fence_before();
-            mbar_arrive(acce);
+            mbar_arrive(&acce[it & 1u]);
         }
     } else if (warp == kToepProdWarps + 4) {
         // ---------------------------------------------------------------- MMA issue (one lane)
@@ -516,7 +523,8 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
             uint32_t cnt = 0, it = 0;
             bool issued_any = false;
             for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, ++it) {
-                if (it > 0 && !mbar_wait_bounded(acce, (it - 1) & 1u, kWaitLimitNs)) {
+                // two accumulator buffers: tile it waits only for the epilogue of tile it - 2
+                if (it > 1 && !mbar_wait_bounded(&acce[it & 1u], ((it >> 1) - 1) & 1u, kWaitLimitNs)) {
                     atomicOr(P.err, ERR_WAIT_TIMEOUT);
                     *s_abort = 1;
                 }
@@ -541,7 +549,7 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
                             const uint32_t core = (uint32_t)(16 * m + 8 * kc + 2 * ks) * 128u;
                             const uint64_t ah = umma_desc(hhi + core, 128u, 128u);
                             const uint64_t al = umma_desc(hlo + core, 128u, 128u);
-                            const uint32_t d = tmem + (uint32_t)(m * R);
+                            const uint32_t d = tmem + (it & 1u) * (uint32_t)(mt * R) + (uint32_t)(m * R);
                             umma_bf16(d, ah, bh, P.idesc, (kc > 0 || ks > 0) ? 1u : 0u);
                             umma_bf16(d, ah, bl, P.idesc, 1u);
                             umma_bf16(d, al, bh, P.idesc, 1u);
@@ -551,7 +559,7 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
                     umma_commit(&empty[slot]);  // the slot is free once these MMAs have read it
                 }
                 if (*s_abort) break;
-                umma_commit(accf);
+                umma_commit(&accf[it & 1u]);
             }
             if (issued_any) {  // every MMA has completed before the tensor memory is released
                 umma_commit(drain);
@@ -615,15 +623,17 @@ int launch_filter_toeplitz(const LoadParams &L, const float *Hf, int p, void *d_
     P.Wk = (W + 63) / 64 * 64;
     P.nk = P.Wk / 64;
     P.mt = (W + 127) / 128;
-    static const int kRows[5] = {0, 256, 256, 160, 128};  // rows per tile: mt R <= 512 accumulator columns
+    // rows per tile: two accumulators of mt x R columns in the 512 of tensor memory (R a multiple of
+    // 32: the producers' row groups)
+    static const int kRows[5] = {0, 128, 128, 64, 64};
     P.R = kRows[P.mt];
-    P.slots = P.R >= 256 ? 2 : 3;
+    P.slots = P.R >= 128 ? 4 : 6;
     P.ncores = 16 * P.mt + P.Wk / 8;
     P.kmax = std::max(P.Wk - 1, 128 * P.mt + 7);
     TK_CHECK(P.kmax <= kToepKmax, TK_ERR_UNSUPPORTED, "filter: Toeplitz kernel table too short");
     P.ntiles = (nrows + P.R - 2) / (P.R - 1);
     uint32_t cols = 32;
-    while (cols < (uint32_t)(P.mt * P.R)) cols <<= 1;
+    while (cols < (uint32_t)(2 * P.mt * P.R)) cols <<= 1;
     P.tmem_cols = cols;
     // kind::f16 descriptor: D F32 (bits 4-5 = 1), A and B BF16 (bits 7-9, 10-12 = 1), both K-major,
     // N >> 3 at bits 17-22, M >> 4 at bits 24-28
@@ -656,7 +666,7 @@ int launch_filter_toeplitz(const LoadParams &L, const float *Hf, int p, void *d_
         std::memcpy(P.khl, it->second.data(), it->second.size() * sizeof(uint32_t));
     }
     const size_t smem = 1024 + (size_t)P.ncores * 256 + (size_t)P.slots * 2 * P.R * 128 +
-                        (size_t)33 * kToepPitch * 4 + 12 * 8 + 128 + (L.vec ? kToepRawBytes : 0);
+                        (size_t)33 * kToepPitch * 4 + 22 * 8 + 128 + (L.vec ? kToepRawBytes : 0);
     TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "filter: Toeplitz form needs %zu B of shared memory", smem);
     const void *fn = nullptr;
     switch (precision) {
