@@ -34,17 +34,18 @@
 //                (the FFT filter's load, tk_filter_core.cuh), split into
 //                bfloat16 parts and write 64-column chunks of G into a ring of
 //                shared-memory slots (mbarriers full/empty);
-//   warp 12      tensor-memory allocation and, from one lane, the MMAs:
+//   warp 16      tensor-memory allocation and, from one lane, the MMAs:
 //                per chunk 4 K-steps x 3 products x mt column tiles of
 //                tcgen05.mma.cta_group::1.kind::f16 (M = 128 output columns,
 //                N = R rows, K = 16) into the tile's accumulator (tile parity);
 //                tcgen05.commit releases the slot, and after the last chunk
 //                signals that accumulator;
-//   warps 8-11   epilogue (TMEM lane quarters 0-3): tcgen05.ld the
-//                accumulator 32 rows at a time, stage it in shared memory,
-//                write the storage format (FP32 samples or the bilinear
-//                coefficient image, scaled by the storage scale) with each
-//                warp storing consecutive columns of one row.
+//   warps 8-15   epilogue, two sets of four (TMEM lane quarters 0-3) taking
+//                alternate 32-row chunks, each set with its own staging
+//                buffer and named barrier: tcgen05.ld the accumulator, stage
+//                it in shared memory, write the storage format (FP32 samples
+//                or the bilinear coefficient image, scaled by the storage
+//                scale) with each warp storing consecutive columns of one row.
 // Every wait is bounded; a timeout sets ERR_WAIT_TIMEOUT and every role
 // leaves its loop; the MMAs issued are drained before the tensor memory is
 // freed.
@@ -64,7 +65,8 @@ namespace tk {
 constexpr int kToepMaxW = 512;        // one pass: the accumulator of mt x R <= 512 columns
 constexpr int kToepKmax = 528;        // |m| <= max(Wk - 1, 128 mt + 7)
 constexpr int kToepProdWarps = 8;
-constexpr int kToepThreads = (kToepProdWarps + 4 + 1) * 32;  // producers, epilogue, MMA
+constexpr int kToepEpiWarps = 8;  // two sets of four (one per TMEM lane quarter), alternate chunks
+constexpr int kToepThreads = (kToepProdWarps + kToepEpiWarps + 1) * 32;  // producers, epilogue, MMA
 constexpr int kToepPitch = 132;       // epilogue staging row pitch (floats): 129 used, 16-byte rows
 
 struct ToepParams {
@@ -209,7 +211,7 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
     unsigned char *hank_lo = hank_hi + (size_t)P.ncores * 128;
     unsigned char *ring = hank_lo + (size_t)P.ncores * 128;  // slot s: hi at s*2*slot_part, lo after it
     float *stage = reinterpret_cast<float *>(ring + (size_t)S * 2 * slot_part);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + 33 * kToepPitch);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(stage + 2 * 33 * kToepPitch);  // a staging buffer per set
     // full/empty per ring slot (up to 8), accf/acce per accumulator buffer (2), drain
     uint64_t *full = bars, *empty = bars + 8, *accf = bars + 16, *acce = bars + 18, *drain = bars + 20;
     volatile int *s_abort = reinterpret_cast<volatile int *>(bars + 21);
@@ -233,13 +235,13 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&accf[b], 1);
-            mbar_init(&acce[b], 4 * 32);
+            mbar_init(&acce[b], kToepEpiWarps * 32);
         }
         mbar_init(drain, 1);
         *s_abort = 0;
         fence_mbar_init();
     }
-    if (warp == kToepProdWarps + 4) {  // the MMA warp owns the tensor memory
+    if (warp == kToepProdWarps + kToepEpiWarps) {  // the MMA warp owns the tensor memory
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
                      "r"(P.tmem_cols)
                      : "memory");
@@ -426,7 +428,7 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
                 mbar_arrive(&full[slot]);
             }
         }
-    } else if (warp < kToepProdWarps + 4) {
+    } else if (warp < kToepProdWarps + kToepEpiWarps) {
         // ---------------------------------------------------------------- epilogue
         // Per 32-row chunk of a column tile: warp q loads its TMEM lane quarter (output columns
         // 32 q .. 32 q + 31, one per thread, 33 rows), and the chunk is staged in shared memory
@@ -434,6 +436,9 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
         // writes rows q + 4 k of columns 4 lane .. 4 lane + 3: each warp store covers consecutive
         // columns of one row.
         const int q = warp & 3;  // TMEM lane quarter
+        const int set = (warp - kToepProdWarps) >> 2;  // chunks of this set's parity, its own staging
+        float *stg = stage + set * 33 * kToepPitch;
+        int ci = 0;
         const int H = P.L.H;
         uint32_t it = 0;
         for (long long tile = blockIdx.x; tile < P.ntiles; tile += gridDim.x, ++it) {
@@ -447,6 +452,7 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
             const long long row0 = tile * (R - 1);
             for (int m = 0; m < mt; ++m) {
                 for (int i0 = 0; i0 < R - 1; i0 += 32) {
+                    if ((ci++ & 1) != set) continue;
                     const uint32_t tq = tmem + ((uint32_t)(32 * q) << 16) + (it & 1u) * (uint32_t)(mt * R);
                     const int ilast = min(i0 + 32, R - 1);
                     {
@@ -456,8 +462,8 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
                         tmem_wait_ld();
                         const bool cin = 128 * m + 32 * q + lane < W;
 #pragma unroll
-                        for (int i = 0; i < 32; ++i) stage[i * kToepPitch + 32 * q + lane] = cin ? v[i] * sigma : 0.f;
-                        stage[32 * kToepPitch + 32 * q + lane] = cin ? v32 * sigma : 0.f;
+                        for (int i = 0; i < 32; ++i) stg[i * kToepPitch + 32 * q + lane] = cin ? v[i] * sigma : 0.f;
+                        stg[32 * kToepPitch + 32 * q + lane] = cin ? v32 * sigma : 0.f;
                     }
                     if (q == 0) {  // the next column tile's first column (warp-uniform loads)
                         const bool nt = m + 1 < mt;
@@ -470,11 +476,11 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
                         if (lane == 0) {
                             const bool nin = nt && 128 * (m + 1) < W;
 #pragma unroll
-                            for (int i = 0; i < 32; ++i) stage[i * kToepPitch + 128] = nin ? t[i] * sigma : 0.f;
-                            stage[32 * kToepPitch + 128] = nin ? t32 * sigma : 0.f;
+                            for (int i = 0; i < 32; ++i) stg[i * kToepPitch + 128] = nin ? t[i] * sigma : 0.f;
+                            stg[32 * kToepPitch + 128] = nin ? t32 * sigma : 0.f;
                         }
                     }
-                    asm volatile("bar.sync 1, 128;" ::: "memory");
+                    asm volatile("bar.sync %0, 128;" ::"r"(1 + set) : "memory");
                     const int cl = 4 * lane, c0 = 128 * m + cl;
                     if (c0 < W) {
                         // detector row r of frame b for row i0 + q (one division), then stepped by 4
@@ -486,17 +492,17 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
                             if (i0 + i < R - 1 && row0 + i0 + i < P.nrows) {
                                 const long long bf = P.fgrp > 0 ? b / P.fgrp * P.fstride + b % P.fgrp : b;
                                 const long long orow = bf * H + r;
-                                const float4 a4 = *reinterpret_cast<const float4 *>(stage + i * kToepPitch + cl);
+                                const float4 a4 = *reinterpret_cast<const float4 *>(stg + i * kToepPitch + cl);
                                 if (MODE == TK_F32) {
                                     *reinterpret_cast<float4 *>(static_cast<float *>(P.out) + orow * P.pitch + c0) = a4;
                                 } else {
-                                    const float a[5] = {a4.x, a4.y, a4.z, a4.w, stage[i * kToepPitch + cl + 4]};
+                                    const float a[5] = {a4.x, a4.y, a4.z, a4.w, stg[i * kToepPitch + cl + 4]};
                                     float bb[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
                                     if (r < H - 1) {  // the next detector row (0 below the last one)
                                         const float4 b4 =
-                                            *reinterpret_cast<const float4 *>(stage + (i + 1) * kToepPitch + cl);
+                                            *reinterpret_cast<const float4 *>(stg + (i + 1) * kToepPitch + cl);
                                         bb[0] = b4.x, bb[1] = b4.y, bb[2] = b4.z, bb[3] = b4.w;
-                                        bb[4] = stage[(i + 1) * kToepPitch + cl + 4];
+                                        bb[4] = stg[(i + 1) * kToepPitch + cl + 4];
                                     }
                                     const size_t base = (size_t)orow * P.pitch;
                                     emit_coef_pair<MODE>(P.out, base, c0, W, a, bb);
@@ -510,13 +516,13 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
                             }
                         }
                     }
-                    asm volatile("bar.sync 1, 128;" ::: "memory");  // the staging is rewritten next
+                    asm volatile("bar.sync %0, 128;" ::"r"(1 + set) : "memory");  // the staging is rewritten next
                 }
             }
             tc_fence_before();
             mbar_arrive(&acce[it & 1u]);
         }
-    } else if (warp == kToepProdWarps + 4) {
+    } else if (warp == kToepProdWarps + kToepEpiWarps) {
         // ---------------------------------------------------------------- MMA issue (one lane)
         if (lane == 0) {
             const uint32_t hhi = smem_u32(hank_hi), hlo = smem_u32(hank_lo), rbase = smem_u32(ring);
@@ -571,7 +577,7 @@ __global__ void __launch_bounds__(kToepThreads, 1) filter_toeplitz_kernel(const 
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == kToepProdWarps + 4)
+    if (warp == kToepProdWarps + kToepEpiWarps)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(P.tmem_cols)
                      : "memory");
 }
@@ -627,7 +633,7 @@ int launch_filter_toeplitz(const LoadParams &L, const float *Hf, int p, void *d_
     // 32: the producers' row groups)
     static const int kRows[5] = {0, 128, 128, 64, 64};
     P.R = kRows[P.mt];
-    P.slots = P.R >= 128 ? 4 : 6;
+    P.slots = P.R >= 128 ? 3 : 5;
     P.ncores = 16 * P.mt + P.Wk / 8;
     P.kmax = std::max(P.Wk - 1, 128 * P.mt + 7);
     TK_CHECK(P.kmax <= kToepKmax, TK_ERR_UNSUPPORTED, "filter: Toeplitz kernel table too short");
@@ -666,7 +672,7 @@ int launch_filter_toeplitz(const LoadParams &L, const float *Hf, int p, void *d_
         std::memcpy(P.khl, it->second.data(), it->second.size() * sizeof(uint32_t));
     }
     const size_t smem = 1024 + (size_t)P.ncores * 256 + (size_t)P.slots * 2 * P.R * 128 +
-                        (size_t)33 * kToepPitch * 4 + 22 * 8 + 128 + (L.vec ? kToepRawBytes : 0);
+                        (size_t)2 * 33 * kToepPitch * 4 + 22 * 8 + 128 + (L.vec ? kToepRawBytes : 0);
     TK_CHECK(smem <= 227 * 1024, TK_ERR_UNSUPPORTED, "filter: Toeplitz form needs %zu B of shared memory", smem);
     const void *fn = nullptr;
     switch (precision) {
