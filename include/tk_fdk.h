@@ -36,7 +36,7 @@ typedef enum tk_status {
     TK_ERR_STATE = 4,       /* call out of sequence (e.g. before initialize) */
     TK_ERR_IO = 5,          /* file I/O failure */
     TK_ERR_DEVICE = 6,      /* a kernel reported a failed self-check */
-    TK_ERR_UNSUPPORTED = 7  /* valid request this build does not handle */
+    TK_ERR_UNSUPPORTED = 7  /* valid request the library does not handle */
 } tk_status;
 
 typedef enum tk_window {   /* ramp filter apodisation */
