@@ -61,8 +61,8 @@ def test_form_selection():
 @pytest.mark.parametrize("W", [8, 24, 64, 130, 200, 256, 300, 384, 500, 512])
 @pytest.mark.parametrize("window", ["ramlak", "hann"])
 def test_toeplitz_filter_matches_fft(orc, cuda, W, window):
-    """FP32 samples: N x H = 24 x 70 rows (several row tiles per CTA, tiles
-    spanning projections), sinogram-major random input."""
+    """FP32 samples: N x H = 24 x 70 rows (row tiles spanning projections),
+    sinogram-major random input."""
     import torch
 
     g = small_geometry(W=W, N=24, H=70, vol=(16, 16, 8))
@@ -84,6 +84,61 @@ def test_toeplitz_filter_matches_fft(orc, cuda, W, window):
     assert not np.array_equal(qt, qf)  # the tensor-core form ran
     assert rel_rmse(qt, qf) < TOEP_RMSE
     assert rel_rmse(qt, q_ref) < TOEP_RMSE
+
+
+@pytest.mark.parametrize("W,N", [(200, 300), (384, 200)])
+def test_toeplitz_many_tiles_per_cta(cuda, W, N):
+    """FP32 samples from N x 256 detector rows: hundreds of row tiles, four to
+    six per CTA, so both tensor-memory accumulators are reused (a tile's MMAs
+    wait for the epilogue of the tile two before) and both epilogue sets take
+    chunks of several tiles."""
+    import torch
+
+    g = small_geometry(W=W, N=N, H=256, vol=(16, 16, 8))
+    rng = np.random.default_rng(W + N)
+    sino = rng.normal(size=(g.H, g.N, g.W)).astype(np.float32)
+    d = to_dev(sino, torch)
+
+    def run():
+        q, _ = device.filter_projections(g, d, window=_lib.TK_WINDOW_HANN)
+        torch.cuda.synchronize()
+        return q.cpu().numpy()[:, :, :g.W]
+
+    qt = with_form(_lib.TK_FILTER_TOEPLITZ, run)
+    qf = with_form(_lib.TK_FILTER_FFT, run)
+    assert device.device_error_flags() == 0
+    assert not np.array_equal(qt, qf)
+    assert rel_rmse(qt, qf) < TOEP_RMSE
+    # every row, not only on average: the worst detector row stays within the bound
+    per_row = np.sqrt(np.mean((qt - qf) ** 2, axis=2) / np.maximum(np.mean(qf ** 2, axis=2), 1e-30))
+    assert float(per_row.max()) < 10 * TOEP_RMSE
+
+
+def test_toeplitz_many_tiles_u16_f16(cuda):
+    """Raw uint16 frames into FP16 coefficients at W = 512 (64-row tiles, four
+    or five per CTA): the uint16 producers and the coefficient epilogue over
+    reused accumulators, against the FFT form."""
+    import torch
+
+    g = small_geometry(W=512, N=160, H=256, vol=(16, 16, 8))
+    rng = np.random.default_rng(5)
+    raw = rng.integers(2000, 60000, size=(g.N, g.H, g.W)).astype(np.uint16)
+    d = torch.from_numpy(raw.view(np.int16)).cuda()
+    ff = device.flatfield(flat_value=60000.0)
+
+    def run():
+        q, s = device.filter_projections(g, d, _lib.TK_INPUT_U16, _lib.TK_LAYOUT_PROJECTION, ff=ff,
+                                         window=_lib.TK_WINDOW_HANN, precision=_lib.TK_F16)
+        torch.cuda.synchronize()
+        return q.cpu().numpy(), float(s.item())
+
+    (qt, st), (qf, sf) = with_form(_lib.TK_FILTER_TOEPLITZ, run), with_form(_lib.TK_FILTER_FFT, run)
+    assert st == sf
+    et, ef = decode_entries(qt, _lib.TK_F16, g), decode_entries(qf, _lib.TK_F16, g)
+    assert device.device_error_flags() == 0
+    assert not np.array_equal(et, ef)
+    rms = np.sqrt(np.mean(ef ** 2))
+    assert np.sqrt(np.mean((et - ef) ** 2)) < 4 * 2.0 ** -10 * rms
 
 
 def decode_entries(raw, precision, g):
