@@ -98,6 +98,37 @@ def test_batch_equals_per_volume(items, precision):
     b.close()
 
 
+def test_batch_many_units_per_cta(cuda):
+    """Three 192^2 x 130 volumes: two for the persistent kernel (432 units each
+    at the default tile shape, the last z chunk of each tile column ragged:
+    several units per persistent CTA, so every CTA's mbarrier ring runs on
+    across units of different items) and one with the quarter-turn symmetry
+    (N = 84, unflipped in x and y) beside it.  Bit for bit against
+    tk_fdk_device."""
+    import torch
+
+    geos = [small_geometry(W=256, N=90, H=200, vol=(192, 192, 130), voxel_mm=1.0),
+            small_geometry(W=256, N=96, H=200, vol=(192, 192, 130), voxel_mm=1.1, dirx=1, rot=0.2),
+            small_geometry(W=240, N=84, H=180, vol=(192, 192, 130), voxel_mm=0.9, dirz=1)]
+    b = Batch(_lib.TK_F16)
+    ins, vols = [], []
+    for k, g in enumerate(geos):
+        ins.append(device.phantom_project(g, head_phantom(g.fov_radius_cm * 0.85, seed=40 + k),
+                                          _lib.TK_LAYOUT_SINOGRAM))
+        vols.append(torch.full((g.Z, g.Y, g.X), float("nan"), device="cuda"))
+        b.submit(g, ins[-1], vols[-1], _lib.TK_INPUT_F32, _lib.TK_LAYOUT_SINOGRAM, None, _lib.TK_WINDOW_HANN)
+    b.plan()
+    assert b.quarter_turn_items() == [False, False, True]
+    b.run(graph=False)
+    torch.cuda.synchronize()
+    for g, x, v in zip(geos, ins, vols):
+        ref = device.fdk_device(g, x, _lib.TK_INPUT_F32, _lib.TK_LAYOUT_SINOGRAM, window=_lib.TK_WINDOW_HANN,
+                                precision=_lib.TK_F16)
+        np.testing.assert_array_equal(v.cpu().numpy(), ref.cpu().numpy())
+    assert device.device_error_flags() == 0
+    b.close()
+
+
 def test_graph_replay_equals_eager_and_rereads_inputs(items):
     import torch
 
