@@ -1271,6 +1271,10 @@ static const BPVariant kVariants[] = {
     TK_BP_CIMG_PK(TK_F16, "f16", 16, 16, 48, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 3, 2),
     TK_BP_CIMG(TK_F32_COEF, "f32c", 16, 16, 32, 2, 3),
+    // two-stage twins of the 16-bit general walks, taken where three staged boxes would leave
+    // room for one CTA per SM only (two_stage_twin)
+    TK_BP_CIMG_F(TK_F16, "f16", 16, 16, 64, 2, 2),
+    TK_BP_CIMG_F(TK_BF16, "bf16", 16, 16, 64, 2, 2),
 };
 
 static int g_variant_override = -1;  // index into kVariants, set by tk_bp_select_variant
@@ -1284,6 +1288,20 @@ static const BPVariant *pick_variant(int precision)
         return &kVariants[g_variant_override];
     for (const auto &v : kVariants)
         if (v.precision == precision) return &v;
+    return nullptr;
+}
+
+// The two-stage variant with v's walk, storage and tile shape (the same
+// arithmetic, so the same bits), or null.
+static const BPVariant *two_stage_twin(const BPVariant *v)
+{
+    const char *lt = std::strchr(v->name, '<');
+    const size_t np = lt ? (size_t)(lt - v->name) : std::strlen(v->name);
+    for (const auto &c : kVariants)
+        if (&c != v && c.precision == v->precision && c.coef == v->coef && !c.qcap && c.STAGES == 2 &&
+            c.TX == v->TX && c.TY == v->TY && c.TZ == v->TZ && std::strncmp(c.name, v->name, np) == 0 &&
+            c.name[np] == '<')
+            return &c;
     return nullptr;
 }
 
@@ -1401,6 +1419,17 @@ static int launch_bp_impl(const tk_geometry &g, const void *d_q, int precision, 
     const int align = v->coef ? (ES >= 16 ? 1 : 16 / ES) : 4;
     int BW, BH;
     if (int rc = bp_box_dims(g, nz, zoff, v->TX, v->TY, v->TZ, v->coef, align, &BW, &BH)) return rc;
+    // A 16-bit general walk whose three staged boxes would fit one CTA per SM only (large
+    // footprints: scale near 1.5 at high magnification) takes its two-stage twin, which keeps two.
+    if (v->coef && !quad && v->STAGES == 3 && g_variant_override < 0 && precision != TK_F32_COEF) {
+        int dev = 0, per_sm = 0;
+        TK_CUDA(cudaGetDevice(&dev));
+        TK_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+        const size_t box = (size_t)((BW * BH + 15) / 16 * 16) * ES;
+        const size_t fixed = (size_t)std::min(g.N, kMaxParamProj) * sizeof(int2) + 3 * sizeof(uint64_t) + 16;
+        if (3 * box + fixed + 1024 > (size_t)per_sm / 2)  // 1 KB reserved per CTA
+            if (const BPVariant *t = two_stage_twin(v)) v = t;
+    }
     BH = std::max(1, BH - g_diag_box_shrink);  // 0 unless a self-check test shrinks the staged box
     TK_CHECK(!v->coef || BW * ES / 4 <= 256, TK_ERR_UNSUPPORTED, "tile footprint of %d entries too wide", BW);
 
