@@ -68,8 +68,8 @@ def half_math_variant():
 # (one ncu pass on the 64-slice slab case, so the full-size launch is captured in one pass, nothing saved or
 # restored).  source_sha1 is the sha1 of tk_bp.cu + tk_bp_core.cuh at capture: a later source reports the
 # traffic as stale (null) instead of a frozen number.
-BP_TRAFFIC = {"kernel": "bp_quad<f16,16,8,16,2,cap6144,f32i,issue1,geo1>", "bytes_per_launch": 338.80e9 + 4.30e9,
-              "source_sha1": "01712d09548d50c29bf67ef3ba65425a5e756370",
+BP_TRAFFIC = {"kernel": "bp_quad<f16,16,8,16,2,cap6144,f32i,issue1,geo1>", "bytes_per_launch": 310.51e9 + 4.30e9,
+              "source_sha1": "a79e5ca07db27cf4acb4799b067280a168fc95b7",
               "capture": "ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum --clock-control none "
                          "-k regex:bp_quad -c 1 python bench.py --steps 1 --warmup 1 --no-e2e --no-rmse --no-extras"}
 
