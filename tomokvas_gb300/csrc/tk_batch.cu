@@ -8,7 +8,9 @@
 // tile units, larger items first.  A run filters each item (one launch per
 // item) and then backprojects all units with ONE persistent launch: CTAs
 // (as many as fit on the SMs) take units from a global counter, so small and
-// large volumes share the GPU without tails.  The mbarrier ring of a CTA
+// large volumes share the GPU without tails.  Items with the quarter-turn
+// symmetry instead get tk_fdk_device's quarter-turn launch, on their filter
+// stream beside the persistent kernel (same kernel and bits as per volume).  The mbarrier ring of a CTA
 // runs on across units (its phase follows the CTA's running projection
 // count).  tk_batch_run can capture the whole run once into a CUDA graph and
 // replay it.  tk_batch_autotune times every compiled tile shape of the
